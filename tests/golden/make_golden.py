@@ -1,0 +1,102 @@
+"""Generate the golden vectors in tests/golden/ from the reference FMD library.
+
+Run from the repository root in a container that has the reference sources:
+
+    make -f oracle/Makefile.ref REF=/root/reference
+    python tests/golden/make_golden.py
+
+The reference is compiled unmodified as a single-rank CPU library
+(oracle/_ref/libfmdref.so) and driven through its own fmd.h API with the
+cases of tests/cases.py; white-box dumps come from oracle/ref_probe.c.
+Outputs: tests/golden/<case>.npz and tests/golden/bin_<case>.npz.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from fmd_gb300 import api  # noqa: E402
+import cases  # noqa: E402
+
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libfmdref.so")
+
+
+def golden_case(lib, name, work):
+    case = cases.CASES[name]
+    md, st = cases.setup(lib, name, work)
+    grp, dt = case["run"][1], case["run"][2]
+    lib.fmd_dync_integrate(md, grp, 0.0, dt)
+    d0 = lib.dump(md)
+    nc, cellh, l, pbc = lib.grid(md)
+    rec = cases.Recorder(lib)
+    cases.run(lib, name, md, rec)
+    d1 = lib.dump(md)
+    out = dict(state_x=st["x"], state_v=st["v"], state_kind=st["kind"], state_group=st["group"],
+               nc=nc, cellh=cellh,
+               s0_cell=d0["cell"], s0_id=d0["id"], s0_x=d0["x"], s0_F=d0["F"], s0_vaream=d0["vaream"],
+               s0_pe=np.array(d0["pe"]),
+               s1_cell=d1["cell"], s1_id=d1["id"], s1_x=d1["x"], s1_v=d1["v"], s1_F=d1["F"],
+               s1_pe=np.array(d1["pe"]), thermo=np.array(rec.rows),
+               errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2),
+               time_iteration=np.array(lib.wb("time_iteration")(md) if lib.has("oref_time_iteration") else -1))
+    lib.fmd_free(md)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "N0", len(d0["id"]), "N1", len(d1["id"]), "PE0", d0["pe"], "rows", len(rec.rows),
+          "errors", rec.errors)
+
+
+def golden_binning(lib, name, work, rounds=4, seed=99):
+    """Displace atoms (some across cell and periodic faces) and let the
+    reference re-bin them; records the cell and in-cell order after each
+    round (src/misc.c:268-308, src/md-ghost.c:827-869)."""
+    case = cases.CASES[name]
+    md, st = cases.setup(lib, name, work)
+    lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+    nc, cellh, l, pbc = lib.grid(md)
+    rng = np.random.default_rng(seed)
+    recs = {}
+    d = lib.dump(md)
+    recs["r0_cell"], recs["r0_id"], recs["r0_x"] = d["cell"], d["id"], d["x"]
+    for r in range(1, rounds + 1):
+        x = d["x"].copy()
+        n = len(x)
+        disp = rng.standard_normal((n, 3)) * 0.2 * cellh
+        big = rng.random(n) < 0.15
+        disp[big] = rng.uniform(-0.97, 0.97, (big.sum(), 3)) * cellh
+        disp = np.clip(disp, -0.97 * cellh, 0.97 * cellh)
+        x += disp
+        recs["in%d_x" % r] = x
+        lib.set_state(md, x, None)
+        lib.wb("refresh")(md)
+        d = lib.dump(md)
+        recs["r%d_cell" % r], recs["r%d_id" % r], recs["r%d_x" % r] = d["cell"], d["id"], d["x"]
+        print("bin", name, "round", r, "N", len(d["id"]))
+    lib.fmd_free(md)
+    np.savez_compressed(os.path.join(HERE, "bin_" + name + ".npz"), nc=nc, cellh=cellh, rounds=rounds, **recs)
+
+
+def main():
+    lib = api.Lib(REF_LIB, prefix="oref_")
+    names = sys.argv[1:] or list(cases.CASES)
+    with tempfile.TemporaryDirectory() as work:
+        for name in names:
+            if name.startswith("bin_"):
+                golden_binning(lib, name[4:], work)
+            else:
+                golden_case(lib, name, work)
+        if not sys.argv[1:]:
+            golden_binning(lib, "lj", work)
+            golden_binning(lib, "morse_open", work)
+
+
+if __name__ == "__main__":
+    main()
