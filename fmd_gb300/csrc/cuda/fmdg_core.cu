@@ -1,0 +1,624 @@
+// Device engine: system lifetime, uploads/downloads, step orchestration.
+//
+// A system owns one CUDA stream.  fmdg_vv_steps captures one
+// velocity-Verlet step (refresh + forces + reductions, ~9 kernels) into a
+// CUDA graph on first use and replays it once per step, so the host issues
+// one graph launch per step and never waits inside the loop; it synchronises
+// only when the caller reads results (thermo, errors, atoms).
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+#include "fmdg_internal.cuh"
+
+static thread_local char g_errmsg[512] = "";
+
+int fmdg_fail(const char *where, cudaError_t e)
+{
+    snprintf(g_errmsg, sizeof g_errmsg, "%s: %s", where, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? FMDG_E_NOMEM : FMDG_E_CUDA;
+}
+
+int fmdg_set_error(const char *msg)
+{
+    snprintf(g_errmsg, sizeof g_errmsg, "%s", msg);
+    return FMDG_E_ARG;
+}
+
+extern "C" const char *fmdg_last_error(void) { return g_errmsg; }
+
+extern "C" int fmdg_device_count(int *count)
+{
+    FMDG_CK(cudaGetDeviceCount(count));
+    return FMDG_OK;
+}
+
+namespace {
+
+template <typename T>
+int dalloc(T **p, size_t n)
+{
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return fmdg_fail("cudaMalloc", e);
+    return FMDG_OK;
+}
+
+void dfree(void *p) { if (p) cudaFree(p); }
+
+void free_atoms(fmdg_sys_t *s)
+{
+    Geo &g = s->g;
+    for (int k = 0; k < 2; k++)
+    {
+        Side &S = g.side[k];
+        dfree(S.x); dfree(S.v); dfree(S.kind); dfree(S.group); dfree(S.atomid);
+        dfree(S.cell_of); dfree(S.cell_start);
+        memset(&S, 0, sizeof S);
+    }
+    dfree(g.F); dfree(g.vaream);
+    dfree(g.bdest); dfree(g.bpath); dfree(g.bslot); dfree(g.brank); dfree(g.bnewidx);
+    dfree(g.dep_count); dfree(g.arr_base); dfree(g.bucket); dfree(g.arr_slot);
+    dfree(g.partials);
+    g.F = g.vaream = nullptr;
+    g.bdest = g.bpath = g.bslot = g.brank = g.bnewidx = nullptr;
+    g.dep_count = g.arr_lower = g.arr_total = g.bucket_fill = g.arr_base = nullptr;
+    g.bucket = g.arr_slot = nullptr;
+    g.partials = nullptr;
+    g.cap = 0;
+    s->atoms = false;
+    if (s->graph_key_valid) { cudaGraphExecDestroy(s->graph); s->graph_key_valid = 0; }
+}
+
+void invalidate_graph(fmdg_sys_t *s)
+{
+    if (s->graph_key_valid) { cudaGraphExecDestroy(s->graph); s->graph_key_valid = 0; }
+}
+
+int read_dyn(fmdg_sys_t *s, Dyn *out)
+{
+    FMDG_CK(cudaMemcpyAsync(out, s->g.dyn, sizeof(Dyn), cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    return FMDG_OK;
+}
+
+__global__ void k_add_velocity(Geo g, int group, double dx, double dy, double dz)
+{
+    const Dyn *dyn = g.dyn;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    if (group >= 0 && S.group[i] != group) return;
+    S.v[i] += dx;
+    S.v[g.cap + i] += dy;
+    S.v[2 * g.cap + i] += dz;
+}
+
+__global__ void k_change_group(Geo g, int old_group, int new_group)
+{
+    const Dyn *dyn = g.dyn;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    if (old_group < 0 || S.group[i] == old_group) S.group[i] = new_group;
+}
+
+__global__ void k_flush(unsigned *buf, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        buf[i] = buf[i] * 1664525u + 1013904223u;
+}
+
+// Independent FMA chains: the issue-rate ceiling of the CUDA cores for T.
+template <typename T>
+__global__ void k_fma_peak(T *out, int iters, T a, T b)
+{
+    T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++)
+    {
+        x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+        x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+    const T r = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (r == (T)12345.678) out[0] = r;
+}
+
+} // namespace
+
+extern "C" int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops)
+{
+    void *buf = nullptr;
+    FMDG_CK(cudaMalloc(&buf, 64));
+    int dev = 0, sms = 0;
+    FMDG_CK(cudaGetDevice(&dev));
+    FMDG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256;
+    const int iters = fp64 ? 2048 : 16384;
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++)
+    {
+        FMDG_CK(cudaEventRecord(s->ev0, s->stream));
+        if (fp64) k_fma_peak<double><<<blocks, threads, 0, s->stream>>>((double *)buf, iters, 0.999999, 1e-7);
+        else k_fma_peak<float><<<blocks, threads, 0, s->stream>>>((float *)buf, iters, 0.999999f, 1e-7f);
+        FMDG_CK(cudaEventRecord(s->ev1, s->stream));
+        FMDG_CK(cudaEventSynchronize(s->ev1));
+        float ms;
+        FMDG_CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaFree(buf);
+    const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_create(fmdg_sys_t **out, int device)
+{
+    *out = nullptr;
+    FMDG_CK(cudaSetDevice(device));
+    fmdg_sys_t *s = (fmdg_sys_t *)calloc(1, sizeof(fmdg_sys_t));
+    if (!s) return FMDG_E_NOMEM;
+    s->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { free(s); return fmdg_fail("cudaStreamCreate", e); }
+    FMDG_CK(cudaEventCreate(&s->ev0));
+    FMDG_CK(cudaEventCreate(&s->ev1));
+    for (int k = 0; k < 5; k++) FMDG_CK(cudaEventCreate(&s->pev[k]));
+    int rc = dalloc(&s->g.dyn, 1);
+    if (rc) return rc;
+    rc = dalloc(&s->g.thermo, 1);
+    if (rc) return rc;
+    FMDG_CK(cudaMemset(s->g.dyn, 0, sizeof(Dyn)));
+    FMDG_CK(cudaMemset(s->g.thermo, 0, sizeof(fmdg_thermo_t)));
+    *out = s;
+    return FMDG_OK;
+}
+
+extern "C" void fmdg_destroy(fmdg_sys_t *s)
+{
+    if (!s) return;
+    cudaSetDevice(s->device);
+    cudaStreamSynchronize(s->stream);
+    free_atoms(s);
+    dfree((void *)s->g.pairs); dfree((void *)s->g.mass); dfree((void *)s->g.eam_elem);
+    dfree((void *)s->g.eF); dfree((void *)s->g.eFDD); dfree((void *)s->g.erho);
+    dfree((void *)s->g.erhoDD); dfree((void *)s->g.ephi); dfree((void *)s->g.ephiDD);
+    dfree(s->g.dyn); dfree(s->g.thermo);
+    dfree(s->l2buf);
+    cudaEventDestroy(s->ev0);
+    cudaEventDestroy(s->ev1);
+    for (int k = 0; k < 5; k++) cudaEventDestroy(s->pev[k]);
+    cudaStreamDestroy(s->stream);
+    free(s);
+}
+
+extern "C" int fmdg_set_box(fmdg_sys_t *s, const double l[3], const int pbc[3], const int nc[3], const double cellh[3])
+{
+    for (int d = 0; d < 3; d++)
+        if (nc[d] < 1 || !(l[d] > 0.0) || !(cellh[d] > 0.0)) return fmdg_set_error("fmdg_set_box: bad geometry");
+    if (s->atoms) free_atoms(s);
+    for (int d = 0; d < 3; d++)
+    {
+        s->g.l[d] = l[d];
+        s->g.pbc[d] = pbc[d] ? 1 : 0;
+        s->g.nc[d] = nc[d];
+        s->g.cellh[d] = cellh[d];
+    }
+    const long long ncell = (long long)nc[0] * nc[1] * nc[2];
+    if (ncell > (1 << 24)) return fmdg_set_error("fmdg_set_box: more than 2^24 cells");
+    s->g.ncell = (int)ncell;
+    s->box_set = true;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, const int *eam_elem)
+{
+    if (nkinds < 1 || nkinds > FMDG_MAXK) return fmdg_set_error("fmdg_set_kinds: 1..8 kinds supported");
+    s->nkinds = nkinds;
+    s->g.nkinds = nkinds;
+    for (int k = 0; k < nkinds; k++)
+    {
+        s->h_mass[k] = mass[k];
+        s->h_eam_elem[k] = eam_elem ? eam_elem[k] : -1;
+    }
+    if (!s->g.mass)
+    {
+        int rc = dalloc((double **)&s->g.mass, FMDG_MAXK);
+        if (rc) return rc;
+        rc = dalloc((int **)&s->g.eam_elem, FMDG_MAXK);
+        if (rc) return rc;
+        rc = dalloc((fmdg_pair_t **)&s->g.pairs, FMDG_MAXK * FMDG_MAXK);
+        if (rc) return rc;
+    }
+    FMDG_CK(cudaMemcpy((void *)s->g.mass, s->h_mass, sizeof(double) * nkinds, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)s->g.eam_elem, s->h_eam_elem, sizeof(int) * nkinds, cudaMemcpyHostToDevice));
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table)
+{
+    if (s->nkinds < 1) return fmdg_set_error("fmdg_set_pairs: set kinds first");
+    const int nk2 = s->nkinds * s->nkinds;
+    s->cats = 0;
+    for (int k = 0; k < nk2; k++)
+    {
+        s->h_pairs[k] = table[k];
+        const int c = table[k].cat;
+        if (c != FMDG_POT_LJ && c != FMDG_POT_MORSE && c != FMDG_POT_EAM)
+            return fmdg_set_error("fmdg_set_pairs: every kind pair needs a potential");
+        s->cats |= 1 << c;
+    }
+    FMDG_CK(cudaMemcpy((void *)s->g.pairs, s->h_pairs, sizeof(fmdg_pair_t) * nk2, cudaMemcpyHostToDevice));
+    s->g.has_eam = (s->cats >> FMDG_POT_EAM) & 1;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int Nr2, double dr2,
+                            const double *F, const double *F_DD, const double *rho, const double *rhoDD,
+                            const double *phi, const double *phiDD)
+{
+    if (nelem < 1 || nelem > FMDG_MAXE || Nrho < 3 || Nr2 < 3) return fmdg_set_error("fmdg_set_eam: bad sizes");
+    Geo &g = s->g;
+    dfree((void *)g.eF); dfree((void *)g.eFDD); dfree((void *)g.erho);
+    dfree((void *)g.erhoDD); dfree((void *)g.ephi); dfree((void *)g.ephiDD);
+    const size_t nF = (size_t)nelem * Nrho, nR = (size_t)nelem * Nr2, nP = (size_t)nelem * nelem * Nr2;
+    int rc;
+    if ((rc = dalloc((double **)&g.eF, nF)) || (rc = dalloc((double **)&g.eFDD, nF)) ||
+        (rc = dalloc((double **)&g.erho, nR)) || (rc = dalloc((double **)&g.erhoDD, nR)) ||
+        (rc = dalloc((double **)&g.ephi, nP)) || (rc = dalloc((double **)&g.ephiDD, nP)))
+        return rc;
+    FMDG_CK(cudaMemcpy((void *)g.eF, F, nF * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)g.eFDD, F_DD, nF * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)g.erho, rho, nR * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)g.erhoDD, rhoDD, nR * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)g.ephi, phi, nP * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)g.ephiDD, phiDD, nP * 8, cudaMemcpyHostToDevice));
+    g.nelem = nelem; g.Nrho = Nrho; g.Nr2 = Nr2; g.drho = drho; g.dr2 = dr2;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_precision(fmdg_sys_t *s, int mode)
+{
+    if (mode != FMDG_PREC_FP64 && mode != FMDG_PREC_MIXED) return fmdg_set_error("fmdg_set_precision: bad mode");
+    s->g.prec = mode;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const double *x, const double *v,
+                           const unsigned *kind, const int *group, const unsigned *atomid)
+{
+    if (!s->box_set) return fmdg_set_error("fmdg_upload: set the box first");
+    if (n < 0) return fmdg_set_error("fmdg_upload: negative atom count");
+    Geo &g = s->g;
+    const int ncell = g.ncell;
+    std::vector<int> start(ncell + 1), cell_of(n > 0 ? n : 1);
+    long long acc = 0;
+    for (int c = 0; c < ncell; c++)
+    {
+        start[c] = (int)acc;
+        for (int k = 0; k < cell_count[c]; k++) cell_of[acc + k] = c;
+        acc += cell_count[c];
+    }
+    start[ncell] = (int)acc;
+    if (acc != n) return fmdg_set_error("fmdg_upload: cell counts do not add up to n");
+    for (int i = 0; i < n; i++)
+        if (kind[i] >= (unsigned)(s->nkinds > 0 ? s->nkinds : FMDG_MAXK))
+            return fmdg_set_error("fmdg_upload: atom kind out of range");
+    free_atoms(s);
+    const int cap = n > 0 ? n : 1;
+    g.cap = cap;
+    int rc;
+    for (int k = 0; k < 2; k++)
+    {
+        Side &S = g.side[k];
+        if ((rc = dalloc(&S.x, 3 * (size_t)cap)) || (rc = dalloc(&S.v, 3 * (size_t)cap)) ||
+            (rc = dalloc(&S.kind, cap)) || (rc = dalloc(&S.group, cap)) || (rc = dalloc(&S.atomid, cap)) ||
+            (rc = dalloc(&S.cell_of, cap)) || (rc = dalloc(&S.cell_start, (size_t)ncell + 1)))
+            return rc;
+    }
+    if ((rc = dalloc(&g.F, 3 * (size_t)cap)) || (rc = dalloc(&g.vaream, cap)) ||
+        (rc = dalloc(&g.bdest, cap)) || (rc = dalloc(&g.bpath, cap)) || (rc = dalloc(&g.bslot, cap)) ||
+        (rc = dalloc(&g.brank, cap)) || (rc = dalloc(&g.bnewidx, cap)) ||
+        (rc = dalloc(&g.dep_count, 4 * (size_t)ncell)) || (rc = dalloc(&g.arr_base, (size_t)ncell + 1)) ||
+        (rc = dalloc(&g.bucket, cap)) || (rc = dalloc(&g.arr_slot, cap)))
+        return rc;
+    g.arr_lower = g.dep_count + ncell;
+    g.arr_total = g.dep_count + 2 * ncell;
+    g.bucket_fill = g.dep_count + 3 * ncell;
+    const int nb = fmdg_grid(cap, 128);
+    if ((rc = dalloc(&g.partials, (size_t)nb * 9 + 8))) return rc;
+    // host SoA staging
+    std::vector<double> hx(3 * (size_t)cap, 0.0), hv(3 * (size_t)cap, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++)
+        {
+            hx[(size_t)d * cap + i] = x[3 * (size_t)i + d];
+            hv[(size_t)d * cap + i] = v[3 * (size_t)i + d];
+        }
+    Side &S = g.side[0];
+    FMDG_CK(cudaMemcpy(S.x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy(S.v, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice));
+    if (n > 0)
+    {
+        FMDG_CK(cudaMemcpy(S.kind, kind, (size_t)n * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(S.group, group, (size_t)n * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(S.atomid, atomid, (size_t)n * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(S.cell_of, cell_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+    }
+    FMDG_CK(cudaMemcpy(S.cell_start, start.data(), ((size_t)ncell + 1) * 4, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemset(g.F, 0, 3 * (size_t)cap * 8));
+    FMDG_CK(cudaMemset(g.vaream, 0, (size_t)cap * 8));
+    Dyn d;
+    memset(&d, 0, sizeof d);
+    d.cur = 0;
+    d.n = n;
+    d.lambda = 1.0;
+    FMDG_CK(cudaMemcpy(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));
+    s->atoms = true;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_natoms(fmdg_sys_t *s, int *n)
+{
+    if (!s->atoms) { *n = 0; return FMDG_OK; }
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    *n = d.n;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_download(fmdg_sys_t *s, int *cell_of, double *x, double *v, double *F, double *vaream,
+                             unsigned *kind, int *group, unsigned *atomid)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    const Geo &g = s->g;
+    const Side &S = g.side[d.cur];
+    const int n = d.n, cap = g.cap;
+    std::vector<double> buf(3 * (size_t)cap);
+    auto get3 = [&](const double *src, double *dst) -> int {
+        FMDG_CK(cudaMemcpy(buf.data(), src, 3 * (size_t)cap * 8, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) dst[3 * (size_t)i + k] = buf[(size_t)k * cap + i];
+        return FMDG_OK;
+    };
+    if (x && (rc = get3(S.x, x))) return rc;
+    if (v && (rc = get3(S.v, v))) return rc;
+    if (F && (rc = get3(g.F, F))) return rc;
+    if (n > 0)
+    {
+        if (vaream) FMDG_CK(cudaMemcpy(vaream, g.vaream, (size_t)n * 8, cudaMemcpyDeviceToHost));
+        if (kind) FMDG_CK(cudaMemcpy(kind, S.kind, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        if (group) FMDG_CK(cudaMemcpy(group, S.group, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        if (atomid) FMDG_CK(cudaMemcpy(atomid, S.atomid, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        if (cell_of) FMDG_CK(cudaMemcpy(cell_of, S.cell_of, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    }
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_state(fmdg_sys_t *s, const double *x, const double *v)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    const Side &S = s->g.side[d.cur];
+    const int n = d.n, cap = s->g.cap;
+    std::vector<double> buf(3 * (size_t)cap, 0.0);
+    auto put3 = [&](const double *src, double *dst) -> int {
+        FMDG_CK(cudaMemcpy(buf.data(), dst, 3 * (size_t)cap * 8, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) buf[(size_t)k * cap + i] = src[3 * (size_t)i + k];
+        FMDG_CK(cudaMemcpy(dst, buf.data(), 3 * (size_t)cap * 8, cudaMemcpyHostToDevice));
+        return FMDG_OK;
+    };
+    if (x && (rc = put3(x, S.x))) return rc;
+    if (v && (rc = put3(v, S.v))) return rc;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_refresh(fmdg_sys_t *s)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    return fmdg_launch_refresh(s, FMDG_REFRESH_ONLY, 0.0, -1, 0);
+}
+
+extern "C" int fmdg_compute_forces(fmdg_sys_t *s, int active_group)
+{
+    if (!s->atoms || !s->cats) return FMDG_E_STATE;
+    int rc = fmdg_launch_forces(s, active_group, 0, 0.0);
+    if (rc) return rc;
+    return fmdg_launch_reduce(s, 0, 0.0, 1.0, 0.0);
+}
+
+extern "C" int fmdg_thermo(fmdg_sys_t *s, int active_group, fmdg_thermo_t *out)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    int rc = fmdg_launch_thermo(s, active_group, 0, 0.0, 1.0, 0.0);
+    if (rc) return rc;
+    return out ? fmdg_get_thermo(s, out) : FMDG_OK;
+}
+
+static int vv_step_launches(fmdg_sys_t *s, double dt, int group, int thermostat, double tau, double T0)
+{
+    int rc = fmdg_launch_refresh(s, FMDG_REFRESH_VV, dt, group, thermostat);
+    if (rc) return rc;
+    rc = fmdg_launch_forces(s, group, 1, dt);
+    if (rc) return rc;
+    return fmdg_launch_reduce(s, thermostat, dt, tau, T0);
+}
+
+// Before the first step of a run the caller computes the forces of the
+// current positions (fmdg_compute_forces) and, with a thermostat, sets the
+// scale from the current temperature (fmdg_prepare_thermostat); each step
+// then leaves the next step's scale on the device.
+extern "C" int fmdg_prepare_thermostat(fmdg_sys_t *s, int group, double dt, double tau, double T0)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    return fmdg_launch_thermo(s, group, 1, dt, tau, T0);
+}
+
+extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_group,
+                             int thermostat, double tau, double T0)
+{
+    if (!s->atoms || !s->cats) return FMDG_E_STATE;
+    if (nsteps <= 0) return FMDG_OK;
+    if (s->profiling)
+    {
+        // phases timed separately with events: 0 refresh, 1 density, 2 force, 3 reduce
+        for (int k = 0; k < nsteps; k++)
+        {
+            FMDG_CK(cudaEventRecord(s->pev[0], s->stream));
+            int rc = fmdg_launch_refresh(s, FMDG_REFRESH_VV, dt, active_group, thermostat);
+            if (rc) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[1], s->stream));
+            if ((rc = fmdg_launch_density(s, active_group))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[2], s->stream));
+            if ((rc = fmdg_launch_pair_forces(s, active_group, 1, dt))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[3], s->stream));
+            if ((rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[4], s->stream));
+            FMDG_CK(cudaEventSynchronize(s->pev[4]));
+            for (int ph = 0; ph < 4; ph++)
+            {
+                float ms = 0.0f;
+                FMDG_CK(cudaEventElapsedTime(&ms, s->pev[ph], s->pev[ph + 1]));
+                s->prof_ms[ph] += ms;
+                s->prof_n[ph] += 1;
+            }
+        }
+        return FMDG_OK;
+    }
+    const bool same = s->graph_key_valid && s->graph_dt == dt && s->graph_group == active_group &&
+                      s->graph_thermo == thermostat && s->graph_tau == tau && s->graph_T0 == T0;
+    if (!same)
+    {
+        invalidate_graph(s);
+        cudaGraph_t graph;
+        FMDG_CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = s->launches;
+        int rc = vv_step_launches(s, dt, active_group, thermostat, tau, T0);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fmdg_fail("cudaStreamEndCapture", e);
+        s->launches = before;
+        e = cudaGraphInstantiate(&s->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fmdg_fail("cudaGraphInstantiate", e);
+        s->graph_key_valid = 1;
+        s->graph_dt = dt; s->graph_group = active_group; s->graph_thermo = thermostat;
+        s->graph_tau = tau; s->graph_T0 = T0;
+        // kernels per captured step
+        const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
+        s->graph_steps = 7 + 1 + (eam ? 1 : 0) + 1;
+    }
+    for (int k = 0; k < nsteps; k++) FMDG_CK(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += (long long)nsteps * (s->graph_steps - 1);  // memset node is not a kernel
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_get_thermo(fmdg_sys_t *s, fmdg_thermo_t *out)
+{
+    FMDG_CK(cudaMemcpyAsync(out, s->g.thermo, sizeof(fmdg_thermo_t), cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_get_errors(fmdg_sys_t *s, unsigned *bits, int clear)
+{
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    *bits = d.err;
+    if (clear && d.err)
+    {
+        unsigned z = 0;
+        FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, err), &z, sizeof z, cudaMemcpyHostToDevice));
+    }
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_add_velocity(fmdg_sys_t *s, int group, const double dv[3])
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    k_add_velocity<<<fmdg_grid(s->g.cap, 256), 256, 0, s->stream>>>(s->g, group, dv[0], dv[1], dv[2]);
+    s->launches++;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_change_group(fmdg_sys_t *s, int old_group, int new_group)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    k_change_group<<<fmdg_grid(s->g.cap, 256), 256, 0, s->stream>>>(s->g, old_group, new_group);
+    s->launches++;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_sync(fmdg_sys_t *s)
+{
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_timer_start(fmdg_sys_t *s)
+{
+    FMDG_CK(cudaEventRecord(s->ev0, s->stream));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_timer_stop(fmdg_sys_t *s, float *ms)
+{
+    FMDG_CK(cudaEventRecord(s->ev1, s->stream));
+    FMDG_CK(cudaEventSynchronize(s->ev1));
+    FMDG_CK(cudaEventElapsedTime(ms, s->ev0, s->ev1));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_profiling(fmdg_sys_t *s, int on)
+{
+    s->profiling = on != 0;
+    memset(s->prof_ms, 0, sizeof s->prof_ms);
+    memset(s->prof_n, 0, sizeof s->prof_n);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches)
+{
+    static const char *names[4] = {"bin", "density", "force", "reduce"};
+    for (int k = 0; k < 4; k++)
+        if (strcmp(name, names[k]) == 0)
+        {
+            *ms = s->prof_ms[k];
+            *launches = s->prof_n[k];
+            return FMDG_OK;
+        }
+    return fmdg_set_error("fmdg_get_profile: unknown phase");
+}
+
+extern "C" int fmdg_launch_count(fmdg_sys_t *s, long long *count)
+{
+    *count = s->launches;
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_flush_l2(fmdg_sys_t *s)
+{
+    if (!s->l2buf)
+    {
+        s->l2bytes = (size_t)256 << 20;
+        FMDG_CK(cudaMalloc(&s->l2buf, s->l2bytes));
+        FMDG_CK(cudaMemset(s->l2buf, 0, s->l2bytes));
+    }
+    k_flush<<<1216, 256, 0, s->stream>>>((unsigned *)s->l2buf, s->l2bytes / 4);
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}

@@ -1,0 +1,134 @@
+// Internal definitions shared by the device-engine translation units.
+//
+// HBM layout of one system (capacity `cap` atoms, `ncell` interior cells):
+//   two ping-pong sides, each holding the atoms sorted by cell:
+//     x[3*cap], v[3*cap]   binary64, structure of arrays (x[d*cap + i])
+//     kind[cap], group[cap], atomid[cap], cell_of[cap], cell_start[ncell+1]
+//   F[3*cap], vaream[cap]  (forces; EAM density, then F'(rho)) in the
+//                          current order only: they are recomputed after
+//                          every refresh, never permuted
+//   binning scratch (per atom / per cell), reduction partials, thermo record.
+// Dynamic scalars that change on the device (current side, atom count,
+// simulation time) live in `Dyn` in device memory so the whole step can be
+// captured once as a CUDA graph and replayed.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "fmdg.h"
+
+#define FMDG_MAXK 8            // atom kinds per system
+#define FMDG_MAXE 4            // EAM elements per system
+
+#define K_BOLTZMANN_D 8.6173303e-5
+
+struct Dyn
+{
+    int cur;            // current ping-pong side
+    int n;              // live atoms
+    int n_next;         // atom count after the refresh in flight
+    int any_move;       // a refresh moved at least one atom
+    unsigned err;       // sticky error bits (FMDG_ERRBIT_*)
+    int pad;
+    double lambda;      // Berendsen scale for the next start step
+    double time;
+};
+
+struct Side
+{
+    double *x, *v;
+    unsigned *kind;
+    int *group;
+    unsigned *atomid;
+    int *cell_of;
+    int *cell_start;
+};
+
+struct Geo   // passed by value to kernels
+{
+    int cap, ncell;
+    int nc[3];
+    int pbc[3];
+    double l[3], cellh[3];
+    Side side[2];
+    double *F, *vaream;
+    // binning scratch
+    int *bdest;        // destination interior cell, -1 deleted, -2 stays
+    int *bpath;        // migration key bits
+    int *bslot;        // final slot of a stayer inside its cell
+    int *brank;        // departure rank inside the source cell
+    int *bnewidx;      // new index of an arriving atom
+    int *dep_count, *arr_lower, *arr_total, *bucket_fill;   // per cell
+    int *arr_base;     // per cell + 1, exclusive scan of arr_total
+    int *new_start;    // alias of the next side's cell_start
+    int *bucket, *arr_slot;   // per arrival
+    // potentials
+    int nkinds;
+    const fmdg_pair_t *pairs;     // nkinds*nkinds, device copy
+    const double *mass;           // nkinds
+    const int *eam_elem;          // nkinds
+    int nelem, Nrho, Nr2;
+    double drho, dr2;
+    const double *eF, *eFDD, *erho, *erhoDD, *ephi, *ephiDD;
+    int has_eam;
+    int prec;
+    // reductions
+    double *partials;             // per block: 8 doubles
+    fmdg_thermo_t *thermo;
+    Dyn *dyn;
+};
+
+struct fmdg_sys
+{
+    int device;
+    cudaStream_t stream;
+    Geo g;
+    Geo *d_geo;
+    bool box_set, atoms;
+    int nkinds;
+    fmdg_pair_t h_pairs[FMDG_MAXK * FMDG_MAXK];
+    double h_mass[FMDG_MAXK];
+    int h_eam_elem[FMDG_MAXK];
+    int cats;                     // bit mask of pair categories present
+    cudaEvent_t ev0, ev1;
+    cudaEvent_t pev[5];
+    bool profiling;
+    float prof_ms[4];
+    int prof_n[4];
+    long long launches;
+    // captured multi-step graph
+    cudaGraphExec_t graph;
+    int graph_key_valid;
+    double graph_dt, graph_tau, graph_T0;
+    int graph_group, graph_thermo, graph_steps;
+    void *l2buf;
+    size_t l2bytes;
+};
+
+// ---- helpers shared by the translation units --------------------------------
+int fmdg_fail(const char *where, cudaError_t e);
+int fmdg_set_error(const char *msg);
+
+#define FMDG_CK(call)                                                    \
+    do {                                                                 \
+        cudaError_t e_ = (call);                                         \
+        if (e_ != cudaSuccess) return fmdg_fail(#call, e_);              \
+    } while (0)
+
+// kernel launch wrappers (defined in their translation units)
+int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int thermostat);
+int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt);
+int fmdg_launch_density(fmdg_sys_t *s, int group);
+int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt);
+int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0);
+int fmdg_force_blocks(const fmdg_sys_t *s);
+int fmdg_launch_reduce(fmdg_sys_t *s, int thermostat, double dt, double tau, double T0);
+
+// refresh modes
+#define FMDG_REFRESH_ONLY  0     // positions already updated
+#define FMDG_REFRESH_VV    1     // velocity-Verlet start step first
+#define FMDG_REFRESH_SE    2     // symplectic Euler kick-drift first
+
+static inline int fmdg_grid(int n, int b) { return (n + b - 1) / b; }
+
+__device__ __forceinline__ void atomic_or_err(Dyn *d, unsigned bit) { atomicOr(&d->err, bit); }

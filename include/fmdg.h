@@ -1,0 +1,160 @@
+/*
+ * fmdg.h -- C-ABI of the GB300 device engine behind libfmd.so.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes
+ * (0 = success, see FMDG_E_*).  The host side of libfmd.so (the fmd.h
+ * implementation, written in C) calls these entry points; the Python test
+ * and benchmark harness calls them through ctypes for kernel-level parity
+ * checks.  Each entry point names the reference routine (FMD 0.4.0, path
+ * within its project) whose per-timestep work it replaces.
+ *
+ * Data model: one device system (fmdg_sys_t) holds the whole periodic box of
+ * one FMD instance in HBM as structure-of-arrays, sorted by interior cell in
+ * the reference's cell order (flat index z + nz*(y + ny*x), src/general.h:56)
+ * and, inside each cell, in the reference's in-cell order.  All arithmetic on
+ * positions, velocities, forces and energies is IEEE binary64 in the drop-in
+ * precision mode.
+ */
+#ifndef FMDG_H
+#define FMDG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FMDG_OK              0
+#define FMDG_E_CUDA          1   /* a CUDA runtime call failed (message: fmdg_last_error) */
+#define FMDG_E_ARG           2   /* invalid argument */
+#define FMDG_E_NOMEM         3   /* device allocation failed */
+#define FMDG_E_STATE         4   /* call made in the wrong state (e.g. no atoms) */
+
+/* sticky device error bits, read with fmdg_get_errors (mirror the reference's
+   error events raised from the per-step code) */
+#define FMDG_ERRBIT_POSITION   0x1  /* atom left the local grid: src/misc.c:286-290 */
+#define FMDG_ERRBIT_RHO_RANGE  0x2  /* EAM density beyond the F(rho) table: src/eam.c:168-171 */
+#define FMDG_ERRBIT_TTM        0x4  /* TTM turi-cell index outside the grid */
+#define FMDG_ERRBIT_INTERNAL   0x8  /* an internal index check failed (the access was skipped) */
+
+/* pair categories: values of the reference's potcat_t (src/potential.h:26-32) */
+#define FMDG_POT_NONE  0
+#define FMDG_POT_LJ    1
+#define FMDG_POT_EAM   2
+#define FMDG_POT_MORSE 3
+
+/* precision modes */
+#define FMDG_PREC_FP64   0   /* drop-in: all pair arithmetic in binary64 */
+#define FMDG_PREC_MIXED  1   /* pair/spline/embedding in binary32, sums in binary64 */
+
+typedef struct fmdg_sys fmdg_sys_t;
+
+/* One entry of the kinds x kinds pair table (src/potential.h:40-45).
+   LJ    (src/lj.h:60-67):    p = {eps4, sig_sqr, cutoff_sqr, 0}
+   Morse (src/morse.h:60-66): p = {D0, alpha, r0, cutoff_sqr}
+   EAM   (src/eam.h:424-430): p = {0, 0, cutoff_sqr, 0}, iloc/jloc = element
+                              indexes of the two kinds inside the EAM tables */
+typedef struct
+{
+    int cat;
+    int iloc, jloc;
+    int pad;
+    double p[4];
+} fmdg_pair_t;
+
+/* Thermodynamic reductions of the active group (src/integrators.c:78-92,
+   src/matter.c:31-68) plus the last potential energy (src/lj.c:89). */
+typedef struct
+{
+    double kinetic;        /* 0.5 * sum m v^2                        */
+    double temperature;    /* sum m v^2 / (3 N k_B)                  */
+    double momentum[3];    /* sum m v (internal units)               */
+    double potential;      /* pair + embedding energy                */
+    double count;          /* atoms in the active group              */
+    double pad;
+} fmdg_thermo_t;
+
+/* --- lifetime -------------------------------------------------------- */
+int  fmdg_create(fmdg_sys_t **out, int device);
+void fmdg_destroy(fmdg_sys_t *s);
+const char *fmdg_last_error(void);
+int  fmdg_device_count(int *count);
+
+/* --- set-up (replaces the single-rank parts of src/subdomain.c:224-305,
+       src/misc.c:41-62 and the potential tables of src/potential.c) ---- */
+/* box length, periodicity and cell grid: nc[d] = (int)(l[d]/rc_max),
+   cellh[d] = l[d]/nc[d] (src/misc.c:41-50) */
+int fmdg_set_box(fmdg_sys_t *s, const double l[3], const int pbc[3], const int nc[3], const double cellh[3]);
+/* masses in internal units (src/potential.c:47); eam_elem[k] = element
+   index of kind k inside the EAM tables or -1 */
+int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, const int *eam_elem);
+int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table /* nkinds*nkinds */);
+/* EAM tables on the r^2 grid (src/eam.c:376-555): F, F_DD [nelem*Nrho];
+   rho, rhoDD [nelem*Nr2]; phi, phiDD [nelem*nelem*Nr2] (symmetric) */
+int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int Nr2, double dr2,
+                 const double *F, const double *F_DD, const double *rho, const double *rhoDD,
+                 const double *phi, const double *phiDD);
+int fmdg_set_precision(fmdg_sys_t *s, int mode);
+
+/* --- atoms (replaces the distribution of the global grid to the local grid,
+       src/matter.c:329-447, and the state gathers of src/misc.c:310-422) -- */
+/* n atoms in cell order: cell_count[c] atoms of cell c, in in-cell order;
+   x, v: n*3 interleaved (x0 y0 z0 x1 ...) */
+int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const double *x, const double *v,
+                const unsigned *kind, const int *group, const unsigned *atomid);
+int fmdg_natoms(fmdg_sys_t *s, int *n);
+/* any output pointer may be NULL; arrays are in cell order */
+int fmdg_download(fmdg_sys_t *s, int *cell_of, double *x, double *v, double *F, double *vaream,
+                  unsigned *kind, int *group, unsigned *atomid);
+/* overwrite positions and/or velocities (cell order, n*3 interleaved) */
+int fmdg_set_state(fmdg_sys_t *s, const double *x, const double *v);
+
+/* --- per-timestep work ---------------------------------------------- */
+/* cell-list refresh with the reference's cell assignment and in-cell order
+   (src/misc.c:268-308 + src/md-ghost.c:827-869) */
+int fmdg_refresh(fmdg_sys_t *s);
+/* force field evaluation: src/forces.c:332-382 (LJ src/lj.c:28-90, Morse
+   src/morse.c:30-92, EAM src/eam.c:29-322, hybrid src/forces.c:33-290) */
+int fmdg_compute_forces(fmdg_sys_t *s, int active_group);
+/* group thermodynamics from current velocities (src/matter.c:31-68) */
+int fmdg_thermo(fmdg_sys_t *s, int active_group, fmdg_thermo_t *out);
+/* velocity-Verlet steps (src/integrators.c:40-126,227-264): startStep with
+   optional Berendsen scaling (lambda from the previous step's temperature),
+   refresh, forces, finishStep.  thermostat=0: tau, T0 ignored. */
+int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_group,
+                  int thermostat, double tau, double T0);
+/* Berendsen scale of the first step of a run from the current velocities
+   (src/integrators.c:44-47 when the kinetic energy is not up to date) */
+int fmdg_prepare_thermostat(fmdg_sys_t *s, int active_group, double dt, double tau, double T0);
+/* last thermodynamic record (device->host copy; synchronises) */
+int fmdg_get_thermo(fmdg_sys_t *s, fmdg_thermo_t *out);
+/* sticky error bits since the last clear; clear=1 resets them */
+int fmdg_get_errors(fmdg_sys_t *s, unsigned *bits, int clear);
+
+/* --- whole-system edits after distribution -------------------------- */
+int fmdg_add_velocity(fmdg_sys_t *s, int group, const double dv[3]);
+int fmdg_change_group(fmdg_sys_t *s, int old_group, int new_group);
+
+/* --- timing (CUDA events on the system's stream) --------------------- */
+int fmdg_sync(fmdg_sys_t *s);
+int fmdg_timer_start(fmdg_sys_t *s);
+int fmdg_timer_stop(fmdg_sys_t *s, float *ms);
+/* with profiling on, fmdg_vv_steps launches each phase between CUDA events
+   (no graph) and accumulates its device time: phases "bin" (start step +
+   refresh), "density" (EAM pass 1 + embedding), "force" (pair forces +
+   finish step), "reduce" (thermo record); ms summed over steps */
+int fmdg_set_profiling(fmdg_sys_t *s, int on);
+int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches);
+int fmdg_launch_count(fmdg_sys_t *s, long long *count);
+/* issue-rate ceiling of the CUDA cores: independent FMA chains over all
+   SMs, 2 flops per FMA (fp64=1: binary64, else binary32) */
+int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops);
+/* write a buffer larger than L2 so the next kernel starts cold */
+int fmdg_flush_l2(fmdg_sys_t *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FMDG_H */
