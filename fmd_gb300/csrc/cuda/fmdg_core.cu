@@ -6,6 +6,7 @@
 // one graph launch per step and never waits inside the loop; it synchronises
 // only when the caller reads results (thermo, errors, atoms).
 #include <stdio.h>
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 #include <vector>
@@ -57,6 +58,8 @@ void free_atoms(fmdg_sys_t *s)
         memset(&S, 0, sizeof S);
     }
     dfree(g.F); dfree(g.vaream);
+    dfree(g.xf4); dfree(g.nbr); dfree(g.nbr_count);
+    g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr;
     dfree(g.bdest); dfree(g.bpath); dfree(g.bslot); dfree(g.brank); dfree(g.bnewidx);
     dfree(g.dep_count); dfree(g.arr_base); dfree(g.bucket); dfree(g.arr_slot);
     dfree(g.partials);
@@ -163,7 +166,7 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     if (e != cudaSuccess) { free(s); return fmdg_fail("cudaStreamCreate", e); }
     FMDG_CK(cudaEventCreate(&s->ev0));
     FMDG_CK(cudaEventCreate(&s->ev1));
-    for (int k = 0; k < 5; k++) FMDG_CK(cudaEventCreate(&s->pev[k]));
+    for (int k = 0; k < 6; k++) FMDG_CK(cudaEventCreate(&s->pev[k]));
     int rc = dalloc(&s->g.dyn, 1);
     if (rc) return rc;
     rc = dalloc(&s->g.thermo, 1);
@@ -183,11 +186,13 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     dfree((void *)s->g.pairs); dfree((void *)s->g.mass); dfree((void *)s->g.eam_elem);
     dfree((void *)s->g.eF); dfree((void *)s->g.eFDD); dfree((void *)s->g.erho);
     dfree((void *)s->g.erhoDD); dfree((void *)s->g.ephi); dfree((void *)s->g.ephiDD);
+    dfree((void *)s->g.pk_rho); dfree((void *)s->g.pk_phi); dfree((void *)s->g.pk_F);
+    dfree((void *)s->g.pkf_rho); dfree((void *)s->g.pkf_phi); dfree((void *)s->g.pkf_F);
     dfree(s->g.dyn); dfree(s->g.thermo);
     dfree(s->l2buf);
     cudaEventDestroy(s->ev0);
     cudaEventDestroy(s->ev1);
-    for (int k = 0; k < 5; k++) cudaEventDestroy(s->pev[k]);
+    for (int k = 0; k < 6; k++) cudaEventDestroy(s->pev[k]);
     cudaStreamDestroy(s->stream);
     free(s);
 }
@@ -276,6 +281,33 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     FMDG_CK(cudaMemcpy((void *)g.ephi, phi, nP * 8, cudaMemcpyHostToDevice));
     FMDG_CK(cudaMemcpy((void *)g.ephiDD, phiDD, nP * 8, cudaMemcpyHostToDevice));
     g.nelem = nelem; g.Nrho = Nrho; g.Nr2 = Nr2; g.drho = drho; g.dr2 = dr2;
+    g.inv_dr2 = 1.0 / dr2;
+    g.inv_drho = 1.0 / drho;
+    // packed interval records {y_k, y_k+1, y''_k, y''_k+1}: one 32-byte
+    // (binary64) or 16-byte (binary32) load per spline evaluation
+    dfree((void *)g.pk_rho); dfree((void *)g.pk_phi); dfree((void *)g.pk_F);
+    dfree((void *)g.pkf_rho); dfree((void *)g.pkf_phi); dfree((void *)g.pkf_F);
+    auto pack = [&](const double *y, const double *ydd, int npts, int nfun, const double4_32a **d64,
+                    const float4 **d32) -> int {
+        const size_t nint = (size_t)npts - 1;
+        std::vector<double4_32a> h64(nint * nfun);
+        std::vector<float4> h32(nint * nfun);
+        for (int f = 0; f < nfun; f++)
+            for (size_t k = 0; k < nint; k++)
+            {
+                const double *yy = y + (size_t)f * npts, *dd = ydd + (size_t)f * npts;
+                h64[f * nint + k] = make_double4_32a(yy[k], yy[k + 1], dd[k], dd[k + 1]);
+                h32[f * nint + k] = make_float4((float)yy[k], (float)yy[k + 1], (float)dd[k], (float)dd[k + 1]);
+            }
+        int rc2;
+        if ((rc2 = dalloc((double4_32a **)d64, h64.size())) || (rc2 = dalloc((float4 **)d32, h32.size()))) return rc2;
+        FMDG_CK(cudaMemcpy((void *)*d64, h64.data(), h64.size() * sizeof(double4_32a), cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        return FMDG_OK;
+    };
+    if ((rc = pack(rho, rhoDD, Nr2, nelem, &g.pk_rho, &g.pkf_rho))) return rc;
+    if ((rc = pack(phi, phiDD, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi))) return rc;
+    if ((rc = pack(F, F_DD, Nrho, nelem, &g.pk_F, &g.pkf_F))) return rc;
     invalidate_graph(s);
     return FMDG_OK;
 }
@@ -325,6 +357,34 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         (rc = dalloc(&g.brank, cap)) || (rc = dalloc(&g.bnewidx, cap)) ||
         (rc = dalloc(&g.dep_count, 4 * (size_t)ncell)) || (rc = dalloc(&g.arr_base, (size_t)ncell + 1)) ||
         (rc = dalloc(&g.bucket, cap)) || (rc = dalloc(&g.arr_slot, cap)))
+        return rc;
+    // neighbour list: size from the densest cell (an atom with more
+    // candidates falls back to a direct stencil scan)
+    double rc2max = 0.0;
+    for (int k = 0; k < s->nkinds * s->nkinds; k++)
+    {
+        const fmdg_pair_t &pp = s->h_pairs[k];
+        const double r2 = pp.cat == FMDG_POT_MORSE ? pp.p[3] : pp.p[2];
+        if (r2 > rc2max) rc2max = r2;
+    }
+    if (!(rc2max > 0.0))
+    {
+        const double hmin = fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
+        rc2max = hmin * hmin;
+    }
+    const double rlist = sqrt(rc2max) + 1e-2;
+    g.rlist2 = (float)(rlist * rlist);
+    int maxcell = 0;
+    for (int c = 0; c < ncell; c++) maxcell = cell_count[c] > maxcell ? cell_count[c] : maxcell;
+    const double nmax = maxcell / (g.cellh[0] * g.cellh[1] * g.cellh[2]);
+    double est = 4.0 / 3.0 * 3.14159265358979 * rlist * rlist * rlist * nmax;
+    int maxnb = (int)(1.3 * est + 16);
+    maxnb = (maxnb + 7) & ~7;
+    if (maxnb < 32) maxnb = 32;
+    if (maxnb > 1024) maxnb = 1024;
+    g.maxnb = maxnb;
+    for (int d = 0; d < 3; d++) g.cellh_f[d] = (float)g.cellh[d];
+    if ((rc = dalloc(&g.xf4, cap)) || (rc = dalloc(&g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(&g.nbr_count, cap)))
         return rc;
     g.arr_lower = g.dep_count + ncell;
     g.arr_total = g.dep_count + 2 * ncell;
@@ -472,21 +532,24 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
     if (nsteps <= 0) return FMDG_OK;
     if (s->profiling)
     {
-        // phases timed separately with events: 0 refresh, 1 density, 2 force, 3 reduce
+        // phases timed separately with events:
+        // 0 refresh, 1 neighbour list, 2 density, 3 force, 4 reduce
         for (int k = 0; k < nsteps; k++)
         {
             FMDG_CK(cudaEventRecord(s->pev[0], s->stream));
             int rc = fmdg_launch_refresh(s, FMDG_REFRESH_VV, dt, active_group, thermostat);
             if (rc) return rc;
             FMDG_CK(cudaEventRecord(s->pev[1], s->stream));
-            if ((rc = fmdg_launch_density(s, active_group))) return rc;
+            if ((rc = fmdg_launch_nlist(s))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[2], s->stream));
-            if ((rc = fmdg_launch_pair_forces(s, active_group, 1, dt))) return rc;
+            if ((rc = fmdg_launch_density(s, active_group))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[3], s->stream));
-            if ((rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0))) return rc;
+            if ((rc = fmdg_launch_pair_forces(s, active_group, 1, dt))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[4], s->stream));
-            FMDG_CK(cudaEventSynchronize(s->pev[4]));
-            for (int ph = 0; ph < 4; ph++)
+            if ((rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[5], s->stream));
+            FMDG_CK(cudaEventSynchronize(s->pev[5]));
+            for (int ph = 0; ph < 5; ph++)
             {
                 float ms = 0.0f;
                 FMDG_CK(cudaEventElapsedTime(&ms, s->pev[ph], s->pev[ph + 1]));
@@ -517,7 +580,8 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
         s->graph_tau = tau; s->graph_T0 = T0;
         // kernels per captured step
         const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
-        s->graph_steps = 7 + 1 + (eam ? 1 : 0) + 1;
+        // memset node + 6 refresh kernels + 2 list kernels + density + force + reduce
+        s->graph_steps = 7 + 2 + (eam ? 1 : 0) + 1 + 1;
     }
     for (int k = 0; k < nsteps; k++) FMDG_CK(cudaGraphLaunch(s->graph, s->stream));
     s->launches += (long long)nsteps * (s->graph_steps - 1);  // memset node is not a kernel
@@ -593,8 +657,8 @@ extern "C" int fmdg_set_profiling(fmdg_sys_t *s, int on)
 
 extern "C" int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches)
 {
-    static const char *names[4] = {"bin", "density", "force", "reduce"};
-    for (int k = 0; k < 4; k++)
+    static const char *names[5] = {"bin", "nlist", "density", "force", "reduce"};
+    for (int k = 0; k < 5; k++)
         if (strcmp(name, names[k]) == 0)
         {
             *ms = s->prof_ms[k];

@@ -1,4 +1,4 @@
-// Pair-force, EAM density/embedding and reduction kernels (binary64 path).
+// Neighbour list, pair-force, EAM density/embedding and reduction kernels.
 //
 // Reference loops replaced (FMD 0.4.0):
 //   LJ    src/lj.c:28-90    with the pair update of src/lj.h:26-58
@@ -7,18 +7,32 @@
 //         F(rho), F'(rho)), src/eam.c:29-146 (forces, pass 0), pair updates
 //         src/eam.h:29-406, cubic spline src/cspline.h:26-27
 //   hybrid src/forces.c:33-290 (per-pair category switch)
-//   ghost images / partial-force fold-back src/md-ghost.c:711-825 and the
-//   PE Allreduce: replaced by periodic image shifts inside the loop and a
-//   deterministic two-level block reduction.
+//   ghost images and the partial-force fold-back src/md-ghost.c:711-825,
+//   the PE Allreduce src/lj.c:89: replaced by periodic image shifts inside
+//   the loops and a deterministic two-level block reduction.
 //
-// The reference visits each pair once (half shell, Newton's third law,
-// scattering into both atoms).  Here each thread owns one atom and gathers
-// over the full 27-cell stencil: every pair is evaluated from both sides,
-// no atomics, deterministic results, and the per-atom energy takes half of
-// each pair term.  Image shifts: a neighbour cell index below 0 (above
-// nc-1) along a periodic axis is the ghost copy of cell nc-1 (0) shifted by
-// -l (+l), exactly the ghost positions of src/md-ghost.c:85-107; along an
-// open axis it is empty.
+// Work decomposition.  The reference visits each pair once (half shell,
+// Newton's third law, scattering into both atoms).  Here one thread owns
+// one atom and gathers over all its neighbours: every pair is evaluated
+// from both sides, there are no atomics and results are deterministic; each
+// atom's energy takes half of each pair term.
+//
+// Per step, after the refresh:
+//   k_prep_local  cell-local binary32 coordinates of every atom (float4)
+//   k_nlist       27-cell stencil scan in binary32 against the largest
+//                 cutoff plus a margin; stores (j, stencil offset) per atom
+//   k_density     EAM pass 1 + embedding over the list
+//   k_force       pair forces over the list + velocity-Verlet finish step
+// An atom with more candidates than the list holds falls back to scanning
+// the stencil directly, so the list size is a performance knob only.
+//
+// Precision modes.  FMDG_PREC_FP64: every pair quantity in binary64, the
+// binary32 list only prunes (its margin keeps every pair within the cutoff).
+// FMDG_PREC_MIXED: pair geometry from the binary32 cell-local coordinates,
+// pair/spline/embedding arithmetic in binary32, forces and energies summed
+// in binary64 (binary32 partial sums of at most 8 pair terms are added to
+// binary64 accumulators).  Pairs within 1e-4 relative of a cutoff are
+// re-tested in binary64 so both modes include exactly the same pairs.
 #include "fmdg_internal.cuh"
 
 namespace {
@@ -28,6 +42,7 @@ enum { CAT_LJ = 1, CAT_EAM = 2, CAT_MORSE = 3, CAT_HYBRID = 4 };
 struct SmemPot
 {
     fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
+    float pf[FMDG_MAXK * FMDG_MAXK][4];
     double mass[FMDG_MAXK];
     int elem[FMDG_MAXK];
 };
@@ -35,7 +50,11 @@ struct SmemPot
 __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
 {
     const int nk2 = g.nkinds * g.nkinds;
-    for (int k = threadIdx.x; k < nk2; k += blockDim.x) sp.pairs[k] = g.pairs[k];
+    for (int k = threadIdx.x; k < nk2; k += blockDim.x)
+    {
+        sp.pairs[k] = g.pairs[k];
+        for (int q = 0; q < 4; q++) sp.pf[k][q] = (float)g.pairs[k].p[q];
+    }
     for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
     {
         sp.mass[k] = g.mass[k];
@@ -44,74 +63,143 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
     __syncthreads();
 }
 
-// natural cubic spline on a uniform grid (src/cspline.h:26-27)
-__device__ __forceinline__ double spl_val(const double *y, const double *ydd, int lo, double a, double b, double h)
+// stencil offset code: (ox+1)*9 + (oy+1)*3 + (oz+1); 13 is the cell itself
+__device__ __forceinline__ int off_x(int code) { return code / 9 - 1; }
+__device__ __forceinline__ int off_y(int code) { return (code / 3) % 3 - 1; }
+__device__ __forceinline__ int off_z(int code) { return code % 3 - 1; }
+
+struct CellXYZ { int x, y, z; };
+
+__device__ __forceinline__ CellXYZ cell_xyz(const Geo &g, int c)
 {
-    return a * y[lo] + b * y[lo + 1] + ((a * a * a - a) * ydd[lo] + (b * b * b - b) * ydd[lo + 1]) * (h * h) / 6.0;
+    CellXYZ r;
+    r.x = c / (g.nc[1] * g.nc[2]);
+    r.y = (c / g.nc[2]) % g.nc[1];
+    r.z = c % g.nc[2];
+    return r;
 }
 
-__device__ __forceinline__ double spl_der(const double *y, const double *ydd, int lo, double a, double b, double h)
+// Neighbour cell index along one axis for home coordinate h and offset o;
+// -1 when the neighbour is outside an open face.  *shift is the image
+// translation of src/md-ghost.c:85-107 (ghost copy of the far layer).
+__device__ __forceinline__ int nb_axis(const Geo &g, int d, int h, int o, double *shift)
 {
-    return (y[lo + 1] - y[lo]) / h + ((3 * b * b - 1) * ydd[lo + 1] - (3 * a * a - 1) * ydd[lo]) * h / 6.0;
-}
-
-// Visit every (atom j, image shift) of the 27-cell stencil around cell c.
-template <typename F>
-__device__ __forceinline__ void for_each_neighbour(const Geo &g, const Side &S, int i, int c, F &&f)
-{
-    const int cx = c / (g.nc[1] * g.nc[2]), cy = (c / g.nc[2]) % g.nc[1], cz = c % g.nc[2];
-    for (int ox = -1; ox <= 1; ox++)
+    int j = h + o;
+    *shift = 0.0;
+    if (j < 0)
     {
-        int jx = cx + ox;
-        double sx = 0.0;
-        if (jx < 0) { if (!g.pbc[0]) continue; jx += g.nc[0]; sx = -g.l[0]; }
-        else if (jx >= g.nc[0]) { if (!g.pbc[0]) continue; jx -= g.nc[0]; sx = g.l[0]; }
-        for (int oy = -1; oy <= 1; oy++)
+        if (!g.pbc[d]) return -1;
+        j += g.nc[d];
+        *shift = -g.l[d];
+    }
+    else if (j >= g.nc[d])
+    {
+        if (!g.pbc[d]) return -1;
+        j -= g.nc[d];
+        *shift = g.l[d];
+    }
+    return j;
+}
+
+// Every (j, stencil code) of the 27-cell stencil of cell c except i itself.
+template <typename F>
+__device__ __forceinline__ void scan_stencil(const Geo &g, const Side &S, int i, CellXYZ ci, F &&f)
+{
+    for (int code = 0; code < 27; code++)
+    {
+        double sx, sy, sz;
+        const int jx = nb_axis(g, 0, ci.x, off_x(code), &sx);
+        const int jy = nb_axis(g, 1, ci.y, off_y(code), &sy);
+        const int jz = nb_axis(g, 2, ci.z, off_z(code), &sz);
+        if (jx < 0 || jy < 0 || jz < 0) continue;
+        const int nb = jz + g.nc[2] * (jy + g.nc[1] * jx);
+        const int jb = S.cell_start[nb], je = S.cell_start[nb + 1];
+        for (int j = jb; j < je; j++)
         {
-            int jy = cy + oy;
-            double sy = 0.0;
-            if (jy < 0) { if (!g.pbc[1]) continue; jy += g.nc[1]; sy = -g.l[1]; }
-            else if (jy >= g.nc[1]) { if (!g.pbc[1]) continue; jy -= g.nc[1]; sy = g.l[1]; }
-            for (int oz = -1; oz <= 1; oz++)
-            {
-                int jz = cz + oz;
-                double sz = 0.0;
-                if (jz < 0) { if (!g.pbc[2]) continue; jz += g.nc[2]; sz = -g.l[2]; }
-                else if (jz >= g.nc[2]) { if (!g.pbc[2]) continue; jz -= g.nc[2]; sz = g.l[2]; }
-                const int nb = jz + g.nc[2] * (jy + g.nc[1] * jx);
-                const bool self = (ox == 0 && oy == 0 && oz == 0);
-                const int jb = S.cell_start[nb], je = S.cell_start[nb + 1];
-                for (int j = jb; j < je; j++)
-                {
-                    if (self && j == i) continue;
-                    f(j, sx, sy, sz);
-                }
-            }
+            if (code == 13 && j == i) continue;
+            f(j, code);
         }
     }
 }
 
-// rv = x_i - (x_j + shift), r2 summed as the reference does (no FMA)
-struct PairGeom
+// list walk with stencil fallback
+template <typename F>
+__device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i, CellXYZ ci, F &&f)
 {
-    double rv[3];
-    double r2;
-};
+    const int cnt = g.nbr_count[i];
+    if (cnt <= g.maxnb)
+    {
+        const int cap = g.cap;
+        for (int k = 0; k < cnt; k++)
+        {
+            const int e = g.nbr[(size_t)k * cap + i];
+            f(e & 0x3ffffff, e >> 26);
+        }
+    }
+    else
+        scan_stencil(g, S, i, ci, f);
+}
 
-__device__ __forceinline__ PairGeom pair_geom(const double xi[3], const Side &S, int cap, int j,
-                                              double sx, double sy, double sz)
+// binary64 pair geometry: rv = x_i - (x_j + image shift), r2 summed without
+// fused multiply-adds as the reference does (src/forces.h:25-34)
+struct Geom64 { double rv[3]; double r2; };
+
+__device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const double xi[3], CellXYZ ci, int j, int code)
 {
-    PairGeom p;
-    const double s[3] = {sx, sy, sz};
+    Geom64 p;
+    const int cap = g.cap;
+    const int h[3] = {ci.x, ci.y, ci.z};
+    const int o[3] = {off_x(code), off_y(code), off_z(code)};
     for (int d = 0; d < 3; d++)
     {
-        double x2 = S.x[d * cap + j];
-        if (s[d] != 0.0) x2 = __dadd_rn(x2, s[d]);
+        double s;
+        nb_axis(g, d, h[d], o[d], &s);
+        double x2 = S.x[(size_t)d * cap + j];
+        if (s != 0.0) x2 = __dadd_rn(x2, s);
         p.rv[d] = __dsub_rn(xi[d], x2);
     }
     p.r2 = __dadd_rn(__dadd_rn(__dmul_rn(p.rv[0], p.rv[0]), __dmul_rn(p.rv[1], p.rv[1])),
                      __dmul_rn(p.rv[2], p.rv[2]));
     return p;
+}
+
+// binary32 pair geometry from cell-local coordinates
+__device__ __forceinline__ float3 geom32(const Geo &g, float4 xi, float4 xj, int code)
+{
+    return make_float3(xi.x - xj.x - (float)off_x(code) * g.cellh_f[0],
+                       xi.y - xj.y - (float)off_y(code) * g.cellh_f[1],
+                       xi.z - xj.z - (float)off_z(code) * g.cellh_f[2]);
+}
+
+// natural cubic spline on a uniform grid (src/cspline.h:26-27), packed
+// interval record t = {y_lo, y_hi, y''_lo, y''_hi}
+__device__ __forceinline__ double spl_val(double4_32a t, double a, double b, double hh6)
+{
+    return a * t.x + b * t.y + ((a * a * a - a) * t.z + (b * b * b - b) * t.w) * hh6;
+}
+__device__ __forceinline__ double spl_der(double4_32a t, double a, double b, double inv_h, double h6)
+{
+    return (t.y - t.x) * inv_h + ((3 * b * b - 1) * t.w - (3 * a * a - 1) * t.z) * h6;
+}
+__device__ __forceinline__ float spl_val(float4 t, float a, float b, float hh6)
+{
+    return a * t.x + b * t.y + ((a * a * a - a) * t.z + (b * b * b - b) * t.w) * hh6;
+}
+__device__ __forceinline__ float spl_der(float4 t, float a, float b, float inv_h, float h6)
+{
+    return (t.y - t.x) * inv_h + ((3.f * b * b - 1.f) * t.w - (3.f * a * a - 1.f) * t.z) * h6;
+}
+
+// is r2 (binary32) within rc2?  Near the cutoff the decision is taken in
+// binary64 from the absolute positions, as the reference does.
+__device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i, CellXYZ ci, int j, int code,
+                                             float r2f, double rc2)
+{
+    const float rc2f = (float)rc2;
+    if (fabsf(r2f - rc2f) > 1e-4f * rc2f) return r2f < rc2f;
+    const int cap = g.cap;
+    const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+    return geom64(g, S, xi, ci, j, code).r2 < rc2;
 }
 
 // Deterministic block reduction of NV doubles; thread 0 writes out[0..NV).
@@ -137,9 +225,86 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
     }
 }
 
-// EAM pass 1 + embedding: rho_i = sum_j f_{elem(j)}(r_ij^2), then
-// vaream_i = F'(rho_i) and the embedding energy F(rho_i) into the partials.
-template <bool HYBRID>
+// binary32 partial sums flushed into binary64 every 8 terms
+template <int NV>
+struct Acc32
+{
+    float part[NV];
+    double sum[NV];
+    int n;
+    __device__ __forceinline__ Acc32() : n(0)
+    {
+        for (int k = 0; k < NV; k++) { part[k] = 0.f; sum[k] = 0.0; }
+    }
+    __device__ __forceinline__ void tick()
+    {
+        if (++n == 8) flush();
+    }
+    __device__ __forceinline__ void flush()
+    {
+        for (int k = 0; k < NV; k++) { sum[k] += (double)part[k]; part[k] = 0.f; }
+        n = 0;
+    }
+};
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void k_prep_local(Geo g)
+{
+    const Dyn *dyn = g.dyn;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
+    const int cap = g.cap;
+    const float lx = (float)(S.x[i] - c.x * g.cellh[0]);
+    const float ly = (float)(S.x[cap + i] - c.y * g.cellh[1]);
+    const float lz = (float)(S.x[2 * (size_t)cap + i] - c.z * g.cellh[2]);
+    g.xf4[i] = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
+}
+
+__global__ void __launch_bounds__(128) k_nlist(Geo g)
+{
+    const Dyn *dyn = g.dyn;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
+    const float4 xi = g.xf4[i];
+    const int cap = g.cap, maxnb = g.maxnb;
+    const float rl2 = g.rlist2;
+    int cnt = 0;
+    for (int code = 0; code < 27; code++)
+    {
+        double sdummy;
+        const int jx = nb_axis(g, 0, ci.x, off_x(code), &sdummy);
+        const int jy = nb_axis(g, 1, ci.y, off_y(code), &sdummy);
+        const int jz = nb_axis(g, 2, ci.z, off_z(code), &sdummy);
+        if (jx < 0 || jy < 0 || jz < 0) continue;
+        const int nb = jz + g.nc[2] * (jy + g.nc[1] * jx);
+        const int jb = S.cell_start[nb], je = S.cell_start[nb + 1];
+        const float ox = (float)off_x(code) * g.cellh_f[0];
+        const float oy = (float)off_y(code) * g.cellh_f[1];
+        const float oz = (float)off_z(code) * g.cellh_f[2];
+        for (int j = jb; j < je; j++)
+        {
+            if (code == 13 && j == i) continue;
+            const float4 xj = g.xf4[j];
+            const float dx = xi.x - xj.x - ox, dy = xi.y - xj.y - oy, dz = xi.z - xj.z - oz;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 < rl2)
+            {
+                if (cnt < maxnb) g.nbr[(size_t)cnt * cap + i] = j | (code << 26);
+                cnt++;
+            }
+        }
+    }
+    g.nbr_count[i] = cnt;
+}
+
+// EAM pass 1 + embedding: rho_i = sum_j f_{elem(j)}(r_ij^2) (src/eam.h:270-406),
+// vaream_i = F'(rho_i), energy F(rho_i) (src/eam.c:160-179).
+template <bool MIXED, bool HYBRID>
 __global__ void __launch_bounds__(128) k_density(Geo g, int group)
 {
     __shared__ SmemPot sp;
@@ -158,37 +323,75 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
         double rho = 0.0;
         if (active)
         {
-            const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * cap + i]};
-            const double h = g.dr2;
-            for_each_neighbour(g, S, i, S.cell_of[i], [&](int j, double sx, double sy, double sz) {
-                if (group >= 0 && S.group[j] != group) return;
-                const int kj = S.kind[j];
-                const fmdg_pair_t &pp = sp.pairs[ki * g.nkinds + kj];
-                if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                const PairGeom p = pair_geom(xi, S, cap, j, sx, sy, sz);
-                if (p.r2 < pp.p[2])
-                {
-                    const int ir2 = min((int)(p.r2 / h), g.Nr2 - 2);
-                    const double a = (ir2 + 1) - p.r2 / h;
-                    const double b = 1 - a;
-                    const int ej = pp.jloc;
-                    rho += spl_val(g.erho + (size_t)ej * g.Nr2, g.erhoDD + (size_t)ej * g.Nr2, ir2, a, b, h);
-                }
-            });
+            const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
+            const int nk = g.nkinds;
+            const int nint = g.Nr2 - 1;
+            if (!MIXED)
+            {
+                const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+                const double h = g.dr2, inv_h = g.inv_dr2, hh6 = h * h / 6.0;
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
+                    if (HYBRID && pp.cat != FMDG_POT_EAM) return;
+                    const Geom64 p = geom64(g, S, xi, ci, j, code);
+                    if (p.r2 < pp.p[2])
+                    {
+                        const double q = p.r2 * inv_h;
+                        const int ir2 = min((int)q, nint - 1);
+                        const double a = (ir2 + 1) - q, b = 1 - a;
+                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], a, b, hh6);
+                    }
+                });
+            }
+            else
+            {
+                const float4 xi = g.xf4[i];
+                const float h = (float)g.dr2, inv_h = (float)g.inv_dr2, hh6 = h * h / 6.f;
+                Acc32<1> ac;
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 xj = g.xf4[j];
+                    const int kj = __float_as_int(xj.w);
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + kj];
+                    if (HYBRID && pp.cat != FMDG_POT_EAM) return;
+                    const float3 rv = geom32(g, xi, xj, code);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                    {
+                        const float q = r2 * inv_h;
+                        const int ir2 = min((int)q, nint - 1);
+                        const float a = (float)(ir2 + 1) - q, b = 1.f - a;
+                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], a, b, hh6);
+                        ac.tick();
+                    }
+                });
+                ac.flush();
+                rho = ac.sum[0];
+            }
             // embedding (src/eam.c:160-179)
-            const double hr = g.drho;
-            int irho = (int)(rho / hr);
+            const double qr = rho * g.inv_drho;
+            int irho = (int)qr;
             if (irho >= g.Nrho - 1 || irho < 0)
             {
                 atomic_or_err(dyn, FMDG_ERRBIT_RHO_RANGE);
                 irho = irho < 0 ? 0 : g.Nrho - 2;
             }
-            const double a = (irho + 1) - rho / hr;
-            const double b = 1 - a;
-            const double *Ft = g.eF + (size_t)ei * g.Nrho;
-            const double *Fdd = g.eFDD + (size_t)ei * g.Nrho;
-            g.vaream[i] = spl_der(Ft, Fdd, irho, a, b, hr);
-            acc[0] = spl_val(Ft, Fdd, irho, a, b, hr);
+            const int nrint = g.Nrho - 1;
+            if (!MIXED)
+            {
+                const double a = (irho + 1) - qr, b = 1 - a, h = g.drho;
+                const double4_32a t = g.pk_F[(size_t)ei * nrint + irho];
+                g.vaream[i] = spl_der(t, a, b, g.inv_drho, h / 6.0);
+                acc[0] = spl_val(t, a, b, h * h / 6.0);
+            }
+            else
+            {
+                const float a = (float)((irho + 1) - qr), b = 1.f - a, h = (float)g.drho;
+                const float4 t = g.pkf_F[(size_t)ei * nrint + irho];
+                g.vaream[i] = (double)spl_der(t, a, b, (float)g.inv_drho, h / 6.f);
+                acc[0] = (double)spl_val(t, a, b, h * h / 6.f);
+            }
         }
         else
             g.vaream[i] = 0.0;
@@ -198,7 +401,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
 
 // Pair forces + per-atom half energies; with finish=1 also the
 // velocity-Verlet finishStep (src/integrators.c:94-126) and its reductions.
-template <int CAT>
+template <int CAT, bool MIXED>
 __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, double dt)
 {
     __shared__ SmemPot sp;
@@ -218,76 +421,155 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
         double pe = 0.0;
         if (active)
         {
-            const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * cap + i]};
-            const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
-            for_each_neighbour(g, S, i, S.cell_of[i], [&](int j, double sx, double sy, double sz) {
-                if (group >= 0 && S.group[j] != group) return;
-                const int kj = S.kind[j];
-                const fmdg_pair_t &pp = sp.pairs[ki * g.nkinds + kj];
-                const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
-                const PairGeom p = pair_geom(xi, S, cap, j, sx, sy, sz);
-                if (cat == FMDG_POT_LJ)
-                {
-                    if (p.r2 < pp.p[2])
+            const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
+            const int nk = g.nkinds;
+            const int nint = g.Nr2 - 1;
+            const size_t ne = g.nelem;
+            if (!MIXED)
+            {
+                const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+                const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
+                const double h = g.dr2, inv_h = g.inv_dr2, hh6 = h * h / 6.0, h6 = h / 6.0;
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
+                    const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
+                    const Geom64 p = geom64(g, S, xi, ci, j, code);
+                    if (cat == FMDG_POT_LJ)
                     {
-                        const double inv_r2 = 1.0 / p.r2;
-                        const double inv_rs2 = pp.p[1] * inv_r2;
-                        const double inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
-                        const double inv_rs12 = inv_rs6 * inv_rs6;
-                        const double factor = 12.0 * pp.p[0] * inv_r2 * (inv_rs12 - 0.5 * inv_rs6);
-                        for (int d = 0; d < 3; d++) f[d] += p.rv[d] * factor;
-                        pe += 0.5 * (pp.p[0] * (inv_rs12 - inv_rs6));
+                        if (p.r2 < pp.p[2])
+                        {
+                            const double inv_r2 = 1.0 / p.r2;
+                            const double inv_rs2 = pp.p[1] * inv_r2;
+                            const double inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
+                            const double inv_rs12 = inv_rs6 * inv_rs6;
+                            const double factor = 12.0 * pp.p[0] * inv_r2 * (inv_rs12 - 0.5 * inv_rs6);
+                            for (int d = 0; d < 3; d++) f[d] += p.rv[d] * factor;
+                            pe += 0.5 * (pp.p[0] * (inv_rs12 - inv_rs6));
+                        }
                     }
-                }
-                else if (cat == FMDG_POT_MORSE)
-                {
-                    if (p.r2 < pp.p[3])
+                    else if (cat == FMDG_POT_MORSE)
                     {
-                        const double r = sqrt(p.r2);
-                        const double inv_r = 1.0 / r;
-                        const double e1 = exp(-pp.p[1] * (r - pp.p[2]));
-                        const double e2 = e1 * e1;
-                        const double factor = 2.0 * pp.p[1] * pp.p[0] * inv_r * (e2 - e1);
-                        for (int d = 0; d < 3; d++) f[d] += factor * p.rv[d];
-                        pe += 0.5 * (pp.p[0] * (e2 - 2.0 * e1));
+                        if (p.r2 < pp.p[3])
+                        {
+                            const double r = sqrt(p.r2);
+                            const double inv_r = 1.0 / r;
+                            const double e1 = exp(-pp.p[1] * (r - pp.p[2]));
+                            const double e2 = e1 * e1;
+                            const double factor = 2.0 * pp.p[1] * pp.p[0] * inv_r * (e2 - e1);
+                            for (int d = 0; d < 3; d++) f[d] += factor * p.rv[d];
+                            pe += 0.5 * (pp.p[0] * (e2 - 2.0 * e1));
+                        }
                     }
-                }
-                else if (cat == FMDG_POT_EAM)
-                {
-                    if (p.r2 < pp.p[2])
+                    else if (cat == FMDG_POT_EAM)
                     {
-                        const double h = g.dr2;
-                        const int ir2 = min((int)(p.r2 / h), g.Nr2 - 2);
-                        const double a = (ir2 + 1) - p.r2 / h;
-                        const double b = 1 - a;
-                        const int ei = pp.iloc, ej = pp.jloc;
-                        const size_t Nr2 = g.Nr2;
-                        const double *ph = g.ephi + ((size_t)ei * g.nelem + ej) * Nr2;
-                        const double *phdd = g.ephiDD + ((size_t)ei * g.nelem + ej) * Nr2;
-                        const double phi_d = spl_der(ph, phdd, ir2, a, b, h);
-                        const double rho_ip = spl_der(g.erho + ei * Nr2, g.erhoDD + ei * Nr2, ir2, a, b, h);
-                        const double rho_jp = (ei == ej) ? rho_ip
-                                            : spl_der(g.erho + ej * Nr2, g.erhoDD + ej * Nr2, ir2, a, b, h);
-                        const double mag = 2 * (fpi * rho_jp + g.vaream[j] * rho_ip + phi_d);
-                        for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
-                        pe += 0.5 * spl_val(ph, phdd, ir2, a, b, h);
+                        if (p.r2 < pp.p[2])
+                        {
+                            const double q = p.r2 * inv_h;
+                            const int ir2 = min((int)q, nint - 1);
+                            const double a = (ir2 + 1) - q, b = 1 - a;
+                            const int ei = pp.iloc, ej = pp.jloc;
+                            const double4_32a tph = g.pk_phi[((size_t)ei * ne + ej) * nint + ir2];
+                            const double phi_d = spl_der(tph, a, b, inv_h, h6);
+                            const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], a, b, inv_h, h6);
+                            const double rho_jp = (ei == ej) ? rho_ip
+                                                : spl_der(g.pk_rho[(size_t)ej * nint + ir2], a, b, inv_h, h6);
+                            const double mag = 2 * (fpi * rho_jp + g.vaream[j] * rho_ip + phi_d);
+                            for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
+                            pe += 0.5 * spl_val(tph, a, b, hh6);
+                        }
                     }
-                }
-            });
+                });
+            }
+            else
+            {
+                const float4 xi = g.xf4[i];
+                const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? (float)g.vaream[i] : 0.f;
+                const float h = (float)g.dr2, inv_h = (float)g.inv_dr2, hh6 = h * h / 6.f, h6 = h / 6.f;
+                Acc32<4> ac;
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 xj = g.xf4[j];
+                    const int kj = __float_as_int(xj.w);
+                    const int pidx = ki * nk + kj;
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
+                    const float3 rv = geom32(g, xi, xj, code);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    if (cat == FMDG_POT_LJ)
+                    {
+                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                        {
+                            const float inv_r2 = __frcp_rn(r2);
+                            const float inv_rs2 = sp.pf[pidx][1] * inv_r2;
+                            const float inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
+                            const float inv_rs12 = inv_rs6 * inv_rs6;
+                            const float eps4 = sp.pf[pidx][0];
+                            const float factor = 12.f * eps4 * inv_r2 * (inv_rs12 - 0.5f * inv_rs6);
+                            ac.part[0] += rv.x * factor;
+                            ac.part[1] += rv.y * factor;
+                            ac.part[2] += rv.z * factor;
+                            ac.part[3] += 0.5f * (eps4 * (inv_rs12 - inv_rs6));
+                            ac.tick();
+                        }
+                    }
+                    else if (cat == FMDG_POT_MORSE)
+                    {
+                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[3]))
+                        {
+                            const float D0 = sp.pf[pidx][0], al = sp.pf[pidx][1], r0 = sp.pf[pidx][2];
+                            const float r = sqrtf(r2);
+                            const float inv_r = __frcp_rn(r);
+                            const float e1 = expf(-al * (r - r0));
+                            const float e2 = e1 * e1;
+                            const float factor = 2.f * al * D0 * inv_r * (e2 - e1);
+                            ac.part[0] += factor * rv.x;
+                            ac.part[1] += factor * rv.y;
+                            ac.part[2] += factor * rv.z;
+                            ac.part[3] += 0.5f * (D0 * (e2 - 2.f * e1));
+                            ac.tick();
+                        }
+                    }
+                    else if (cat == FMDG_POT_EAM)
+                    {
+                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                        {
+                            const float q = r2 * inv_h;
+                            const int ir2 = min((int)q, nint - 1);
+                            const float a = (float)(ir2 + 1) - q, b = 1.f - a;
+                            const int ei = pp.iloc, ej = pp.jloc;
+                            const float4 tph = g.pkf_phi[((size_t)ei * ne + ej) * nint + ir2];
+                            const float phi_d = spl_der(tph, a, b, inv_h, h6);
+                            const float rho_ip = spl_der(g.pkf_rho[(size_t)ei * nint + ir2], a, b, inv_h, h6);
+                            const float rho_jp = (ei == ej) ? rho_ip
+                                               : spl_der(g.pkf_rho[(size_t)ej * nint + ir2], a, b, inv_h, h6);
+                            const float mag = 2.f * (fpi * rho_jp + (float)g.vaream[j] * rho_ip + phi_d);
+                            ac.part[0] -= mag * rv.x;
+                            ac.part[1] -= mag * rv.y;
+                            ac.part[2] -= mag * rv.z;
+                            ac.part[3] += 0.5f * spl_val(tph, a, b, hh6);
+                            ac.tick();
+                        }
+                    }
+                });
+                ac.flush();
+                for (int d = 0; d < 3; d++) f[d] = ac.sum[d];
+                pe = ac.sum[3];
+            }
         }
-        for (int d = 0; d < 3; d++) g.F[d * cap + i] = f[d];
+        for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
         acc[0] = pe;
         if (active)
         {
             const double m = sp.mass[ki];
-            double v[3] = {S.v[i], S.v[cap + i], S.v[2 * cap + i]};
+            double v[3] = {S.v[i], S.v[cap + i], S.v[2 * (size_t)cap + i]};
             if (finish)
             {
                 const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
                 for (int d = 0; d < 3; d++)
                 {
                     v[d] = __dadd_rn(v[d], __dmul_rn(coef, f[d]));
-                    S.v[d * cap + i] = v[d];
+                    S.v[(size_t)d * cap + i] = v[d];
                 }
             }
             acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
@@ -297,10 +579,8 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
             acc[5] = 1.0;
         }
     }
-    double tmp[6];
-    for (int k = 0; k < 6; k++) tmp[k] = acc[k];
     __shared__ double blk[6];
-    block_reduce_store<6>(tmp, blk);
+    block_reduce_store<6>(acc, blk);
     if (threadIdx.x == 0)
         for (int k = 0; k < 6; k++) g.partials[(size_t)k * gridDim.x + blockIdx.x] = blk[k];
 }
@@ -318,7 +598,7 @@ __global__ void __launch_bounds__(128) k_thermo(Geo g, int group)
     if (i < n && (group < 0 || S.group[i] == group))
     {
         const double m = g.mass[S.kind[i]];
-        const double v[3] = {S.v[i], S.v[cap + i], S.v[2 * cap + i]};
+        const double v[3] = {S.v[i], S.v[cap + i], S.v[2 * (size_t)cap + i]};
         acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         acc[2] = m * v[0];
         acc[3] = m * v[1];
@@ -375,29 +655,56 @@ __global__ void k_reduce_final(Geo g, int nblocks, int keep_pe, int with_emb, in
 
 int fmdg_force_blocks(const fmdg_sys_t *s) { return fmdg_grid(s->g.cap > 0 ? s->g.cap : 1, 128); }
 
+int fmdg_launch_nlist(fmdg_sys_t *s)
+{
+    const int nb = fmdg_force_blocks(s);
+    k_prep_local<<<fmdg_grid(s->g.cap, 256), 256, 0, s->stream>>>(s->g);
+    k_nlist<<<nb, 128, 0, s->stream>>>(s->g);
+    s->launches += 2;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
 int fmdg_launch_density(fmdg_sys_t *s, int group)
 {
     const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
     if (!eam) return FMDG_OK;
     const int nb = fmdg_force_blocks(s);
-    const int ncat = __builtin_popcount(s->cats);
-    if (ncat > 1) k_density<true><<<nb, 128, 0, s->stream>>>(s->g, group);
-    else k_density<false><<<nb, 128, 0, s->stream>>>(s->g, group);
+    const bool hyb = __builtin_popcount(s->cats) > 1;
+    const bool mixed = s->g.prec == FMDG_PREC_MIXED;
+    cudaStream_t st = s->stream;
+    if (mixed)
+    {
+        if (hyb) k_density<true, true><<<nb, 128, 0, st>>>(s->g, group);
+        else k_density<true, false><<<nb, 128, 0, st>>>(s->g, group);
+    }
+    else
+    {
+        if (hyb) k_density<false, true><<<nb, 128, 0, st>>>(s->g, group);
+        else k_density<false, false><<<nb, 128, 0, st>>>(s->g, group);
+    }
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
 }
 
-int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt)
+template <bool MIXED>
+static void launch_force_t(fmdg_sys_t *s, int nb, int group, int finish, double dt)
 {
     Geo &g = s->g;
-    const int nb = fmdg_force_blocks(s);
     cudaStream_t st = s->stream;
     const int ncat = __builtin_popcount(s->cats);
-    if (ncat > 1) k_force<CAT_HYBRID><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else if (s->cats == (1 << FMDG_POT_LJ)) k_force<CAT_LJ><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else if (s->cats == (1 << FMDG_POT_MORSE)) k_force<CAT_MORSE><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else k_force<CAT_EAM><<<nb, 128, 0, st>>>(g, group, finish, dt);
+    if (ncat > 1) k_force<CAT_HYBRID, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
+    else if (s->cats == (1 << FMDG_POT_LJ)) k_force<CAT_LJ, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
+    else if (s->cats == (1 << FMDG_POT_MORSE)) k_force<CAT_MORSE, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
+    else k_force<CAT_EAM, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
+}
+
+int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt)
+{
+    const int nb = fmdg_force_blocks(s);
+    if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<true>(s, nb, group, finish, dt);
+    else launch_force_t<false>(s, nb, group, finish, dt);
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
@@ -405,8 +712,9 @@ int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt)
 
 int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt)
 {
-    int rc = fmdg_launch_density(s, group);
+    int rc = fmdg_launch_nlist(s);
     if (rc) return rc;
+    if ((rc = fmdg_launch_density(s, group))) return rc;
     return fmdg_launch_pair_forces(s, group, finish, dt);
 }
 

@@ -52,6 +52,17 @@ struct Geo   // passed by value to kernels
     double l[3], cellh[3];
     Side side[2];
     double *F, *vaream;
+    // per-step neighbour list (built after every refresh)
+    float4 *xf4;       // cell-local coordinates (binary32) + kind bits, current order
+    int *nbr;          // nbr[k*cap + i] = j | (stencil offset code << 26)
+    int *nbr_count;    // true count (entries beyond maxnb are not stored)
+    int maxnb;
+    float rlist2;      // binary32 prefilter radius^2 (largest cutoff + margin)
+    float cellh_f[3];
+    // packed spline tables: per interval k {y_k, y_k+1, y''_k, y''_k+1}
+    const double4_32a *pk_rho, *pk_phi, *pk_F;     // binary64
+    const float4 *pkf_rho, *pkf_phi, *pkf_F;   // binary32 copies (mixed mode)
+    double inv_dr2, inv_drho;
     // binning scratch
     int *bdest;        // destination interior cell, -1 deleted, -2 stays
     int *bpath;        // migration key bits
@@ -91,10 +102,10 @@ struct fmdg_sys
     int h_eam_elem[FMDG_MAXK];
     int cats;                     // bit mask of pair categories present
     cudaEvent_t ev0, ev1;
-    cudaEvent_t pev[5];
+    cudaEvent_t pev[6];
     bool profiling;
-    float prof_ms[4];
-    int prof_n[4];
+    float prof_ms[5];
+    int prof_n[5];
     long long launches;
     // captured multi-step graph
     cudaGraphExec_t graph;
@@ -119,6 +130,8 @@ int fmdg_set_error(const char *msg);
 int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int thermostat);
 int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt);
 int fmdg_launch_density(fmdg_sys_t *s, int group);
+int fmdg_launch_nlist(fmdg_sys_t *s);
+int fmdg_pack_tables(fmdg_sys_t *s);
 int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt);
 int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0);
 int fmdg_force_blocks(const fmdg_sys_t *s);

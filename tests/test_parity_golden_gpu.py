@@ -98,3 +98,29 @@ def test_binning_order_exact(gpu_lib, name):
             np.testing.assert_array_equal(d["cell"], b["r%d_cell" % r], err_msg=f"round {r}")
             np.testing.assert_array_equal(d["x"], b["r%d_x" % r], err_msg=f"round {r}")
         gpu_lib.fmd_free(md)
+
+
+MIXED_FORCE_TOL = 1e-5   # mixed mode: max |dF| / max |F| against the binary64 reference
+MIXED_PE_TOL = 1e-6      # relative potential energy
+
+
+@pytest.mark.parametrize("name", ["lj", "lj_small", "morse_open", "eam", "hybrid"])
+def test_mixed_precision_forces(gpu_lib, name):
+    """binary32 pair arithmetic with binary64 sums stays within the stated
+    bound of the reference's binary64 forces and energy at step 0."""
+    import ctypes as C
+    g = load_golden(name)
+    case = cases.CASES[name]
+    st = dict(names=case["names"], kind=g["state_kind"], group=g["state_group"], x=g["state_x"], v=g["state_v"])
+    gpu_lib.L.fmdx_set_precision.argtypes = [C.c_void_p, C.c_int]
+    with tempfile.TemporaryDirectory() as work:
+        md, _ = cases.setup(gpu_lib, name, work, state=st)
+        gpu_lib.L.fmdx_set_precision(md, 1)
+        gpu_lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+        d0 = gpu_lib.dump(md)
+        gpu_lib.fmd_free(md)
+    np.testing.assert_array_equal(d0["id"], g["s0_id"])
+    err = np.abs(d0["F"] - g["s0_F"]).max() / np.abs(g["s0_F"]).max()
+    assert err <= MIXED_FORCE_TOL, f"mixed force error {err:.3e}"
+    pe_err = abs(d0["pe"] - float(g["s0_pe"])) / abs(float(g["s0_pe"]))
+    assert pe_err <= MIXED_PE_TOL, f"mixed PE error {pe_err:.3e}"
