@@ -283,21 +283,30 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     g.nelem = nelem; g.Nrho = Nrho; g.Nr2 = Nr2; g.drho = drho; g.dr2 = dr2;
     g.inv_dr2 = 1.0 / dr2;
     g.inv_drho = 1.0 / drho;
-    // packed interval records {y_k, y_k+1, y''_k, y''_k+1}: one 32-byte
-    // (binary64) or 16-byte (binary32) load per spline evaluation
+    // Per-interval cubic coefficients of the natural spline (src/cspline.h:26-27)
+    // in the local coordinate b = x/h - k in [0,1): with C = y''*h^2/6,
+    //   y(b)   = k0 + k1 b + k2 b^2 + k3 b^3,
+    //   k0 = y_k, k1 = y_k+1 - y_k - 2C_k - C_k+1, k2 = 3C_k, k3 = C_k+1 - C_k,
+    //   dy/dx  = (k1 + 2 k2 b + 3 k3 b^2) / h,
+    // algebraically the reference's a/b form (a = 1-b).  Computed in binary64;
+    // the binary32 copy keeps k1 (the per-interval increment) to full relative
+    // precision, which the two-sample difference y_k+1 - y_k would not.
     dfree((void *)g.pk_rho); dfree((void *)g.pk_phi); dfree((void *)g.pk_F);
     dfree((void *)g.pkf_rho); dfree((void *)g.pkf_phi); dfree((void *)g.pkf_F);
-    auto pack = [&](const double *y, const double *ydd, int npts, int nfun, const double4_32a **d64,
+    auto pack = [&](const double *y, const double *ydd, double h, int npts, int nfun, const double4_32a **d64,
                     const float4 **d32) -> int {
         const size_t nint = (size_t)npts - 1;
         std::vector<double4_32a> h64(nint * nfun);
         std::vector<float4> h32(nint * nfun);
+        const double hh6 = h * h / 6.0;
         for (int f = 0; f < nfun; f++)
             for (size_t k = 0; k < nint; k++)
             {
                 const double *yy = y + (size_t)f * npts, *dd = ydd + (size_t)f * npts;
-                h64[f * nint + k] = make_double4_32a(yy[k], yy[k + 1], dd[k], dd[k + 1]);
-                h32[f * nint + k] = make_float4((float)yy[k], (float)yy[k + 1], (float)dd[k], (float)dd[k + 1]);
+                const double c0 = dd[k] * hh6, c1 = dd[k + 1] * hh6;
+                const double k0 = yy[k], k1 = yy[k + 1] - yy[k] - 2.0 * c0 - c1, k2 = 3.0 * c0, k3 = c1 - c0;
+                h64[f * nint + k] = make_double4_32a(k0, k1, k2, k3);
+                h32[f * nint + k] = make_float4((float)k0, (float)k1, (float)k2, (float)k3);
             }
         int rc2;
         if ((rc2 = dalloc((double4_32a **)d64, h64.size())) || (rc2 = dalloc((float4 **)d32, h32.size()))) return rc2;
@@ -305,9 +314,9 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
         FMDG_CK(cudaMemcpy((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
         return FMDG_OK;
     };
-    if ((rc = pack(rho, rhoDD, Nr2, nelem, &g.pk_rho, &g.pkf_rho))) return rc;
-    if ((rc = pack(phi, phiDD, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi))) return rc;
-    if ((rc = pack(F, F_DD, Nrho, nelem, &g.pk_F, &g.pkf_F))) return rc;
+    if ((rc = pack(rho, rhoDD, dr2, Nr2, nelem, &g.pk_rho, &g.pkf_rho))) return rc;
+    if ((rc = pack(phi, phiDD, dr2, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi))) return rc;
+    if ((rc = pack(F, F_DD, drho, Nrho, nelem, &g.pk_F, &g.pkf_F))) return rc;
     invalidate_graph(s);
     return FMDG_OK;
 }

@@ -171,23 +171,23 @@ __device__ __forceinline__ float3 geom32(const Geo &g, float4 xi, float4 xj, int
                        xi.z - xj.z - (float)off_z(code) * g.cellh_f[2]);
 }
 
-// natural cubic spline on a uniform grid (src/cspline.h:26-27), packed
-// interval record t = {y_lo, y_hi, y''_lo, y''_hi}
-__device__ __forceinline__ double spl_val(double4_32a t, double a, double b, double hh6)
+// natural cubic spline on a uniform grid (src/cspline.h:26-27) as a cubic
+// in the fraction b of interval k: t = {k0, k1, k2, k3}
+__device__ __forceinline__ double spl_val(double4_32a t, double b)
 {
-    return a * t.x + b * t.y + ((a * a * a - a) * t.z + (b * b * b - b) * t.w) * hh6;
+    return ((t.w * b + t.z) * b + t.y) * b + t.x;
 }
-__device__ __forceinline__ double spl_der(double4_32a t, double a, double b, double inv_h, double h6)
+__device__ __forceinline__ double spl_der(double4_32a t, double b, double inv_h)
 {
-    return (t.y - t.x) * inv_h + ((3 * b * b - 1) * t.w - (3 * a * a - 1) * t.z) * h6;
+    return ((3.0 * t.w * b + 2.0 * t.z) * b + t.y) * inv_h;
 }
-__device__ __forceinline__ float spl_val(float4 t, float a, float b, float hh6)
+__device__ __forceinline__ float spl_val(float4 t, float b)
 {
-    return a * t.x + b * t.y + ((a * a * a - a) * t.z + (b * b * b - b) * t.w) * hh6;
+    return ((t.w * b + t.z) * b + t.y) * b + t.x;
 }
-__device__ __forceinline__ float spl_der(float4 t, float a, float b, float inv_h, float h6)
+__device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
 {
-    return (t.y - t.x) * inv_h + ((3.f * b * b - 1.f) * t.w - (3.f * a * a - 1.f) * t.z) * h6;
+    return ((3.f * t.w * b + 2.f * t.z) * b + t.y) * inv_h;
 }
 
 // is r2 (binary32) within rc2?  Near the cutoff the decision is taken in
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
             if (!MIXED)
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
-                const double h = g.dr2, inv_h = g.inv_dr2, hh6 = h * h / 6.0;
+                const double inv_h = g.inv_dr2;
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
@@ -339,15 +339,14 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
                     {
                         const double q = p.r2 * inv_h;
                         const int ir2 = min((int)q, nint - 1);
-                        const double a = (ir2 + 1) - q, b = 1 - a;
-                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], a, b, hh6);
+                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], q - ir2);
                     }
                 });
             }
             else
             {
                 const float4 xi = g.xf4[i];
-                const float h = (float)g.dr2, inv_h = (float)g.inv_dr2, hh6 = h * h / 6.f;
+                const float inv_h = (float)g.inv_dr2;
                 Acc32<1> ac;
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
@@ -361,8 +360,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
                     {
                         const float q = r2 * inv_h;
                         const int ir2 = min((int)q, nint - 1);
-                        const float a = (float)(ir2 + 1) - q, b = 1.f - a;
-                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], a, b, hh6);
+                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], q - (float)ir2);
                         ac.tick();
                     }
                 });
@@ -380,17 +378,17 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
             const int nrint = g.Nrho - 1;
             if (!MIXED)
             {
-                const double a = (irho + 1) - qr, b = 1 - a, h = g.drho;
+                const double b = qr - irho;
                 const double4_32a t = g.pk_F[(size_t)ei * nrint + irho];
-                g.vaream[i] = spl_der(t, a, b, g.inv_drho, h / 6.0);
-                acc[0] = spl_val(t, a, b, h * h / 6.0);
+                g.vaream[i] = spl_der(t, b, g.inv_drho);
+                acc[0] = spl_val(t, b);
             }
             else
             {
-                const float a = (float)((irho + 1) - qr), b = 1.f - a, h = (float)g.drho;
+                const float b = (float)(qr - irho);
                 const float4 t = g.pkf_F[(size_t)ei * nrint + irho];
-                g.vaream[i] = (double)spl_der(t, a, b, (float)g.inv_drho, h / 6.f);
-                acc[0] = (double)spl_val(t, a, b, h * h / 6.f);
+                g.vaream[i] = (double)spl_der(t, b, (float)g.inv_drho);
+                acc[0] = (double)spl_val(t, b);
             }
         }
         else
@@ -429,7 +427,7 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
-                const double h = g.dr2, inv_h = g.inv_dr2, hh6 = h * h / 6.0, h6 = h / 6.0;
+                const double inv_h = g.inv_dr2;
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
@@ -467,16 +465,16 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
                         {
                             const double q = p.r2 * inv_h;
                             const int ir2 = min((int)q, nint - 1);
-                            const double a = (ir2 + 1) - q, b = 1 - a;
+                            const double b = q - ir2;
                             const int ei = pp.iloc, ej = pp.jloc;
                             const double4_32a tph = g.pk_phi[((size_t)ei * ne + ej) * nint + ir2];
-                            const double phi_d = spl_der(tph, a, b, inv_h, h6);
-                            const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], a, b, inv_h, h6);
+                            const double phi_d = spl_der(tph, b, inv_h);
+                            const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], b, inv_h);
                             const double rho_jp = (ei == ej) ? rho_ip
-                                                : spl_der(g.pk_rho[(size_t)ej * nint + ir2], a, b, inv_h, h6);
+                                                : spl_der(g.pk_rho[(size_t)ej * nint + ir2], b, inv_h);
                             const double mag = 2 * (fpi * rho_jp + g.vaream[j] * rho_ip + phi_d);
                             for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
-                            pe += 0.5 * spl_val(tph, a, b, hh6);
+                            pe += 0.5 * spl_val(tph, b);
                         }
                     }
                 });
@@ -485,7 +483,7 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
             {
                 const float4 xi = g.xf4[i];
                 const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? (float)g.vaream[i] : 0.f;
-                const float h = (float)g.dr2, inv_h = (float)g.inv_dr2, hh6 = h * h / 6.f, h6 = h / 6.f;
+                const float inv_h = (float)g.inv_dr2;
                 Acc32<4> ac;
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
@@ -536,18 +534,18 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
                         {
                             const float q = r2 * inv_h;
                             const int ir2 = min((int)q, nint - 1);
-                            const float a = (float)(ir2 + 1) - q, b = 1.f - a;
+                            const float b = q - (float)ir2;
                             const int ei = pp.iloc, ej = pp.jloc;
                             const float4 tph = g.pkf_phi[((size_t)ei * ne + ej) * nint + ir2];
-                            const float phi_d = spl_der(tph, a, b, inv_h, h6);
-                            const float rho_ip = spl_der(g.pkf_rho[(size_t)ei * nint + ir2], a, b, inv_h, h6);
+                            const float phi_d = spl_der(tph, b, inv_h);
+                            const float rho_ip = spl_der(g.pkf_rho[(size_t)ei * nint + ir2], b, inv_h);
                             const float rho_jp = (ei == ej) ? rho_ip
-                                               : spl_der(g.pkf_rho[(size_t)ej * nint + ir2], a, b, inv_h, h6);
+                                               : spl_der(g.pkf_rho[(size_t)ej * nint + ir2], b, inv_h);
                             const float mag = 2.f * (fpi * rho_jp + (float)g.vaream[j] * rho_ip + phi_d);
                             ac.part[0] -= mag * rv.x;
                             ac.part[1] -= mag * rv.y;
                             ac.part[2] -= mag * rv.z;
-                            ac.part[3] += 0.5f * spl_val(tph, a, b, hh6);
+                            ac.part[3] += 0.5f * spl_val(tph, b);
                             ac.tick();
                         }
                     }
