@@ -1,0 +1,74 @@
+/*
+ * CPU restatement of FMD 0.4.0's per-timestep hot path -- TEST
+ * INFRASTRUCTURE ONLY.  Used by tests/ as the checker for the GPU engine,
+ * by __graft_entry__.smoke(), and by bench.py as the timed CPU baseline.
+ * Nothing in the product (libfmd.so) links or calls it.
+ *
+ * It follows the reference's algorithms (file:line in fmd_oracle.c) with the
+ * same binary64 arithmetic: per-cell atom lists with swap-remove refresh and
+ * periodic migration, half-shell cell-pair loops with Newton's third law,
+ * LJ / Morse / EAM (r^2-grid cubic splines) / hybrid pair updates, velocity
+ * Verlet with Berendsen scaling, group thermodynamics.  Ghost cells are
+ * represented by image shifts of the interior cells.  Parity pins: the
+ * golden vectors in tests/golden/ were produced by the reference compiled
+ * from its own sources; tests/test_oracle_cpu.py checks this restatement
+ * against them.
+ *
+ * The interface mirrors include/fmdg.h so tests drive both identically.
+ */
+#ifndef FMD_ORACLE_H
+#define FMD_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_sys oracle_sys_t;
+
+typedef struct
+{
+    int cat;           /* 1 LJ, 2 EAM, 3 Morse */
+    int iloc, jloc;
+    int pad;
+    double p[4];       /* as fmdg_pair_t */
+} oracle_pair_t;
+
+typedef struct
+{
+    double kinetic, temperature, momentum[3], potential, count, pad;
+} oracle_thermo_t;
+
+oracle_sys_t *oracle_create(void);
+void oracle_destroy(oracle_sys_t *o);
+int oracle_set_threads(oracle_sys_t *o, int nthreads);
+int oracle_set_box(oracle_sys_t *o, const double l[3], const int pbc[3], const int nc[3], const double cellh[3]);
+int oracle_set_kinds(oracle_sys_t *o, int nkinds, const double *mass, const int *eam_elem);
+int oracle_set_pairs(oracle_sys_t *o, const oracle_pair_t *table);
+/* EAM tables: either given directly (same layout as fmdg_set_eam) ... */
+int oracle_set_eam(oracle_sys_t *o, int nelem, int Nrho, double drho, int Nr2, double dr2,
+                   const double *F, const double *F_DD, const double *rho, const double *rhoDD,
+                   const double *phi, const double *phiDD);
+/* ... or read from a DYNAMO setfl file (src/eam.c:376-555); returns the
+   number of elements and writes the element names (space separated) */
+int oracle_load_setfl(oracle_sys_t *o, const char *path, char *names, int names_len, double *cutoff);
+/* the r^2-grid tables of element `el` after oracle_load_setfl */
+int oracle_eam_table(oracle_sys_t *o, int el, int which, double *out, int *n);
+
+int oracle_upload(oracle_sys_t *o, int n, const int *cell_count, const double *x, const double *v,
+                  const unsigned *kind, const int *group, const unsigned *atomid);
+int oracle_natoms(oracle_sys_t *o);
+int oracle_download(oracle_sys_t *o, int *cell_of, double *x, double *v, double *F, double *vaream,
+                    unsigned *kind, int *group, unsigned *atomid);
+int oracle_set_state(oracle_sys_t *o, const double *x, const double *v);
+int oracle_refresh(oracle_sys_t *o);
+int oracle_compute_forces(oracle_sys_t *o, int group);
+int oracle_thermo(oracle_sys_t *o, int group, oracle_thermo_t *out);
+int oracle_vv_steps(oracle_sys_t *o, int nsteps, double dt, int group, int thermostat, double tau, double T0);
+int oracle_get_thermo(oracle_sys_t *o, oracle_thermo_t *out);
+unsigned oracle_errors(oracle_sys_t *o);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

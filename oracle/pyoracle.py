@@ -1,0 +1,162 @@
+"""ctypes wrapper of the CPU oracle (oracle/fmd_oracle.c) -- test
+infrastructure: used by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline only.  The oracle is built by `fmd_gb300.build.build_oracle()`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+MASS_UNIT = 9.6485332907e+03
+
+P = C.c_void_p
+
+
+class PairT(C.Structure):
+    _fields_ = [("cat", C.c_int), ("iloc", C.c_int), ("jloc", C.c_int), ("pad", C.c_int), ("p", C.c_double * 4)]
+
+
+class ThermoT(C.Structure):
+    _fields_ = [("kinetic", C.c_double), ("temperature", C.c_double), ("momentum", C.c_double * 3),
+                ("potential", C.c_double), ("count", C.c_double), ("pad", C.c_double)]
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def _lib():
+    if not os.path.exists(LIB):
+        from fmd_gb300.build import build_oracle
+        build_oracle()
+    L = C.CDLL(LIB)
+    L.oracle_create.restype = P
+    for name, args in [("oracle_destroy", [P]), ("oracle_set_threads", [P, C.c_int]),
+                       ("oracle_set_box", [P, P, P, P, P]), ("oracle_set_kinds", [P, C.c_int, P, P]),
+                       ("oracle_set_pairs", [P, P]),
+                       ("oracle_load_setfl", [P, C.c_char_p, C.c_char_p, C.c_int, P]),
+                       ("oracle_eam_table", [P, C.c_int, C.c_int, P, P]),
+                       ("oracle_upload", [P, C.c_int, P, P, P, P, P, P]), ("oracle_natoms", [P]),
+                       ("oracle_download", [P, P, P, P, P, P, P, P, P]), ("oracle_set_state", [P, P, P]),
+                       ("oracle_refresh", [P]), ("oracle_compute_forces", [P, C.c_int]),
+                       ("oracle_thermo", [P, C.c_int, P]),
+                       ("oracle_vv_steps", [P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double]),
+                       ("oracle_get_thermo", [P, P]), ("oracle_errors", [P])]:
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_uint if name == "oracle_errors" else (None if name == "oracle_destroy" else C.c_int)
+    return L
+
+
+class Oracle:
+    """One system of the CPU restatement."""
+
+    def __init__(self, threads: int = 1):
+        self.L = _lib()
+        self.o = C.c_void_p(self.L.oracle_create())
+        self.L.oracle_set_threads(self.o, threads)
+
+    def close(self):
+        if self.o:
+            self.L.oracle_destroy(self.o)
+            self.o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup(self, box, pbc, nc, cellh, kinds, pots, setfl=None):
+        """kinds: [(name, mass_amu)]; pots: tuples as in tests/cases.py:
+        ("lj", k1, k2, sigma, eps, rc), ("morse", k1, k2, D0, alpha, r0, rc),
+        ("eam", k1, k2) (uses `setfl`)."""
+        l = np.ascontiguousarray(box, dtype=np.float64)
+        self.L.oracle_set_box(self.o, _ptr(l), _ptr(np.ascontiguousarray(pbc, dtype=np.int32)),
+                              _ptr(np.ascontiguousarray(nc, dtype=np.int32)), _ptr(np.ascontiguousarray(cellh, dtype=np.float64)))
+        nk = len(kinds)
+        elem = -np.ones(nk, np.int32)
+        enames = []
+        eam_rc = None
+        if setfl is not None:
+            buf = C.create_string_buffer(1024)
+            rc = C.c_double(0)
+            ne = self.L.oracle_load_setfl(self.o, setfl.encode(), buf, 1024, C.byref(rc))
+            assert ne > 0, ne
+            enames = buf.value.decode().split()
+            eam_rc = rc.value
+        table = (PairT * (nk * nk))()
+        for p in pots:
+            k1, k2 = p[1], p[2]
+            for a, b in ((k1, k2), (k2, k1)):
+                t = table[a * nk + b]
+                if p[0] == "lj":
+                    t.cat = 1
+                    t.p[0], t.p[1], t.p[2] = 4.0 * p[4], p[3] * p[3], p[5] * p[5]
+                elif p[0] == "morse":
+                    t.cat = 3
+                    t.p[0], t.p[1], t.p[2], t.p[3] = p[3], p[4], p[5], p[6] * p[6]
+                else:
+                    t.cat = 2
+                    t.p[2] = eam_rc * eam_rc
+                    t.iloc = enames.index(kinds[a][0])
+                    t.jloc = enames.index(kinds[b][0])
+                    elem[a] = t.iloc
+                    elem[b] = t.jloc
+        mass = np.array([m / MASS_UNIT for _, m in kinds])
+        self.L.oracle_set_kinds(self.o, nk, _ptr(mass), _ptr(elem))
+        self.L.oracle_set_pairs(self.o, C.cast(table, P))
+
+    def upload(self, cell, x, v, kind, group, atomid, ncell):
+        counts = np.bincount(np.asarray(cell), minlength=ncell).astype(np.int32)
+        x = np.ascontiguousarray(x, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        kind = np.ascontiguousarray(kind, np.uint32)
+        group = np.ascontiguousarray(group, np.int32)
+        atomid = np.ascontiguousarray(atomid, np.uint32)
+        rc = self.L.oracle_upload(self.o, len(kind), _ptr(counts), _ptr(x), _ptr(v), _ptr(kind), _ptr(group),
+                                  _ptr(atomid))
+        assert rc == 0
+
+    def dump(self):
+        n = self.L.oracle_natoms(self.o)
+        out = dict(cell=np.zeros(n, np.int32), id=np.zeros(n, np.uint32), kind=np.zeros(n, np.uint32),
+                   group=np.zeros(n, np.int32), x=np.zeros((n, 3)), v=np.zeros((n, 3)), F=np.zeros((n, 3)),
+                   vaream=np.zeros(n))
+        self.L.oracle_download(self.o, _ptr(out["cell"]), _ptr(out["x"]), _ptr(out["v"]), _ptr(out["F"]),
+                               _ptr(out["vaream"]), _ptr(out["kind"]), _ptr(out["group"]), _ptr(out["id"]))
+        th = ThermoT()
+        self.L.oracle_get_thermo(self.o, C.byref(th))
+        out["pe"] = th.potential
+        return out
+
+    def set_state(self, x=None, v=None):
+        x = None if x is None else np.ascontiguousarray(x, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        self.L.oracle_set_state(self.o, _ptr(x), _ptr(v))
+
+    def refresh(self):
+        return self.L.oracle_refresh(self.o)
+
+    def forces(self, group=-1):
+        self.L.oracle_compute_forces(self.o, group)
+
+    def thermo(self, group=-1):
+        th = ThermoT()
+        self.L.oracle_thermo(self.o, group, C.byref(th))
+        return th
+
+    def get_thermo(self):
+        th = ThermoT()
+        self.L.oracle_get_thermo(self.o, C.byref(th))
+        return th
+
+    def vv(self, nsteps, dt, group=-1, thermostat=0, tau=1.0, T0=0.0):
+        return self.L.oracle_vv_steps(self.o, nsteps, dt, group, thermostat, tau, T0)
+
+    def errors(self):
+        return self.L.oracle_errors(self.o)

@@ -1,0 +1,106 @@
+"""CPU: the restated oracle (oracle/fmd_oracle.c) reproduces the golden
+vectors produced by the reference FMD library -- step-0 forces, energies,
+EAM F'(rho), the thermodynamic series, final positions and the exact cell
+order after refreshes.  This pins the oracle used by the GPU parity tests."""
+import os
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+import cases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+from fmd_gb300 import workloads  # noqa: E402
+import pyoracle  # noqa: E402
+
+
+def oracle_for_case(name, g, work, threads=1):
+    case = cases.CASES[name]
+    kinds = [(n, cases.MASS[n]) for n in case["names"]]
+    pots = []
+    setfl = None
+    for p in case["pots"]:
+        if p[0] == "eam_analytic":
+            setfl = os.path.join(work, "analytic.eam.alloy")
+            if not os.path.exists(setfl):
+                workloads.write_analytic_eam(setfl)
+            pots.append(("eam", p[1], p[2]))
+        else:
+            pots.append(p)
+    o = pyoracle.Oracle(threads=threads)
+    o.setup(case["box"], case["pbc"], g["nc"], g["cellh"], kinds, pots, setfl)
+    ids = g["s0_id"]
+    o.upload(g["s0_cell"], g["s0_x"], g["state_v"][ids], g["state_kind"][ids], g["state_group"][ids], ids,
+             int(np.prod(g["nc"])))
+    return o
+
+
+def run_oracle_case(name, threads=1):
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    case = cases.CASES[name]
+    r = case["run"]
+    grp, dt = r[1], r[2]
+    with tempfile.TemporaryDirectory() as work:
+        o = oracle_for_case(name, g, work, threads)
+    o.forces(grp)
+    d0 = o.dump()
+    thermostat = 1 if r[0] == "equilibrate" else 0
+    tau, T0 = (r[3], r[4]) if thermostat else (1.0, 0.0)
+    th = o.thermo(grp)
+    rows = [(0.0, th.temperature, th.kinetic + th.potential, th.kinetic)]
+    done = 0
+    while done < case["steps"]:
+        k = min(case["every"], case["steps"] - done)
+        assert o.vv(k, dt, grp, thermostat, tau, T0) == 0
+        done += k
+        th = o.get_thermo()
+        rows.append((done * dt, th.temperature, th.kinetic + th.potential, th.kinetic))
+    d1 = o.dump()
+    o.close()
+    return g, d0, d1, np.array(rows)
+
+
+@pytest.mark.parametrize("name", list(cases.CASES))
+def test_oracle_matches_reference(name):
+    g, d0, d1, rows = run_oracle_case(name)
+    np.testing.assert_array_equal(d0["id"], g["s0_id"])
+    fmax = np.abs(g["s0_F"]).max()
+    assert np.abs(d0["F"] - g["s0_F"]).max() <= 1e-12 * fmax
+    assert abs(d0["pe"] - float(g["s0_pe"])) <= 1e-12 * abs(float(g["s0_pe"]))
+    if name in ("eam", "hybrid"):
+        assert np.abs(d0["vaream"] - g["s0_vaream"]).max() <= 1e-12 * np.abs(g["s0_vaream"]).max()
+    gt = g["thermo"]
+    assert rows.shape[0] == gt.shape[0]
+    np.testing.assert_allclose(rows[:, 1:], gt[:, 1:], rtol=1e-10, atol=1e-10)
+    np.testing.assert_array_equal(d1["id"], g["s1_id"])
+    np.testing.assert_array_equal(d1["cell"], g["s1_cell"])
+    assert np.abs(d1["x"] - g["s1_x"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["lj", "morse_open"])
+def test_oracle_binning_order(name):
+    b = dict(np.load(os.path.join(GOLDEN, "bin_" + name + ".npz")))
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    with tempfile.TemporaryDirectory() as work:
+        o = oracle_for_case(name, g, work)
+    for r in range(1, int(b["rounds"]) + 1):
+        o.set_state(b["in%d_x" % r], None)
+        assert o.refresh() == 0
+        d = o.dump()
+        np.testing.assert_array_equal(d["id"], b["r%d_id" % r])
+        np.testing.assert_array_equal(d["cell"], b["r%d_cell" % r])
+        np.testing.assert_array_equal(d["x"], b["r%d_x" % r])
+        o.set_state(d["x"], None)
+    o.close()
+
+
+def test_oracle_threads_agree():
+    """The OpenMP variant (per-thread buffers) gives the same forces."""
+    g, d0, _, _ = run_oracle_case("eam", threads=1)
+    g2, e0, _, _ = run_oracle_case("eam", threads=4)
+    assert np.abs(d0["F"] - e0["F"]).max() <= 1e-13 * np.abs(d0["F"]).max()
