@@ -74,6 +74,55 @@ def summarize_clocks(samples):
             "samples": len(samples)}
 
 
+def numpy_state_cell_order(nc, cellh):
+    """The workload's atoms binned the way the reference distributes them:
+    cell = floor(x/cellh), insertion order kept inside each cell."""
+    from fmd_gb300 import workloads
+    w = WORKLOAD
+    x, v = workloads.fcc_state(*w["cells"], w["a"], w["T"], w["mass"], seed=w["seed"])
+    ic = np.floor(x / np.asarray(cellh)).astype(np.int64)
+    cell = ic[:, 2] + nc[2] * (ic[:, 1] + nc[1] * ic[:, 0])
+    order = np.argsort(cell, kind="stable")
+    n = len(x)
+    return (cell[order].astype(np.int32), x[order], v[order], np.zeros(n, np.uint32), np.zeros(n, np.int32),
+            order.astype(np.uint32))
+
+
+def eam_geometry():
+    w = WORKLOAD
+    box = [c * w["a"] for c in w["cells"]]
+    from fmd_gb300 import workloads
+    nc = [int(b / workloads.EAM_RC) for b in box]
+    cellh = [b / n for b, n in zip(box, nc)]
+    return box, nc, cellh
+
+
+def cpu_port_run(threads, target_s=12.0, max_steps=20):
+    """Time the CPU oracle port (restated reference algorithm, OpenMP with
+    per-thread buffers) on the same workload; returns (atom-steps/s, steps)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from fmd_gb300 import workloads
+    w = WORKLOAD
+    box, nc, cellh = eam_geometry()
+    with tempfile.TemporaryDirectory() as work:
+        setfl = workloads.write_analytic_eam(os.path.join(work, "analytic.eam.alloy"))
+        o = pyoracle.Oracle(threads=threads)
+        o.setup(box, [1, 1, 1], nc, cellh, [("Cu", w["mass"])], [("eam", 0, 0)], setfl)
+    cell, x, v, kind, group, ids = numpy_state_cell_order(nc, cellh)
+    o.upload(cell, x, v, kind, group, ids, int(np.prod(nc)))
+    o.forces(-1)
+    t0 = time.perf_counter()
+    o.vv(1, w["dt"])
+    t1 = time.perf_counter()
+    k = int(max(1, min(max_steps, target_s / max(t1 - t0, 1e-6))))
+    t2 = time.perf_counter()
+    o.vv(k, w["dt"])
+    t3 = time.perf_counter()
+    o.close()
+    return len(x) * k / (t3 - t2), k
+
+
 def make_system(lib, api, work, precision):
     from fmd_gb300 import workloads
     w = WORKLOAD
@@ -165,7 +214,30 @@ def run_ours(args):
         ck(L.fmdg_measure_fma_peak(dev, 0, C.byref(peak32)), "peak")
         errs = C.c_uint(0)
         L.fmdg_get_errors(dev, C.byref(errs), 0)
+        # end to end through the C-ABI with pinned host buffers
+        L.fmdg_host_alloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        L.fmdg_host_free.argtypes = [C.c_void_p]
+        L.fmdg_run_host.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int] + [C.c_void_p] * 6
+        nb = 3 * natoms * 8
+        bufs = [C.c_void_p() for _ in range(5)]
+        for k, b in enumerate(bufs):
+            ck(L.fmdg_host_alloc(C.byref(b), nb if k < 4 else natoms * 4), "pinned alloc")
+        th = (C.c_double * 8)()
+        ck(L.fmdg_run_host(dev, 0, dt, -1, None, None, bufs[0], bufs[1], bufs[4], th), "e2e prime")
+        xin, vin, xout, vout = bufs[0], bufs[1], bufs[2], bufs[3]
+        e2e_steps = max(3, args.steps)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ck(L.fmdg_run_host(dev, 1, dt, -1, xin, vin, xout, vout, bufs[4], th), "e2e step")
+            xin, xout = xout, xin
+            vin, vout = vout, vin
+        t1 = time.perf_counter()
+        e2e_value = natoms * e2e_steps / (t1 - t0)
+        for b in bufs:
+            L.fmdg_host_free(b)
         lib.fmd_free(md)
+    cores = os.cpu_count() or 1
+    cpu_value, cpu_steps = cpu_port_run(cores)
 
     ms_per_step = total_ms / args.steps
     value = natoms / (ms_per_step * 1e-3)
@@ -190,8 +262,37 @@ def run_ours(args):
                      "traffic": None},
         "clocks": clocks,
         "device_errors": errs.value,
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 2 * 3 * natoms * 8,
+                "d2h_bytes_per_step": 2 * 3 * natoms * 8 + natoms * 4 + 64,
+                "how": "fmdg_run_host: positions+velocities in from pinned host memory, one step, "
+                       "positions+velocities+atom ids+thermo record out; wall clock"},
+        "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cpu_steps} velocity-Verlet steps of the same 256000-atom EAM system "
+                                   "(restated reference algorithm, OpenMP, per-thread force buffers)"},
     }
     return out
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores: the
+    oracle port (the reference's own sources are not present on the GPU
+    host), all threads, same workload, metric and unit."""
+    cores = os.cpu_count() or 1
+    vals = []
+    for _ in range(max(1, min(args.steps, 3))):
+        v, k = cpu_port_run(cores, target_s=8.0, max_steps=10)
+        vals.append(v)
+    value = float(np.median(vals))
+    w = WORKLOAD
+    out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 0,
+           "steps": len(vals), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
+                                  "300 K, dt 1 fs, NVE", "atoms": int(np.prod(w["cells"])) * 4},
+           "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                            "sample": f"median of {len(vals)} timed samples of up to 10 steps each"},
+           "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
 
 
 def main():
@@ -205,7 +306,9 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
-        print(json.dumps({"impl": "reference", "unavailable": "CPU oracle port not built yet"}))
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
         return
     out = run_ours(args)
     print(json.dumps(out))

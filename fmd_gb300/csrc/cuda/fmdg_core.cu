@@ -597,6 +597,52 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
     return FMDG_OK;
 }
 
+extern "C" int fmdg_host_alloc(void **p, size_t bytes)
+{
+    FMDG_CK(cudaHostAlloc(p, bytes ? bytes : 1, cudaHostAllocDefault));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_host_free(void *p)
+{
+    FMDG_CK(cudaFreeHost(p));
+    return FMDG_OK;
+}
+
+// Host-buffer entry point: positions/velocities in, nsteps velocity-Verlet
+// steps, positions/velocities/atom ids (new order) and the thermo record out.
+// Host arrays are structure-of-arrays, 3 rows of n (the current atom count);
+// pinned buffers (fmdg_host_alloc) make the copies asynchronous.
+extern "C" int fmdg_run_host(fmdg_sys_t *s, int nsteps, double dt, int group, const double *x_in,
+                             const double *v_in, double *x_out, double *v_out, unsigned *id_out,
+                             fmdg_thermo_t *th_out)
+{
+    if (!s->atoms || !s->cats) return FMDG_E_STATE;
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    const size_t cap = s->g.cap, n = d.n;
+    if (n > 0)
+    {
+        const Side &S = s->g.side[d.cur];
+        if (x_in) FMDG_CK(cudaMemcpy2DAsync(S.x, cap * 8, x_in, n * 8, n * 8, 3, cudaMemcpyHostToDevice, s->stream));
+        if (v_in) FMDG_CK(cudaMemcpy2DAsync(S.v, cap * 8, v_in, n * 8, n * 8, 3, cudaMemcpyHostToDevice, s->stream));
+    }
+    if ((rc = fmdg_vv_steps(s, nsteps, dt, group, 0, 1.0, 0.0))) return rc;
+    if ((rc = read_dyn(s, &d))) return rc;
+    const size_t m = d.n;
+    if (m > 0)
+    {
+        const Side &T = s->g.side[d.cur];
+        if (x_out) FMDG_CK(cudaMemcpy2DAsync(x_out, m * 8, T.x, cap * 8, m * 8, 3, cudaMemcpyDeviceToHost, s->stream));
+        if (v_out) FMDG_CK(cudaMemcpy2DAsync(v_out, m * 8, T.v, cap * 8, m * 8, 3, cudaMemcpyDeviceToHost, s->stream));
+        if (id_out) FMDG_CK(cudaMemcpyAsync(id_out, T.atomid, m * 4, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (th_out) FMDG_CK(cudaMemcpyAsync(th_out, s->g.thermo, sizeof(fmdg_thermo_t), cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    return FMDG_OK;
+}
+
 extern "C" int fmdg_get_thermo(fmdg_sys_t *s, fmdg_thermo_t *out)
 {
     FMDG_CK(cudaMemcpyAsync(out, s->g.thermo, sizeof(fmdg_thermo_t), cudaMemcpyDeviceToHost, s->stream));

@@ -132,6 +132,17 @@ int fmdg_get_thermo(fmdg_sys_t *s, fmdg_thermo_t *out);
 /* sticky error bits since the last clear; clear=1 resets them */
 int fmdg_get_errors(fmdg_sys_t *s, unsigned *bits, int clear);
 
+/* --- host-buffer path ------------------------------------------------ */
+/* pinned host memory for the host-buffer path */
+int fmdg_host_alloc(void **p, size_t bytes);
+int fmdg_host_free(void *p);
+/* positions/velocities in (structure of arrays: 3 rows of n, n = current
+   atom count, current order), nsteps velocity-Verlet steps
+   (src/integrators.c:227-264 without events), positions/velocities/atom ids
+   in the new order and the thermo record out; any pointer may be NULL */
+int fmdg_run_host(fmdg_sys_t *s, int nsteps, double dt, int group, const double *x_in, const double *v_in,
+                  double *x_out, double *v_out, unsigned *id_out, fmdg_thermo_t *th_out);
+
 /* --- whole-system edits after distribution -------------------------- */
 int fmdg_add_velocity(fmdg_sys_t *s, int group, const double dv[3]);
 int fmdg_change_group(fmdg_sys_t *s, int old_group, int new_group);
