@@ -237,7 +237,10 @@ def run_ours(args):
             L.fmdg_host_free(b)
         lib.fmd_free(md)
     cores = os.cpu_count() or 1
-    cpu_value, cpu_steps = cpu_port_run(cores)
+    if args.skip_cpu:
+        cpu_value, cpu_steps = None, 0
+    else:
+        cpu_value, cpu_steps = cpu_port_run(cores)
 
     ms_per_step = total_ms / args.steps
     value = natoms / (ms_per_step * 1e-3)
@@ -302,6 +305,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
