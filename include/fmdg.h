@@ -143,6 +143,25 @@ int fmdg_host_free(void *p);
 int fmdg_run_host(fmdg_sys_t *s, int nsteps, double dt, int group, const double *x_in, const double *v_in,
                   double *x_out, double *v_out, unsigned *id_out, fmdg_thermo_t *th_out);
 
+/* --- allocation-free pair forces ------------------------------------ */
+/* No counterpart in the reference.  Binary64 LJ / Morse forces and the
+   total potential energy for callers that cannot let a library allocate
+   device memory (work being recorded into a CUDA graph, hosts that own all
+   device memory through their own pool, serving loops that must not incur
+   cudaMalloc's implicit synchronisation).  Every input and output is the
+   caller's device memory: x (structure of arrays, 3 rows of n), kind[n],
+   cell_start[ncell+1] and cell_of[n] of atoms sorted by cell (flat cell
+   index z + nz*(y + ny*x)); F (3 rows of n) and *pe (one double) receive the
+   result.  pairs: host table of nkinds*nkinds entries (LJ or Morse only,
+   nkinds <= 4).  stream: a cudaStream_t or NULL.  Scratch is a fixed
+   512 KiB file-scope device array: at most 1048576 atoms per call (larger
+   n returns FMDG_E_ARG with a message); the first call on a device looks up
+   that array's address and should come before any stream capture; calls
+   that overlap on the GPU share the array and race. */
+int fmdg_pair_forces_noalloc(int n, const int nc[3], const int pbc[3], const double l[3], int nkinds,
+                             const fmdg_pair_t *pairs, const double *x, const unsigned *kind,
+                             const int *cell_start, const int *cell_of, double *F, double *pe, void *stream);
+
 /* --- whole-system edits after distribution -------------------------- */
 int fmdg_add_velocity(fmdg_sys_t *s, int group, const double dv[3]);
 int fmdg_change_group(fmdg_sys_t *s, int old_group, int new_group);
