@@ -321,9 +321,12 @@ __global__ void k_bin_scatter(Geo g)
     T.cell_of[idx] = D;
 }
 
-__global__ void k_bin_flip(Geo g)
+// swaps sides after a refresh that moved atoms; advances the device copy of
+// the simulation time by one step (src/integrators.c:203, :256)
+__global__ void k_bin_flip(Geo g, double advance)
 {
     Dyn *dyn = g.dyn;
+    dyn->time += advance;
     if (dyn->any_move)
     {
         dyn->cur ^= 1;
@@ -347,7 +350,7 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
     k_bin_cells<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(g);
     k_bin_arrivals<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(g);
     k_bin_scatter<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(g);
-    k_bin_flip<<<1, 1, 0, st>>>(g);
+    k_bin_flip<<<1, 1, 0, st>>>(g, mode == FMDG_REFRESH_ONLY ? 0.0 : dt);
     s->launches += 6;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;

@@ -173,6 +173,7 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     if (rc) return rc;
     FMDG_CK(cudaMemset(s->g.dyn, 0, sizeof(Dyn)));
     FMDG_CK(cudaMemset(s->g.thermo, 0, sizeof(fmdg_thermo_t)));
+    s->ttm_turi = -1;
     *out = s;
     return FMDG_OK;
 }
@@ -188,6 +189,15 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     dfree((void *)s->g.erhoDD); dfree((void *)s->g.ephi); dfree((void *)s->g.ephiDD);
     dfree((void *)s->g.pk_rho); dfree((void *)s->g.pk_phi); dfree((void *)s->g.pk_F);
     dfree((void *)s->g.pkf_rho); dfree((void *)s->g.pkf_phi); dfree((void *)s->g.pkf_F);
+    for (int k = 0; k < s->nturi; k++)
+    {
+        DTuri &t = s->turi[k];
+        dfree(t.acc); dfree(t.tacc); dfree(t.mass); dfree(t.vcm); dfree(t.Ti); dfree(t.num);
+        dfree(t.Te); dfree(t.Te2); dfree(t.xi); dfree(t.Ke); dfree(t.Ce); dfree(t.Gc); dfree(t.srcz);
+        dfree(t.Te_pre);
+        dfree((void *)t.p.T_C); dfree((void *)t.p.Ct); dfree((void *)t.p.C_DD);
+        dfree((void *)t.p.T_G); dfree((void *)t.p.Gt); dfree((void *)t.p.G_DD);
+    }
     dfree(s->g.dyn); dfree(s->g.thermo);
     dfree(s->l2buf);
     cudaEventDestroy(s->ev0);
@@ -422,10 +432,14 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     FMDG_CK(cudaMemset(g.F, 0, 3 * (size_t)cap * 8));
     FMDG_CK(cudaMemset(g.vaream, 0, (size_t)cap * 8));
     Dyn d;
+    FMDG_CK(cudaMemcpy(&d, g.dyn, sizeof d, cudaMemcpyDeviceToHost));
+    const double keep_time = d.time, keep_dt = d.dt;
     memset(&d, 0, sizeof d);
     d.cur = 0;
     d.n = n;
     d.lambda = 1.0;
+    d.time = keep_time;
+    d.dt = keep_dt;
     FMDG_CK(cudaMemcpy(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));
     s->atoms = true;
     return FMDG_OK;
@@ -521,7 +535,23 @@ static int vv_step_launches(fmdg_sys_t *s, double dt, int group, int thermostat,
     if (rc) return rc;
     rc = fmdg_launch_forces(s, group, 1, dt);
     if (rc) return rc;
-    return fmdg_launch_reduce(s, thermostat, dt, tau, T0);
+    rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0);
+    if (rc) return rc;
+    // fields of every turi after the step (src/integrators.c:258-259)
+    for (int k = 0; k < s->nturi; k++)
+        if ((rc = fmdg_launch_turi(s, k, dt))) return rc;
+    return FMDG_OK;
+}
+
+// symplectic Euler under TTM (src/integrators.c:129-179, 198-224)
+static int se_step_launches(fmdg_sys_t *s, double dt, int group)
+{
+    int rc = fmdg_launch_refresh(s, FMDG_REFRESH_SE, dt, group, 0);
+    if (rc) return rc;
+    for (int k = 0; k < s->nturi; k++)
+        if ((rc = fmdg_launch_turi(s, k, dt))) return rc;
+    if ((rc = fmdg_launch_forces(s, group, 0, dt))) return rc;
+    return fmdg_launch_reduce(s, 0, dt, 1.0, 0.0);
 }
 
 // Before the first step of a run the caller computes the forces of the
@@ -568,8 +598,9 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
         }
         return FMDG_OK;
     }
-    const bool same = s->graph_key_valid && s->graph_dt == dt && s->graph_group == active_group &&
-                      s->graph_thermo == thermostat && s->graph_tau == tau && s->graph_T0 == T0;
+    const bool same = s->graph_key_valid && s->graph_mode == 0 && s->graph_dt == dt &&
+                      s->graph_group == active_group && s->graph_thermo == thermostat && s->graph_tau == tau &&
+                      s->graph_T0 == T0;
     if (!same)
     {
         invalidate_graph(s);
@@ -587,13 +618,213 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
         s->graph_key_valid = 1;
         s->graph_dt = dt; s->graph_group = active_group; s->graph_thermo = thermostat;
         s->graph_tau = tau; s->graph_T0 = T0;
+        s->graph_mode = 0;
         // kernels per captured step
         const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
         // memset node + 6 refresh kernels + 2 list kernels + density + force + reduce
         s->graph_steps = 7 + 2 + (eam ? 1 : 0) + 1 + 1;
+        for (int k = 0; k < s->nturi; k++) s->graph_steps += 5 + (s->turi[k].ttm ? 1 : 0);
     }
     for (int k = 0; k < nsteps; k++) FMDG_CK(cudaGraphLaunch(s->graph, s->stream));
     s->launches += (long long)nsteps * (s->graph_steps - 1);  // memset node is not a kernel
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_se_steps(fmdg_sys_t *s, int nsteps, double dt, int active_group)
+{
+    if (!s->atoms || !s->cats) return FMDG_E_STATE;
+    if (nsteps <= 0) return FMDG_OK;
+    if (s->profiling)
+    {
+        for (int k = 0; k < nsteps; k++)
+        {
+            int rc = se_step_launches(s, dt, active_group);
+            if (rc) return rc;
+        }
+        return FMDG_OK;
+    }
+    const bool same = s->graph_key_valid && s->graph_mode == 1 && s->graph_dt == dt && s->graph_group == active_group;
+    if (!same)
+    {
+        invalidate_graph(s);
+        cudaGraph_t graph;
+        FMDG_CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        const long long before = s->launches;
+        int rc = se_step_launches(s, dt, active_group);
+        cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fmdg_fail("cudaStreamEndCapture", e);
+        s->graph_steps = (int)(s->launches - before) + 1;
+        s->launches = before;
+        e = cudaGraphInstantiate(&s->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fmdg_fail("cudaGraphInstantiate", e);
+        s->graph_key_valid = 1;
+        s->graph_mode = 1;
+        s->graph_dt = dt;
+        s->graph_group = active_group;
+    }
+    for (int k = 0; k < nsteps; k++) FMDG_CK(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += (long long)nsteps * (s->graph_steps - 1);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_set_time(fmdg_sys_t *s, double time, double dt)
+{
+    Dyn d;
+    int rc = read_dyn(s, &d);
+    if (rc) return rc;
+    d.time = time;
+    d.dt = dt;
+    FMDG_CK(cudaMemcpy(s->g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_turi_add(fmdg_sys_t *s, const int dims_local[3], const int g2l[3], const double tcellh[3],
+                             double starttime, double stoptime, int *handle)
+{
+    if (s->nturi >= FMDG_MAXT) return fmdg_set_error("fmdg_turi_add: at most 4 turies per system");
+    DTuri &t = s->turi[s->nturi];
+    memset(&t, 0, sizeof t);
+    long long nc = 1;
+    for (int d = 0; d < 3; d++)
+    {
+        if (dims_local[d] < 1 || !(tcellh[d] > 0)) return fmdg_set_error("fmdg_turi_add: bad geometry");
+        t.dims[d] = dims_local[d];
+        t.g2l[d] = g2l[d];
+        t.tcellh[d] = tcellh[d];
+        t.inv_tcellh[d] = 1.0 / tcellh[d];
+        nc *= dims_local[d];
+    }
+    if (nc > (1 << 22)) return fmdg_set_error("fmdg_turi_add: too many turi cells");
+    t.ncells = (int)nc;
+    t.tcell_volume = tcellh[0] * tcellh[1] * tcellh[2];
+    t.starttime = starttime;
+    t.stoptime = stoptime;
+    int rc;
+    if ((rc = dalloc(&t.acc, 5 * nc)) || (rc = dalloc(&t.tacc, nc)) || (rc = dalloc(&t.mass, nc)) ||
+        (rc = dalloc(&t.vcm, 3 * nc)) || (rc = dalloc(&t.Ti, nc)) || (rc = dalloc(&t.num, nc)))
+        return rc;
+    FMDG_CK(cudaMemset(t.num, 0, nc * sizeof(unsigned)));
+    FMDG_CK(cudaMemset(t.mass, 0, nc * sizeof(double)));
+    FMDG_CK(cudaMemset(t.vcm, 0, 3 * nc * sizeof(double)));
+    FMDG_CK(cudaMemset(t.Ti, 0, nc * sizeof(double)));
+    *handle = s->nturi++;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, const fmdg_ttm_params_t *p)
+{
+    if (turi < 0 || turi >= s->nturi) return fmdg_set_error("fmdg_ttm_setup: bad turi");
+    DTuri &t = s->turi[turi];
+    if (t.dims[0] != 1 || t.dims[1] != 1) return fmdg_set_error("fmdg_ttm_setup: 1-D grids along z only");
+    if (p->type != 1 && p->type != 2) return fmdg_set_error("fmdg_ttm_setup: type 1 or 2");
+    if (p->ratio < 1) return fmdg_set_error("fmdg_ttm_setup: timestep ratio must be positive");
+    if (itc_lo < 1 || itc_hi > t.dims[2] - 1 || itc_lo >= itc_hi) return fmdg_set_error("fmdg_ttm_setup: range");
+    const int nz = t.dims[2];
+    int rc;
+    if (!t.Te)
+    {
+        if ((rc = dalloc(&t.Te, nz)) || (rc = dalloc(&t.Te2, nz)) || (rc = dalloc(&t.xi, nz)) ||
+            (rc = dalloc(&t.Ke, nz)) || (rc = dalloc(&t.Ce, nz)) || (rc = dalloc(&t.Gc, nz)) ||
+            (rc = dalloc(&t.srcz, nz)) || (rc = dalloc(&t.Te_pre, nz)))
+            return rc;
+        std::vector<double> m1(nz, -1.0), z0(nz, 0.0);
+        FMDG_CK(cudaMemcpy(t.Te, m1.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.Te2, m1.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.Te_pre, m1.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.xi, z0.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.Ke, z0.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.Ce, z0.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(t.Gc, z0.data(), nz * 8, cudaMemcpyHostToDevice));
+    }
+    dfree((void *)t.p.T_C); dfree((void *)t.p.Ct); dfree((void *)t.p.C_DD);
+    dfree((void *)t.p.T_G); dfree((void *)t.p.Gt); dfree((void *)t.p.G_DD);
+    TtmParams q;
+    memset(&q, 0, sizeof q);
+    q.type = p->type; q.ratio = p->ratio; q.min_atoms = p->min_atoms; q.nC = p->nC; q.nG = p->nG;
+    q.C_gamma = p->C_gamma; q.K = p->K; q.G = p->G; q.dz2 = p->dz2; q.frontsurf = p->frontsurf;
+    q.laser_t0 = p->laser_t0; q.laser_tdiff = p->laser_tdiff; q.laser_m_2sig2_inv = p->laser_m_2sig2_inv;
+    q.laser_m_absdepth_inv = p->laser_m_absdepth_inv; q.laser_factor = p->laser_factor;
+    q.Kzh_v2 = p->Kzh_v2; q.Kzh_A = p->Kzh_A; q.Kzh_B = p->Kzh_B;
+    if (p->type == 2)
+    {
+        if (p->nC < 2 || p->nG < 2 || !p->T_C || !p->Ct || !p->C_DD || !p->T_G || !p->Gt || !p->G_DD)
+            return fmdg_set_error("fmdg_ttm_setup: type 2 needs C(Te) and G(Te) tables");
+        auto up = [&](const double *h, int n, const double **d) -> int {
+            int r = dalloc((double **)d, n);
+            if (r) return r;
+            FMDG_CK(cudaMemcpy((void *)*d, h, (size_t)n * 8, cudaMemcpyHostToDevice));
+            return FMDG_OK;
+        };
+        if ((rc = up(p->T_C, p->nC, &q.T_C)) || (rc = up(p->Ct, p->nC, &q.Ct)) || (rc = up(p->C_DD, p->nC, &q.C_DD)) ||
+            (rc = up(p->T_G, p->nG, &q.T_G)) || (rc = up(p->Gt, p->nG, &q.Gt)) || (rc = up(p->G_DD, p->nG, &q.G_DD)))
+            return rc;
+    }
+    t.p = q;
+    t.ttm = 1;
+    t.itc_lo = itc_lo;
+    t.itc_hi = itc_hi;
+    s->ttm_turi = turi;
+    Geo &g = s->g;
+    g.ttm_on = 1;
+    g.ttm_g2l_z = t.g2l[2];
+    g.ttm_nz = nz;
+    g.ttm_tcellh_z = t.tcellh[2];
+    g.ttm_inv_tcellh_z = t.inv_tcellh[2];
+    g.ttm_start = t.starttime;
+    g.ttm_stop = t.stoptime;
+    g.ttm_xi = t.xi;
+    g.ttm_vcm = t.vcm;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_ttm_set_te(fmdg_sys_t *s, int turi, const double *Te)
+{
+    if (turi < 0 || turi >= s->nturi || !s->turi[turi].Te) return fmdg_set_error("fmdg_ttm_set_te: no TTM");
+    DTuri &t = s->turi[turi];
+    FMDG_CK(cudaMemcpy(t.Te, Te, (size_t)t.dims[2] * 8, cudaMemcpyHostToDevice));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_turi_download(fmdg_sys_t *s, int turi, unsigned *num, double *mass, double *vcm, double *Ti,
+                                  double *Te, double *xi)
+{
+    if (turi < 0 || turi >= s->nturi) return fmdg_set_error("fmdg_turi_download: bad turi");
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    DTuri &t = s->turi[turi];
+    const size_t nc = t.ncells;
+    if (num) FMDG_CK(cudaMemcpy(num, t.num, nc * 4, cudaMemcpyDeviceToHost));
+    if (mass) FMDG_CK(cudaMemcpy(mass, t.mass, nc * 8, cudaMemcpyDeviceToHost));
+    if (vcm) FMDG_CK(cudaMemcpy(vcm, t.vcm, 3 * nc * 8, cudaMemcpyDeviceToHost));
+    if (Ti) FMDG_CK(cudaMemcpy(Ti, t.Ti, nc * 8, cudaMemcpyDeviceToHost));
+    if (t.Te)
+    {
+        if (Te) FMDG_CK(cudaMemcpy(Te, t.Te, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
+        if (xi) FMDG_CK(cudaMemcpy(xi, t.xi, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
+    }
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_ttm_download_te(fmdg_sys_t *s, int turi, int presolve, double *Te)
+{
+    if (turi < 0 || turi >= s->nturi || !s->turi[turi].Te) return fmdg_set_error("fmdg_ttm_download_te: no TTM");
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    DTuri &t = s->turi[turi];
+    FMDG_CK(cudaMemcpy(Te, presolve ? t.Te_pre : t.Te, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
+    return FMDG_OK;
+}
+
+extern "C" int fmdg_turi_update(fmdg_sys_t *s, double dt)
+{
+    if (!s->atoms) return FMDG_E_STATE;
+    for (int k = 0; k < s->nturi; k++)
+    {
+        int rc = fmdg_launch_turi(s, k, dt);
+        if (rc) return rc;
+    }
     return FMDG_OK;
 }
 

@@ -555,6 +555,26 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
                 pe = ac.sum[3];
             }
         }
+        if (active && g.ttm_on)
+        {
+            // TTM friction (src/forces.c:292-330, 1-D): F_z += xi m (v_z - vcm_z)
+            const double time = dyn->time, hdt = dyn->dt / 2.0;
+            if ((time >= g.ttm_start - hdt) && ((time < g.ttm_stop + hdt) || g.ttm_stop < g.ttm_start))
+            {
+                const double z = S.x[2 * (size_t)cap + i];
+                const double q = z * g.ttm_inv_tcellh_z;
+                const double r = rint(q);
+                int it = (fabs(q - r) <= 1e-9 * fmax(1.0, fabs(q))) ? (int)__ddiv_rn(z, g.ttm_tcellh_z) : (int)q;
+                it += g.ttm_g2l_z;
+                if (it >= 0 && it < g.ttm_nz)
+                {
+                    const double m = sp.mass[ki];
+                    f[2] += g.ttm_xi[it] * m * (S.v[2 * (size_t)cap + i] - g.ttm_vcm[3 * it + 2]);
+                }
+                else
+                    atomic_or_err(dyn, FMDG_ERRBIT_TTM);
+            }
+        }
         for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
         acc[0] = pe;
         if (active)

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "fmdg.h"
+#include "fmdg_turi.cuh"
 
 #define FMDG_MAXK 8            // atom kinds per system
 #define FMDG_MAXE 4            // EAM elements per system
@@ -31,7 +32,8 @@ struct Dyn
     unsigned err;       // sticky error bits (FMDG_ERRBIT_*)
     int pad;
     double lambda;      // Berendsen scale for the next start step
-    double time;
+    double time;        // simulation time (advanced by every step)
+    double dt;          // time step of the current run (turi windows)
 };
 
 struct Side
@@ -83,6 +85,11 @@ struct Geo   // passed by value to kernels
     const double *eF, *eFDD, *erho, *erhoDD, *ephi, *ephiDD;
     int has_eam;
     int prec;
+    // TTM friction term (src/forces.c:292-330), 1-D along z
+    int ttm_on;
+    int ttm_g2l_z, ttm_nz;
+    double ttm_tcellh_z, ttm_inv_tcellh_z, ttm_start, ttm_stop;
+    const double *ttm_xi, *ttm_vcm;
     // reductions
     double *partials;             // per block: 8 doubles
     fmdg_thermo_t *thermo;
@@ -114,6 +121,11 @@ struct fmdg_sys
     int graph_group, graph_thermo, graph_steps;
     void *l2buf;
     size_t l2bytes;
+    // continuum grids
+    DTuri turi[FMDG_MAXT];
+    int nturi;
+    int ttm_turi;                 // index of the TTM turi or -1
+    int graph_mode;               // 0 velocity Verlet, 1 symplectic Euler
 };
 
 // ---- helpers shared by the translation units --------------------------------
@@ -128,6 +140,7 @@ int fmdg_set_error(const char *msg);
 
 // kernel launch wrappers (defined in their translation units)
 int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int thermostat);
+int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt);
 int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt);
 int fmdg_launch_density(fmdg_sys_t *s, int group);
 int fmdg_launch_nlist(fmdg_sys_t *s);

@@ -39,7 +39,7 @@ static bool any_timer_due(const fmd_t *md, double t)
     return false;
 }
 
-static void send_timer_events(fmd_t *md)
+void _fmdh_send_timer_events(fmd_t *md)
 {
     for (int i = 0; i < md->timers_num; i++)
         if (timer_due(md, &md->timers[i], md->time))
@@ -51,7 +51,7 @@ static void send_timer_events(fmd_t *md)
 }
 
 /* device error bits become the reference's error events */
-static void check_device_errors(fmd_t *md)
+void _fmdh_check_device_errors(fmd_t *md)
 {
     unsigned bits = 0;
     if (!_fmdh_dev_ok(md, fmdg_get_errors(md->dev, &bits, 1), "fmdg_get_errors")) return;
@@ -63,7 +63,10 @@ static void check_device_errors(fmd_t *md)
     if (bits & FMDG_ERRBIT_INTERNAL)
         FMD_ERR(md, FMD_ERR_FUNCTION_FAILED, true, "device engine index check failed");
     if (bits & FMDG_ERRBIT_TTM)
-        FMD_ERR(md, FMD_ERR_UNEXPECTED_POSITION, true, "atom outside the TTM grid");
+        FMD_ERR(md, FMD_ERR_UNEXPECTED_POSITION, true, "atom outside the turi grid");
+    if (bits & FMDG_ERRBIT_TTM_TABLE)
+        FMD_ERR(md, FMD_ERR_OUTSIDE_REAL_INTERVAL, true,
+                "electron temperature outside the tabulated interval of the TTM");
 }
 
 static void set_active_group(fmd_t *md, int GroupID)
@@ -102,13 +105,19 @@ static void vv_integrate(fmd_t *md, double duration, bool thermostat)
     const double dt = md->timestep;
     const double tau = thermostat ? md->BerendsenThermostatParam : 1.0;
     const double T0 = thermostat ? md->DesiredTemperature : 0.0;
+    if (md->turies_num > 0)
+    {
+        if (!_fmdh_prepare_turies(md)) return;
+        if (!_fmdh_dev_ok(md, fmdg_set_time(md->dev, md->time, dt), "fmdg_set_time")) return;
+    }
     if (!initial_forces(md)) return;
+    if (md->turies_num > 0 && !_fmdh_dev_ok(md, fmdg_turi_update(md->dev, dt), "fmdg_turi_update")) return;
     if (thermostat &&
         !_fmdh_dev_ok(md, fmdg_prepare_thermostat(md->dev, md->ActiveGroup, dt, tau, T0), "thermostat"))
         return;
     if (md->turies_num > 0) _fmdh_turies_update(md, true, true, true);
-    check_device_errors(md);
-    if (md->EventHandler != NULL) send_timer_events(md);
+    _fmdh_check_device_errors(md);
+    if (md->EventHandler != NULL) _fmdh_send_timer_events(md);
     while (md->time < start + duration)
     {
         int k = 0;
@@ -130,8 +139,8 @@ static void vv_integrate(fmd_t *md, double duration, bool thermostat)
         md->thermo_pending = true;
         md->KineticEnergyUpdated = true;
         if (md->turies_num > 0) _fmdh_turies_update(md, true, true, true);
-        check_device_errors(md);
-        if (md->EventHandler != NULL) send_timer_events(md);
+        _fmdh_check_device_errors(md);
+        if (md->EventHandler != NULL) _fmdh_send_timer_events(md);
     }
 }
 

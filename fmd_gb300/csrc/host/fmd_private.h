@@ -177,6 +177,11 @@ void _fmdh_turies_free(fmd_t *md);
 void _fmdh_turies_update(fmd_t *md, bool xupd, bool vupd, bool fupd);
 void _fmdh_ttm_get_ready(fmd_t *md);
 void _fmdh_se_integrate(fmd_t *md, double duration);
+bool _fmdh_prepare_turies(fmd_t *md);
+
+/* fmd_dync.c */
+void _fmdh_send_timer_events(fmd_t *md);
+void _fmdh_check_device_errors(fmd_t *md);
 
 /* rng (fmd_matter.c) */
 double _fmdh_rng_uniform(fmd_t *md, unsigned long long *state);

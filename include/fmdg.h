@@ -37,6 +37,7 @@ extern "C" {
 #define FMDG_ERRBIT_RHO_RANGE  0x2  /* EAM density beyond the F(rho) table: src/eam.c:168-171 */
 #define FMDG_ERRBIT_TTM        0x4  /* TTM turi-cell index outside the grid */
 #define FMDG_ERRBIT_INTERNAL   0x8  /* an internal index check failed (the access was skipped) */
+#define FMDG_ERRBIT_TTM_TABLE  0x10 /* electron temperature outside a TTM table: src/ttm.c:162-183 */
 
 /* pair categories: values of the reference's potcat_t (src/potential.h:26-32) */
 #define FMDG_POT_NONE  0
@@ -131,6 +132,50 @@ int fmdg_prepare_thermostat(fmdg_sys_t *s, int active_group, double dt, double t
 int fmdg_get_thermo(fmdg_sys_t *s, fmdg_thermo_t *out);
 /* sticky error bits since the last clear; clear=1 resets them */
 int fmdg_get_errors(fmdg_sys_t *s, unsigned *bits, int clear);
+
+/* --- continuum grids and the two-temperature model -------------------- */
+/* Parameters of a 1-D TTM solver (src/ttm.h:35-90) in internal units
+   (eV, A, ps, K); table pointers are host arrays copied by fmdg_ttm_setup. */
+typedef struct
+{
+    int type;                /* 1: C = gamma Te, constant K, G; 2: tabulated C, G, Zhigilei K */
+    int ratio;               /* MD steps / electron substeps (timestep_ratio) */
+    unsigned min_atoms;      /* cells with fewer atoms are deactivated */
+    int nC, nG;
+    int pad;
+    double C_gamma, K, G, dz2, frontsurf;
+    double laser_t0, laser_tdiff, laser_m_2sig2_inv, laser_m_absdepth_inv, laser_factor;
+    double Kzh_v2, Kzh_A, Kzh_B;
+    const double *T_C, *Ct, *C_DD, *T_G, *Gt, *G_DD;
+} fmdg_ttm_params_t;
+
+/* a turi grid (src/turi.c:648-738): local dimensions incl. margins,
+   itc_local = (int)(x/tcellh) + g2l, active in [starttime, stoptime] */
+int fmdg_turi_add(fmdg_sys_t *s, const int dims_local[3], const int g2l[3], const double tcellh[3],
+                  double starttime, double stoptime, int *handle);
+/* attach the 1-D TTM electron solver to turi `turi` along z (interior
+   cells [itc_lo, itc_hi)); its xi and vcm drive the friction term */
+int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, const fmdg_ttm_params_t *p);
+/* electron temperature of every local cell (margins included) */
+int fmdg_ttm_set_te(fmdg_sys_t *s, int turi, const double *Te);
+/* per-cell fields of turi `turi` (local cells incl. margins); any output may
+   be NULL: num, mass (internal units), vcm (3 per cell), Ti, Te, xi */
+int fmdg_turi_download(fmdg_sys_t *s, int turi, unsigned *num, double *mass, double *vcm, double *Ti,
+                       double *Te, double *xi);
+/* electron temperature of every local cell: presolve=1 gives the state after
+   cell activation and before the substeps of the last update (what the
+   reference's Te field holds during its field-update event), 0 the state
+   after the substeps */
+int fmdg_ttm_download_te(fmdg_sys_t *s, int turi, int presolve, double *Te);
+/* simulation time and time step the device uses for turi windows, the
+   laser source and the friction term; steps advance the time by dt */
+int fmdg_set_time(fmdg_sys_t *s, double time, double dt);
+/* field update of every turi at the current time (src/turi.c:1627-1665):
+   mass, vcm, number, temperature; then the TTM solver */
+int fmdg_turi_update(fmdg_sys_t *s, double dt);
+/* symplectic-Euler steps under TTM coupling (src/integrators.c:129-225):
+   kick-drift, refresh, time += dt, turi updates, forces + friction term */
+int fmdg_se_steps(fmdg_sys_t *s, int nsteps, double dt, int active_group);
 
 /* --- host-buffer path ------------------------------------------------ */
 /* pinned host memory for the host-buffer path */

@@ -66,6 +66,30 @@ def _group_state():
     return s
 
 
+def _ttm_state():
+    x, v = workloads.fcc_state(6, 6, 16, 3.615, 300.0, MASS["Cu"], seed=41, origin=(0.0, 0.0, 8 * 3.615), disp=0.03)
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
+def _custom_state():
+    x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
+    v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
+    return dict(names=["Ar"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
+def write_ttm_tables(work):
+    """Synthetic type-2 tables (same two-column layout and units as the
+    reference's table files: T in 1e4 K; C in 1e5 J/m^3K; G in 1e17 W/m^3K)."""
+    T = np.linspace(0.0, 5.0, 201)                  # 0 .. 50 000 K
+    C = 96.6 * (T * 1e4) / 1e5 * (1.0 / (1.0 + 0.05 * T))
+    G = 1.0 + 0.3 * np.tanh(T - 1.0)
+    pc = os.path.join(work, "Ce_syn.dat")
+    pg = os.path.join(work, "G_syn.dat")
+    np.savetxt(pc, np.stack([T, C], 1), fmt="%.10e")
+    np.savetxt(pg, np.stack([T, G], 1), fmt="%.10e")
+    return pc, pg
+
+
 CASES = {
     "lj": dict(box=(52.6, 52.6, 52.6), pbc=(1, 1, 1), names=["Ar"],
                pots=[("lj", 0, 0, 3.405, 0.0104, 8.5125)], state=_lj_state,
@@ -85,6 +109,19 @@ CASES = {
     "eam": dict(box=(28.92, 28.92, 28.92), pbc=(1, 1, 1), names=["Cu"],
                 pots=[("eam_analytic", 0, 0)], state=_eam_state,
                 run=("integrate", -1, 0.001), steps=60, every=10),
+    "ttm1": dict(box=(21.69, 21.69, 144.6), pbc=(1, 1, 0), names=["Cu"], pots=[("eam_analytic", 0, 0)],
+                 state=_ttm_state, run=("integrate", -1, 0.001), steps=30, every=10,
+                 turi=dict(cat=1, dims=(1, 1, 20), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100, frac=0.1,
+                           laser=(500.0, 0.0, 0.02e-12, 100e-15, 15e-9))),
+    "ttm2": dict(box=(21.69, 21.69, 144.6), pbc=(1, 1, 0), names=["Cu"], pots=[("eam_analytic", 0, 0)],
+                 state=_ttm_state, run=("integrate", -1, 0.001), steps=30, every=10,
+                 turi=dict(cat=2, dims=(1, 1, 20), zhigilei=(1.57e6, 2.66e6, 2.41e11), Te=300.0, ratio=100,
+                           frac=0.1, laser=(2000.0, 0.1, 0.02e-12, 100e-15, 15e-9))),
+    "turi_custom": dict(box=(42.08, 42.08, 42.08), pbc=(1, 1, 1), names=["Ar"],
+                        pots=[("lj", 0, 0, 3.405, 0.0104, 8.5125)], state=_custom_state,
+                        run=("integrate", -1, 0.002), steps=20, every=10,
+                        turi=dict(cat=0, dims=(2, 2, 3),
+                                  fields=["TEMPERATURE", "NUMBER_DENSITY", "VCM", "MASS"])),
     "hybrid": dict(box=(40.0, 30.0, 30.0), pbc=(1, 1, 1), names=["Cu", "Ar"],
                    pots=[("eam_analytic", 0, 0), ("lj", 1, 1, 3.4, 0.0104, 8.5),
                          ("lj", 0, 1, 2.87, 0.0652, 7.175)], state=_hybrid_state,
@@ -119,7 +156,39 @@ def setup(lib: api.Lib, name: str, workdir: str, state: dict | None = None):
     api.write_state(spath, 0.0, case["box"], case["pbc"], state["names"], state["kind"],
                     state["group"], state["x"], state["v"])
     lib.fmd_io_loadState(md, spath.encode(), False)
+    if "turi" in case:
+        # the TTM set-up reads the group's atom count (src/ttm.c:77), which
+        # the reference only knows once a temperature has been computed
+        lib.fmd_matt_getTemperature(md)
+        # after the matter exists: the reference builds its local grid here
+        setup_turi(lib, md, case["turi"], workdir)
     return md, state
+
+
+def setup_turi(lib, md, tu, workdir):
+    """Turi + TTM parameters through the fmd.h API; stores the handle."""
+    import ctypes as C
+    h = lib.fmd_turi_add(md, tu["cat"], *tu["dims"], 0.0, -1.0)
+    tu["_handle"] = h
+    if tu["cat"] == 0:
+        for f in tu["fields"]:
+            lib.fmd_field_add(md, h, getattr(api, "FMD_FIELD_" + f), 0.01)
+        return
+    if tu["cat"] == 1:
+        lib._fmd_ttm_setHeatCapacity_linear(md, h, api.HeatCapacityLinear(tu["gamma"]))
+        lib._fmd_ttm_setHeatConductivity_constant1(md, h, tu["K"])
+        lib._fmd_ttm_setCouplingFactor_constant1(md, h, tu["G"])
+    else:
+        pc, pg = write_ttm_tables(workdir)
+        lib._fmd_ttm_setHeatCapacity_file(md, h, pc.encode())
+        v, A, B = tu["zhigilei"]
+        lib._fmd_ttm_setHeatConductivity_zhigilei(md, h, api.HeatConductivityZhigilei(v, A, B))
+        lib._fmd_ttm_setCouplingFactor_file(md, h, pg.encode())
+    lib.fmd_ttm_setElectronTemperature(md, h, tu["Te"])
+    lib.fmd_ttm_setTimestepRatio(md, h, tu["ratio"])
+    lib.fmd_ttm_setCellActivationFraction(md, h, tu["frac"])
+    f, R, t0, dur, depth = tu["laser"]
+    lib._fmd_ttm_setLaserSource_gaussian(md, h, api.LaserGaussian(f, R, t0, dur, depth))
 
 
 class Recorder:
@@ -142,10 +211,65 @@ class Recorder:
                 self.errors.append((p.error, bool(p.major)))
 
         self.cb = api.EventHandler(handler)
+        self.fields = []       # (time, turi, field, values) at every field update event
+        self.field_cats = {}
+
+    def record_fields(self, md, turi):
+        """also record every field-update event and the field's array"""
+        import ctypes as C
+        lib = self.lib
+        self.turi = turi
+
+        def handler(mdp, event, usp, params):
+            if event == api.FMD_EVENT_TIMER_TICK:
+                t = lib.fmd_dync_getTime(mdp)
+                self.rows.append((t, lib.fmd_matt_getTemperature(mdp), lib.fmd_matt_getTotalEnergy(mdp),
+                                  lib.fmd_matt_getKineticEnergy(mdp)))
+            elif event == api.FMD_EVENT_ERROR:
+                p = C.cast(params, C.POINTER(api.ErrorParams)).contents
+                self.errors.append((p.error, bool(p.major)))
+            elif event == api.FMD_EVENT_FIELD_UPDATE:
+                p = C.cast(params, C.POINTER(api.FieldUpdateParams)).contents
+                vals = None
+                cat = self.field_cats.get(p.field)
+                if cat is not None and cat != api.FMD_FIELD_TTM_XI:
+                    arr = C.c_void_p()
+                    dims = (C.c_uint * 3)()
+                    a3s = lib.fmd_field_getArray(mdp, p.turi, p.field, C.byref(arr), dims)
+                    if a3s:
+                        vals = read_array3(arr, dims, cat)
+                        lib.fmd_array3s_free(a3s)
+                self.fields.append((lib.fmd_dync_getTime(mdp), p.turi, p.field, vals))
+
+        self.cb = api.EventHandler(handler)
+        for cat in range(7):
+            fi = lib.fmd_field_find(md, turi, cat)
+            if fi >= 0:
+                self.field_cats[fi] = cat
 
     def attach(self, md, interval):
         self.lib.fmd_setEventHandler(md, None, self.cb)
-        self.timer = self.lib.fmd_timer_makeSimple(md, 0.0, interval, -1.0)
+        if self.timer is None:
+            self.timer = self.lib.fmd_timer_makeSimple(md, 0.0, interval, -1.0)
+
+
+def read_array3(arr, dims, cat):
+    """Copy an fmd_array3_t (void***) of the given field category."""
+    import ctypes as C
+    n0, n1, n2 = dims[0], dims[1], dims[2]
+    p0 = C.cast(arr, C.POINTER(C.POINTER(C.c_void_p)))
+    if cat == api.FMD_FIELD_NUMBER:
+        et, k = C.c_uint, 1
+    elif cat == api.FMD_FIELD_VCM:
+        et, k = C.c_double, 3
+    else:
+        et, k = C.c_double, 1
+    out = np.zeros((n0, n1, n2, k))
+    for i in range(n0):
+        for j in range(n1):
+            row = C.cast(p0[i][j], C.POINTER(et))
+            out[i, j] = np.ctypeslib.as_array(row, shape=(n2 * k,)).reshape(n2, k)
+    return out
 
 
 def run(lib: api.Lib, name: str, md, rec: Recorder | None = None, steps=None):

@@ -34,10 +34,13 @@ def golden_case(lib, name, work):
     case = cases.CASES[name]
     md, st = cases.setup(lib, name, work)
     grp, dt = case["run"][1], case["run"][2]
+    rec = cases.Recorder(lib)
+    if "turi" in case:
+        rec.record_fields(md, case["turi"]["_handle"])
+        lib.fmd_setEventHandler(md, None, rec.cb)
     lib.fmd_dync_integrate(md, grp, 0.0, dt)
     d0 = lib.dump(md)
     nc, cellh, l, pbc = lib.grid(md)
-    rec = cases.Recorder(lib)
     cases.run(lib, name, md, rec)
     d1 = lib.dump(md)
     out = dict(state_x=st["x"], state_v=st["v"], state_kind=st["kind"], state_group=st["group"],
@@ -48,6 +51,16 @@ def golden_case(lib, name, work):
                s1_pe=np.array(d1["pe"]), thermo=np.array(rec.rows),
                errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2),
                time_iteration=np.array(lib.wb("time_iteration")(md) if lib.has("oref_time_iteration") else -1))
+    if "turi" in case:
+        ev = [(t, tu, f) for (t, tu, f, _) in rec.fields]
+        out["field_events"] = np.array(ev, dtype=np.float64).reshape(-1, 3)
+        for k, (t, tu, f, vals) in enumerate(rec.fields):
+            if vals is not None:
+                out["field_%03d" % k] = vals
+        ttm = lib.ttm_1d(md)
+        if ttm is not None:
+            for kk, vv in ttm.items():
+                out["ttm_" + kk] = vv
     lib.fmd_free(md)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "N0", len(d0["id"]), "N1", len(d1["id"]), "PE0", d0["pe"], "rows", len(rec.rows),
@@ -85,17 +98,22 @@ def golden_binning(lib, name, work, rounds=4, seed=99):
 
 
 def main():
-    lib = api.Lib(REF_LIB, prefix="oref_")
     names = sys.argv[1:] or list(cases.CASES)
+    if len(names) > 1 or not sys.argv[1:]:
+        # one process per case: the reference's fmd_free reads the instance
+        # after freeing it (src/misc.c:650-660), so instances are not reused
+        import subprocess
+        for name in names + ([] if sys.argv[1:] else ["bin_lj", "bin_morse_open"]):
+            subprocess.run([sys.executable, os.path.abspath(__file__), name], check=True)
+        return
+    lib = api.Lib(REF_LIB, prefix="oref_")
     with tempfile.TemporaryDirectory() as work:
         for name in names:
             if name.startswith("bin_"):
                 golden_binning(lib, name[4:], work)
             else:
                 golden_case(lib, name, work)
-        if not sys.argv[1:]:
-            golden_binning(lib, "lj", work)
-            golden_binning(lib, "morse_open", work)
+
 
 
 if __name__ == "__main__":

@@ -65,7 +65,7 @@ def run_oracle_case(name, threads=1):
     return g, d0, d1, np.array(rows)
 
 
-@pytest.mark.parametrize("name", list(cases.CASES))
+@pytest.mark.parametrize("name", [n for n in cases.CASES if "turi" not in cases.CASES[n]])
 def test_oracle_matches_reference(name):
     g, d0, d1, rows = run_oracle_case(name)
     np.testing.assert_array_equal(d0["id"], g["s0_id"])

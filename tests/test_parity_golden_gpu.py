@@ -42,11 +42,15 @@ def run_case(lib, name):
     with tempfile.TemporaryDirectory() as work:
         md, _ = cases.setup(lib, name, work, state=st)
         grp, dt = case["run"][1], case["run"][2]
+        rec = cases.Recorder(lib)
+        if "turi" in case:
+            rec.record_fields(md, case["turi"]["_handle"])
+            lib.fmd_setEventHandler(md, None, rec.cb)
         lib.fmd_dync_integrate(md, grp, 0.0, dt)
         d0 = lib.dump(md)
-        rec = cases.Recorder(lib)
         cases.run(lib, name, md, rec)
         d1 = lib.dump(md)
+        rec.ttm = lib.ttm_1d(md) if "turi" in case else None
         lib.fmd_free(md)
     return g, d0, d1, rec
 
@@ -76,6 +80,28 @@ def test_case_parity(gpu_lib, name):
     np.testing.assert_array_equal(d1["cell"], g["s1_cell"])
     np.testing.assert_array_equal(d1["id"], g["s1_id"])
     assert np.abs(d1["x"] - g["s1_x"]).max() <= POS_TOL
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if "turi" in cases.CASES[n]])
+def test_turi_fields(gpu_lib, name):
+    """Field-update events (order, turi, field, time) and every field array
+    seen by the handler match the reference; the final TTM state (Te, xi, Ti,
+    number of atoms per cell) matches on the interior cells."""
+    g, d0, d1, rec = run_case(gpu_lib, name)
+    ev = np.array([(t, tu, f) for (t, tu, f, _) in rec.fields]).reshape(-1, 3)
+    np.testing.assert_array_equal(ev[:, 1:], g["field_events"][:, 1:])
+    np.testing.assert_allclose(ev[:, 0], g["field_events"][:, 0], rtol=0, atol=1e-12)
+    for k, (_, _, _, vals) in enumerate(rec.fields):
+        key = "field_%03d" % k
+        if key in g:
+            np.testing.assert_allclose(vals, g[key], rtol=1e-9, atol=1e-9, equal_nan=True, err_msg=key)
+    if "ttm_Te" in g:
+        lo, hi = 1, len(g["ttm_Te"]) - 1
+        t = rec.ttm
+        np.testing.assert_array_equal(t["num"][lo:hi], g["ttm_num"][lo:hi])
+        for q in ("Te", "xi", "Ti"):
+            np.testing.assert_allclose(t[q][lo:hi], g["ttm_" + q][lo:hi], rtol=1e-9, atol=1e-9, equal_nan=True,
+                                       err_msg=q)
 
 
 @pytest.mark.parametrize("name", ["lj", "morse_open"])
