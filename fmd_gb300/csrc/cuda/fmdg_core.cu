@@ -817,11 +817,12 @@ extern "C" int fmdg_ttm_download_te(fmdg_sys_t *s, int turi, int presolve, doubl
     return FMDG_OK;
 }
 
-extern "C" int fmdg_turi_update(fmdg_sys_t *s, double dt)
+extern "C" int fmdg_turi_update(fmdg_sys_t *s, double dt, unsigned mask)
 {
     if (!s->atoms) return FMDG_E_STATE;
     for (int k = 0; k < s->nturi; k++)
     {
+        if (!(mask & (1u << k))) continue;
         int rc = fmdg_launch_turi(s, k, dt);
         if (rc) return rc;
     }

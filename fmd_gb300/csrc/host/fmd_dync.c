@@ -111,11 +111,16 @@ static void vv_integrate(fmd_t *md, double duration, bool thermostat)
         if (!_fmdh_dev_ok(md, fmdg_set_time(md->dev, md->time, dt), "fmdg_set_time")) return;
     }
     if (!initial_forces(md)) return;
-    if (md->turies_num > 0 && !_fmdh_dev_ok(md, fmdg_turi_update(md->dev, dt), "fmdg_turi_update")) return;
+    unsigned due = 0;
+    if (md->turies_num > 0)
+    {
+        due = _fmdh_turies_due(md);
+        if (due && !_fmdh_dev_ok(md, fmdg_turi_update(md->dev, dt, due), "fmdg_turi_update")) return;
+    }
     if (thermostat &&
         !_fmdh_dev_ok(md, fmdg_prepare_thermostat(md->dev, md->ActiveGroup, dt, tau, T0), "thermostat"))
         return;
-    if (md->turies_num > 0) _fmdh_turies_update(md, true, true, true);
+    if (md->turies_num > 0) _fmdh_turies_updated(md, due, false);
     _fmdh_check_device_errors(md);
     if (md->EventHandler != NULL) _fmdh_send_timer_events(md);
     while (md->time < start + duration)

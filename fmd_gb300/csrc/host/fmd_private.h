@@ -178,6 +178,8 @@ void _fmdh_turies_update(fmd_t *md, bool xupd, bool vupd, bool fupd);
 void _fmdh_ttm_get_ready(fmd_t *md);
 void _fmdh_se_integrate(fmd_t *md, double duration);
 bool _fmdh_prepare_turies(fmd_t *md);
+unsigned _fmdh_turies_due(fmd_t *md);
+void _fmdh_turies_updated(fmd_t *md, unsigned mask, bool with_ttm);
 
 /* fmd_dync.c */
 void _fmdh_send_timer_events(fmd_t *md);

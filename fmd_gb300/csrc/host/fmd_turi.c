@@ -66,6 +66,7 @@ struct turi
     double frontsurf;
     unsigned initial_atoms_num, min_atoms_num;
     bool in_te_event;        /* handler is running for this turi's Te event */
+    int last_iter;           /* time_iteration of the last field update */
 };
 
 struct _fmd_array3s
@@ -146,6 +147,7 @@ fmd_handle_t fmd_turi_add(fmd_t *md, fmd_turi_t cat, int dimx, int dimy, int dim
     }
     t->tcell_volume = t->tcellh[0] * t->tcellh[1] * t->tcellh[2];
     t->dev = -1;
+    t->last_iter = -1;
     t->CellActivFrac = 0.1;
     if (cat != FMD_TURI_CUSTOM)
     {
@@ -253,14 +255,36 @@ static bool within_window(const fmd_t *md, const turi_t *t)
            ((md->time < t->stoptime + md->timestep / 2.0) || t->stoptime < t->starttime);
 }
 
-/* field-update events after the device has updated the turies */
+/* Turies due for an update at the current iteration: inside their time
+   window and not yet updated at this time_iteration (the reference marks
+   every field with the iteration of its last update and skips marked
+   fields, src/turi.c:1646). */
+unsigned _fmdh_turies_due(fmd_t *md)
+{
+    unsigned mask = 0;
+    for (int ti = 0; ti < md->turies_num; ti++)
+        if (within_window(md, &md->turies[ti]) && md->turies[ti].last_iter != md->time_iteration)
+            mask |= 1u << ti;
+    return mask;
+}
+
+/* after the device updated the turies in `mask`: mark them and send the
+   field-update events in the reference's order */
+void _fmdh_turies_updated(fmd_t *md, unsigned mask, bool with_ttm)
+{
+    for (int ti = 0; ti < md->turies_num; ti++)
+        if (mask & (1u << ti))
+        {
+            md->turies[ti].last_iter = md->time_iteration;
+            if (md->EventHandler != NULL) field_events(md, ti, &md->turies[ti], with_ttm);
+        }
+}
+
 void _fmdh_turies_update(fmd_t *md, bool xupd, bool vupd, bool fupd)
 {
-    if (md->EventHandler == NULL) return;
-    const bool with_ttm = xupd && vupd && !fupd;
+    (void)vupd;
     if (!xupd) return;   /* (F,F,T) after (T,T,F): every field is already updated */
-    for (int ti = 0; ti < md->turies_num; ti++)
-        if (within_window(md, &md->turies[ti])) field_events(md, ti, &md->turies[ti], with_ttm);
+    _fmdh_turies_updated(md, _fmdh_turies_due(md), !fupd);
 }
 
 /* ----------------------------------------------------------- device */
@@ -350,8 +374,9 @@ void _fmdh_se_integrate(fmd_t *md, double duration)
     _fmdh_ttm_get_ready(md);
     if (md->active_ttm_turi && !upload_ttm(md, md->active_ttm_turi)) return;
     if (!_fmdh_dev_ok(md, fmdg_set_time(md->dev, md->time, dt), "fmdg_set_time")) return;
-    if (!_fmdh_dev_ok(md, fmdg_turi_update(md->dev, dt), "fmdg_turi_update")) return;
-    _fmdh_turies_update(md, true, true, false);
+    const unsigned due = _fmdh_turies_due(md);
+    if (due && !_fmdh_dev_ok(md, fmdg_turi_update(md->dev, dt, due), "fmdg_turi_update")) return;
+    _fmdh_turies_updated(md, due, true);
     if (!_fmdh_dev_ok(md, fmdg_compute_forces(md->dev, md->ActiveGroup), "fmdg_compute_forces")) return;
     md->thermo_pending = true;
     md->KineticEnergyUpdated = true;

@@ -170,9 +170,10 @@ int fmdg_ttm_download_te(fmdg_sys_t *s, int turi, int presolve, double *Te);
 /* simulation time and time step the device uses for turi windows, the
    laser source and the friction term; steps advance the time by dt */
 int fmdg_set_time(fmdg_sys_t *s, double time, double dt);
-/* field update of every turi at the current time (src/turi.c:1627-1665):
-   mass, vcm, number, temperature; then the TTM solver */
-int fmdg_turi_update(fmdg_sys_t *s, double dt);
+/* field update of the turies selected by bit k of mask at the current time
+   (src/turi.c:1627-1665): mass, vcm, number, temperature; then the TTM
+   solver */
+int fmdg_turi_update(fmdg_sys_t *s, double dt, unsigned mask);
 /* symplectic-Euler steps under TTM coupling (src/integrators.c:129-225):
    kick-drift, refresh, time += dt, turi updates, forces + friction term */
 int fmdg_se_steps(fmdg_sys_t *s, int nsteps, double dt, int active_group);
