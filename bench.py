@@ -204,7 +204,7 @@ def run_ours(args):
         nprof = max(3, min(10, args.steps))
         ck(L.fmdg_vv_steps(dev, nprof, dt, -1, 0, 1.0, 0.0), "profile")
         phases = {}
-        for ph in ("bin", "nlist", "density", "force", "reduce"):
+        for ph in ("bin", "nlist", "density", "force", "turi"):
             pms, pn = C.c_float(0.0), C.c_int(0)
             L.fmdg_get_profile(dev, ph.encode(), C.byref(pms), C.byref(pn))
             phases[ph] = pms.value / max(pn.value, 1)

@@ -90,7 +90,7 @@ __global__ void k_bin_classify(Geo g, int mode, double dt, int group, int thermo
     bool departs = false, outside = false;
     for (int d = 0; d < 3; d++)
     {
-        const double q = floor(__ddiv_rn(x[d], g.cellh[d]));
+        const double q = floor_div(x[d], g.cellh[d], g.inv_cellh[d]);
         // local index including the ghost margin (ic_start = 1)
         if (!(q >= -1.0 && q <= (double)g.nc[d])) outside = true;
         jc[d] = outside ? 0 : (int)q + 1;

@@ -218,6 +218,7 @@ extern "C" int fmdg_set_box(fmdg_sys_t *s, const double l[3], const int pbc[3], 
         s->g.pbc[d] = pbc[d] ? 1 : 0;
         s->g.nc[d] = nc[d];
         s->g.cellh[d] = cellh[d];
+        s->g.inv_cellh[d] = 1.0 / cellh[d];
     }
     const long long ncell = (long long)nc[0] * nc[1] * nc[2];
     if (ncell > (1 << 24)) return fmdg_set_error("fmdg_set_box: more than 2^24 cells");
@@ -516,9 +517,7 @@ extern "C" int fmdg_refresh(fmdg_sys_t *s)
 extern "C" int fmdg_compute_forces(fmdg_sys_t *s, int active_group)
 {
     if (!s->atoms || !s->cats) return FMDG_E_STATE;
-    int rc = fmdg_launch_forces(s, active_group, 0, 0.0);
-    if (rc) return rc;
-    return fmdg_launch_reduce(s, 0, 0.0, 1.0, 0.0);
+    return fmdg_launch_forces(s, active_group, 0, 0.0, 0, 1.0, 0.0);
 }
 
 extern "C" int fmdg_thermo(fmdg_sys_t *s, int active_group, fmdg_thermo_t *out)
@@ -533,9 +532,7 @@ static int vv_step_launches(fmdg_sys_t *s, double dt, int group, int thermostat,
 {
     int rc = fmdg_launch_refresh(s, FMDG_REFRESH_VV, dt, group, thermostat);
     if (rc) return rc;
-    rc = fmdg_launch_forces(s, group, 1, dt);
-    if (rc) return rc;
-    rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0);
+    rc = fmdg_launch_forces(s, group, 1, dt, thermostat, tau, T0);
     if (rc) return rc;
     // fields of every turi after the step (src/integrators.c:258-259)
     for (int k = 0; k < s->nturi; k++)
@@ -550,8 +547,7 @@ static int se_step_launches(fmdg_sys_t *s, double dt, int group)
     if (rc) return rc;
     for (int k = 0; k < s->nturi; k++)
         if ((rc = fmdg_launch_turi(s, k, dt))) return rc;
-    if ((rc = fmdg_launch_forces(s, group, 0, dt))) return rc;
-    return fmdg_launch_reduce(s, 0, dt, 1.0, 0.0);
+    return fmdg_launch_forces(s, group, 0, dt, 0, 1.0, 0.0);
 }
 
 // Before the first step of a run the caller computes the forces of the
@@ -572,7 +568,7 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
     if (s->profiling)
     {
         // phases timed separately with events:
-        // 0 refresh, 1 neighbour list, 2 density, 3 force, 4 reduce
+        // 0 refresh, 1 neighbour list, 2 density, 3 force (+ thermo record), 4 turi fields
         for (int k = 0; k < nsteps; k++)
         {
             FMDG_CK(cudaEventRecord(s->pev[0], s->stream));
@@ -583,9 +579,10 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
             FMDG_CK(cudaEventRecord(s->pev[2], s->stream));
             if ((rc = fmdg_launch_density(s, active_group))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[3], s->stream));
-            if ((rc = fmdg_launch_pair_forces(s, active_group, 1, dt))) return rc;
+            if ((rc = fmdg_launch_pair_forces(s, active_group, 1, dt, thermostat, tau, T0))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[4], s->stream));
-            if ((rc = fmdg_launch_reduce(s, thermostat, dt, tau, T0))) return rc;
+            for (int k = 0; k < s->nturi; k++)
+                if ((rc = fmdg_launch_turi(s, k, dt))) return rc;
             FMDG_CK(cudaEventRecord(s->pev[5], s->stream));
             FMDG_CK(cudaEventSynchronize(s->pev[5]));
             for (int ph = 0; ph < 5; ph++)
@@ -621,8 +618,8 @@ extern "C" int fmdg_vv_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
         s->graph_mode = 0;
         // kernels per captured step
         const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
-        // memset node + 6 refresh kernels + 2 list kernels + density + force + reduce
-        s->graph_steps = 7 + 2 + (eam ? 1 : 0) + 1 + 1;
+        // memset node + 6 refresh kernels + 2 list kernels + density + force
+        s->graph_steps = 7 + 2 + (eam ? 1 : 0) + 1;
         for (int k = 0; k < s->nturi; k++) s->graph_steps += 5 + (s->turi[k].ttm ? 1 : 0);
     }
     for (int k = 0; k < nsteps; k++) FMDG_CK(cudaGraphLaunch(s->graph, s->stream));
@@ -944,7 +941,7 @@ extern "C" int fmdg_set_profiling(fmdg_sys_t *s, int on)
 
 extern "C" int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches)
 {
-    static const char *names[5] = {"bin", "nlist", "density", "force", "reduce"};
+    static const char *names[5] = {"bin", "nlist", "density", "force", "turi"};
     for (int k = 0; k < 5; k++)
         if (strcmp(name, names[k]) == 0)
         {

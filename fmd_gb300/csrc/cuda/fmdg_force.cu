@@ -397,10 +397,63 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
     block_reduce_store<1>(acc, g.partials + (size_t)gridDim.x * 8 + blockIdx.x);
 }
 
+// Second level: sums the per-block partials in a fixed order, writes the
+// thermo record (src/integrators.c:78-92) and, when a Berendsen thermostat
+// is active, the velocity scale of the next start step
+// (src/integrators.c:44-50): lambda = sqrt(1 + dt/tau * (T0/T - 1)).
+// Run by one whole block of at most 256 threads.
+__device__ void final_reduce(const Geo &g, int nblocks, int keep_pe, int with_emb, int thermostat,
+                             double dt, double tau, double T0)
+{
+    __shared__ double red[8][7];
+    const int t = threadIdx.x;
+    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int b = t; b < nblocks; b += blockDim.x)
+    {
+        for (int k = 0; k < 6; k++) s[k] += __ldcg(&g.partials[(size_t)k * nblocks + b]);
+        if (with_emb) s[6] += __ldcg(&g.partials[(size_t)nblocks * 8 + b]);
+    }
+    for (int k = 0; k < 7; k++)
+        for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], off);
+    if ((t & 31) == 0)
+        for (int k = 0; k < 7; k++) red[t >> 5][k] = s[k];
+    __syncthreads();
+    if (t == 0)
+    {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            for (int k = 0; k < 7; k++) red[0][k] += red[w][k];
+        fmdg_thermo_t *th = g.thermo;
+        const double mv2 = red[0][1];
+        const double N = red[0][5];
+        th->kinetic = 0.5 * mv2;
+        th->temperature = mv2 / (3.0 * N * K_BOLTZMANN_D);
+        th->momentum[0] = red[0][2];
+        th->momentum[1] = red[0][3];
+        th->momentum[2] = red[0][4];
+        th->count = N;
+        if (!keep_pe) th->potential = red[0][0] + red[0][6];
+        if (thermostat)
+            g.dyn->lambda = sqrt(1 + dt / tau * (T0 / th->temperature - 1));
+    }
+}
+
+__global__ void k_reduce_final(Geo g, int nblocks, int keep_pe, int with_emb, int thermostat,
+                               double dt, double tau, double T0)
+{
+    final_reduce(g, nblocks, keep_pe, with_emb, thermostat, dt, tau, T0);
+}
+
+// thermo-record arguments of the fused last-block reduction
+struct RedArgs
+{
+    int with_emb, thermostat;
+    double tau, T0;
+};
+
 // Pair forces + per-atom half energies; with finish=1 also the
 // velocity-Verlet finishStep (src/integrators.c:94-126) and its reductions.
 template <int CAT, bool MIXED>
-__global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, double dt)
+__global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, double dt, RedArgs ra)
 {
     __shared__ SmemPot sp;
     load_pot(g, sp);
@@ -598,9 +651,22 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
         }
     }
     __shared__ double blk[6];
+    __shared__ unsigned ticket;
     block_reduce_store<6>(acc, blk);
     if (threadIdx.x == 0)
+    {
         for (int k = 0; k < 6; k++) g.partials[(size_t)k * gridDim.x + blockIdx.x] = blk[k];
+        __threadfence();
+        ticket = atomicAdd(&g.dyn->blocks_done, 1u);
+    }
+    __syncthreads();
+    // the last block to finish sums every block's partials in a fixed order
+    if (ticket == gridDim.x - 1)
+    {
+        __threadfence();
+        final_reduce(g, gridDim.x, 0, ra.with_emb, ra.thermostat, dt, ra.tau, ra.T0);
+        if (threadIdx.x == 0) g.dyn->blocks_done = 0;
+    }
 }
 
 // Thermodynamics of the active group from the current velocities
@@ -627,46 +693,6 @@ __global__ void __launch_bounds__(128) k_thermo(Geo g, int group)
     block_reduce_store<6>(acc, blk);
     if (threadIdx.x == 0)
         for (int k = 0; k < 6; k++) g.partials[(size_t)k * gridDim.x + blockIdx.x] = blk[k];
-}
-
-// Second level: sums the per-block partials in a fixed order, writes the
-// thermo record (src/integrators.c:78-92) and, when a Berendsen thermostat
-// is active, the velocity scale of the next start step
-// (src/integrators.c:44-50): lambda = sqrt(1 + dt/tau * (T0/T - 1)).
-__global__ void k_reduce_final(Geo g, int nblocks, int keep_pe, int with_emb, int thermostat,
-                               double dt, double tau, double T0)
-{
-    __shared__ double red[256][7];
-    const int t = threadIdx.x;
-    double s[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int b = t; b < nblocks; b += blockDim.x)
-    {
-        for (int k = 0; k < 6; k++) s[k] += g.partials[(size_t)k * nblocks + b];
-        if (with_emb) s[6] += g.partials[(size_t)nblocks * 8 + b];
-    }
-    for (int k = 0; k < 7; k++) red[t][k] = s[k];
-    __syncthreads();
-    for (int off = blockDim.x / 2; off > 0; off >>= 1)
-    {
-        if (t < off)
-            for (int k = 0; k < 7; k++) red[t][k] += red[t + off][k];
-        __syncthreads();
-    }
-    if (t == 0)
-    {
-        fmdg_thermo_t *th = g.thermo;
-        const double mv2 = red[0][1];
-        const double N = red[0][5];
-        th->kinetic = 0.5 * mv2;
-        th->temperature = mv2 / (3.0 * N * K_BOLTZMANN_D);
-        th->momentum[0] = red[0][2];
-        th->momentum[1] = red[0][3];
-        th->momentum[2] = red[0][4];
-        th->count = N;
-        if (!keep_pe) th->potential = red[0][0] + red[0][6];
-        if (thermostat)
-            g.dyn->lambda = sqrt(1 + dt / tau * (T0 / th->temperature - 1));
-    }
 }
 
 } // namespace
@@ -707,33 +733,40 @@ int fmdg_launch_density(fmdg_sys_t *s, int group)
 }
 
 template <bool MIXED>
-static void launch_force_t(fmdg_sys_t *s, int nb, int group, int finish, double dt)
+static void launch_force_t(fmdg_sys_t *s, int nb, int group, int finish, double dt, RedArgs ra)
 {
     Geo &g = s->g;
     cudaStream_t st = s->stream;
     const int ncat = __builtin_popcount(s->cats);
-    if (ncat > 1) k_force<CAT_HYBRID, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else if (s->cats == (1 << FMDG_POT_LJ)) k_force<CAT_LJ, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else if (s->cats == (1 << FMDG_POT_MORSE)) k_force<CAT_MORSE, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
-    else k_force<CAT_EAM, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt);
+    if (ncat > 1) k_force<CAT_HYBRID, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
+    else if (s->cats == (1 << FMDG_POT_LJ)) k_force<CAT_LJ, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
+    else if (s->cats == (1 << FMDG_POT_MORSE)) k_force<CAT_MORSE, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
+    else k_force<CAT_EAM, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
 }
 
-int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt)
+// pair forces; the kernel's last block also writes the thermo record
+int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau,
+                            double T0)
 {
     const int nb = fmdg_force_blocks(s);
-    if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<true>(s, nb, group, finish, dt);
-    else launch_force_t<false>(s, nb, group, finish, dt);
+    RedArgs ra;
+    ra.with_emb = (s->cats & (1 << FMDG_POT_EAM)) != 0;
+    ra.thermostat = thermostat;
+    ra.tau = tau;
+    ra.T0 = T0;
+    if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<true>(s, nb, group, finish, dt, ra);
+    else launch_force_t<false>(s, nb, group, finish, dt, ra);
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
 }
 
-int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt)
+int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0)
 {
     int rc = fmdg_launch_nlist(s);
     if (rc) return rc;
     if ((rc = fmdg_launch_density(s, group))) return rc;
-    return fmdg_launch_pair_forces(s, group, finish, dt);
+    return fmdg_launch_pair_forces(s, group, finish, dt, thermostat, tau, T0);
 }
 
 // thermo-only reduction (no force evaluation); keeps the potential energy
@@ -744,17 +777,6 @@ int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, doub
     k_thermo<<<nb, 128, 0, s->stream>>>(g, group);
     k_reduce_final<<<1, 256, 0, s->stream>>>(g, nb, 1, 0, thermostat, dt, tau, T0);
     s->launches += 2;
-    FMDG_CK(cudaGetLastError());
-    return FMDG_OK;
-}
-
-int fmdg_launch_reduce(fmdg_sys_t *s, int thermostat, double dt, double tau, double T0)
-{
-    Geo &g = s->g;
-    const int nb = fmdg_force_blocks(s);
-    const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
-    k_reduce_final<<<1, 256, 0, s->stream>>>(g, nb, 0, eam ? 1 : 0, thermostat, dt, tau, T0);
-    s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
 }

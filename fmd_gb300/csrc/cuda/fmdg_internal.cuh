@@ -30,7 +30,7 @@ struct Dyn
     int n_next;         // atom count after the refresh in flight
     int any_move;       // a refresh moved at least one atom
     unsigned err;       // sticky error bits (FMDG_ERRBIT_*)
-    int pad;
+    unsigned blocks_done;   // ticket of the force kernel's last-block reduction
     double lambda;      // Berendsen scale for the next start step
     double time;        // simulation time (advanced by every step)
     double dt;          // time step of the current run (turi windows)
@@ -51,7 +51,7 @@ struct Geo   // passed by value to kernels
     int cap, ncell;
     int nc[3];
     int pbc[3];
-    double l[3], cellh[3];
+    double l[3], cellh[3], inv_cellh[3];
     Side side[2];
     double *F, *vaream;
     // per-step neighbour list (built after every refresh)
@@ -141,14 +141,13 @@ int fmdg_set_error(const char *msg);
 // kernel launch wrappers (defined in their translation units)
 int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int thermostat);
 int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt);
-int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt);
+int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0);
 int fmdg_launch_density(fmdg_sys_t *s, int group);
 int fmdg_launch_nlist(fmdg_sys_t *s);
 int fmdg_pack_tables(fmdg_sys_t *s);
-int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt);
+int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0);
 int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0);
 int fmdg_force_blocks(const fmdg_sys_t *s);
-int fmdg_launch_reduce(fmdg_sys_t *s, int thermostat, double dt, double tau, double T0);
 
 // refresh modes
 #define FMDG_REFRESH_ONLY  0     // positions already updated
@@ -158,3 +157,15 @@ int fmdg_launch_reduce(fmdg_sys_t *s, int thermostat, double dt, double tau, dou
 static inline int fmdg_grid(int n, int b) { return (n + b - 1) / b; }
 
 __device__ __forceinline__ void atomic_or_err(Dyn *d, unsigned bit) { atomicOr(&d->err, bit); }
+
+// floor(x/h) exactly as binary64 division would give it: the product with
+// 1/h (relative error <= 2^-52) decides unless it lies within 1e-9 of an
+// integer, where the IEEE quotient is evaluated.
+__device__ __forceinline__ double floor_div(double x, double h, double inv_h)
+{
+    const double q = x * inv_h;
+    const double f = floor(q);
+    const double tol = 1e-9 * fmax(1.0, fabs(q));
+    if (q - f < tol || (f + 1.0) - q < tol) return floor(__ddiv_rn(x, h));
+    return f;
+}

@@ -219,7 +219,7 @@ int fmdg_timer_stop(fmdg_sys_t *s, float *ms);
 /* with profiling on, fmdg_vv_steps launches each phase between CUDA events
    (no graph) and accumulates its device time: phases "bin" (start step +
    refresh), "density" (EAM pass 1 + embedding), "force" (pair forces +
-   finish step), "reduce" (thermo record); ms summed over steps */
+   finish step), "turi" (field updates); ms summed over steps */
 int fmdg_set_profiling(fmdg_sys_t *s, int on);
 int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches);
 int fmdg_launch_count(fmdg_sys_t *s, long long *count);
