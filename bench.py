@@ -1,21 +1,33 @@
 """Benchmark: atom-steps/s of FMD's per-timestep hot path on one GB300.
 
-Workload (default): the 256 000-atom EAM system -- FCC 40x40x40 cells,
-a = 3.615 A, Cu mass, periodic, analytic EAM tabulated on 10 000 r and
-10 000 rho points, 300 K Maxwell velocities from seed 2, dt = 1 fs,
-NVE velocity Verlet.  Synthetic inputs built through the fmd.h API
-(no dataset involved).  One "step" = one MD time step of the whole system
-(refresh, EAM density + embedding, forces, both half-kicks, reductions).
+Workloads
+  served (default)  the served job stream: independent FCC cubes (500 to
+                    200 000 atoms, log-uniform), potential uniform over the
+                    argon LJ / copper Morse / analytic copper EAM, 50-1200 K,
+                    step counts uniform in [1000, 20000], Poisson arrivals at
+                    50 jobs/s (seed 5).  A bounded sample is timed: the first
+                    --jobs jobs with every step count and arrival time
+                    multiplied by --step-scale (the offered load relative to
+                    the device's capacity is unchanged).  Mixed precision
+                    (binary32 pair arithmetic, binary64 sums), packed per
+                    potential, chunks of steps replayed as CUDA graphs.
+  eam256k           one 256 000-atom EAM system (FCC 40x40x40, a = 3.615 A,
+                    300 K, seed 2, dt 1 fs), the single-system drop-in path.
 
-    python bench.py [--steps K] [--warmup W] [--precision fp64|mixed]
+    python bench.py [--steps K] [--warmup W] [--workload served|eam256k]
     python bench.py --impl reference     # CPU oracle port on the host cores
 
-Timing: device time with CUDA events on the engine's stream, one event
-pair per step, L2 flushed (256 MB write) before every timed step; the
-working set (~30 MB) is smaller than L2, so flushing is the rule used.
-`e2e` drives the same steps through the C-ABI with host buffers: every
-step uploads positions+velocities from pinned host memory, runs the step
-and reads positions, velocities and the thermo record back.
+served: `value` = every job of the sample resident in HBM, K time steps of
+the whole fleet (all packs, one graph replay per pack per step) between
+CUDA events; the fleet's working set (GBs) is larger than L2.  `e2e` = the
+sample streamed through the request loop (fmdg_srv_* C-ABI) from host
+arrays: arrivals, admission, upload, steps, results, wall clock; p50/p99
+job latency.  `plain` = the same jobs one at a time through the plain
+single-system binary64 path (the path libfmd.so's fmd_dync_integrate
+drives), wall clock including each job's set-up.
+eam256k: device time with CUDA events per step, L2 flushed (256 MB write)
+before every timed step; `e2e` drives the same steps through the C-ABI
+with pinned host buffers.
 """
 from __future__ import annotations
 
@@ -42,6 +54,11 @@ WORKLOAD = dict(name="eam256k", cells=(40, 40, 40), a=3.615, T=300.0, seed=2, dt
 PAIRS_PER_ATOM = 29.5
 FLOP_DENSITY = 26.0 * PAIRS_PER_ATOM + 26.0
 FLOP_FORCE = 68.0 * PAIRS_PER_ATOM
+# served stream: algorithmic flops of the pair-force kernel per atom-step
+# (unique pairs inside rc x flops per pair of the reference's formulas):
+# LJ 35.5 x 31 (src/lj.h:35-56), Morse 91 x 31 (src/morse.h:35-56),
+# EAM 29.5 x 68 (src/eam.h:186-226)
+SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0}
 
 
 def clocks_sampler(stop, out):
@@ -276,11 +293,243 @@ def run_ours(args):
     return out
 
 
+# ---------------------------------------------------------------- served stream
+SERVED_JOBS = 256
+SERVED_STEP_SCALE = 0.02
+
+
+def served_config(args):
+    return {"workload": "served job stream (2048-job stream, seed 5: FCC cubes 500-200000 atoms log-uniform, "
+                        "LJ argon / Morse copper / analytic-EAM copper, 50-1200 K, Poisson arrivals at 50/s); "
+                        f"sample: first {args.jobs} jobs, step counts and arrival times x {args.step_scale}",
+            "jobs": args.jobs, "step_scale": args.step_scale, "precision": "mixed",
+            "step": "one velocity-Verlet step of every resident job (value); one job (e2e, plain)",
+            "l2": "fleet working set larger than L2 (no flush needed)"}
+
+
+def served_jobs(args):
+    from fmd_gb300 import serve
+    jobs = serve.served_stream(args.jobs, seed=5, step_scale=args.step_scale)
+    for j in jobs:
+        j["x"], j["v"], j["l"] = serve.job_atoms(j)
+    return jobs
+
+
+def cpu_port_jobs(jobs, threads, budget_s=12.0, max_steps=10):
+    """The CPU oracle port (restated reference algorithm, OpenMP, per-thread
+    buffers) on the first jobs of the sample, one at a time; returns
+    (atom-steps/s, description of the sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from fmd_gb300 import serve, workloads
+    done_as, spent, used = 0.0, 0.0, []
+    with tempfile.TemporaryDirectory() as work:
+        setfl = workloads.write_analytic_eam(os.path.join(work, "analytic.eam.alloy"))
+        for j in jobs:
+            if spent >= budget_s:
+                break
+            P = serve.POTENTIALS[j["pot"]]
+            nc, cellh, order, counts = serve.host_binning(j["x"], j["l"], P["rc"])
+            if j["pot"] == "lj":
+                pots = [("lj", 0, 0, 3.405, 0.0104, 8.5125)]
+            elif j["pot"] == "morse":
+                pots = [("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)]
+            else:
+                pots = [("eam", 0, 0)]
+            o = pyoracle.Oracle(threads=threads)
+            o.setup([j["l"]] * 3, [1, 1, 1], [nc] * 3, [cellh] * 3, [("Cu", P["mass"])], pots,
+                    setfl if j["pot"] == "eam" else None)
+            n = len(order)
+            cell = np.repeat(np.arange(nc ** 3, dtype=np.int32), counts)
+            o.upload(cell, j["x"][order], j["v"][order], np.zeros(n, np.uint32), np.zeros(n, np.int32),
+                     order.astype(np.uint32), nc ** 3)
+            o.forces(-1)
+            k = max(1, min(max_steps, j["steps"]))
+            t0 = time.perf_counter()
+            o.vv(k, P["dt"])
+            dt = time.perf_counter() - t0
+            o.close()
+            done_as += n * k
+            spent += dt
+            used.append(f"{j['pot']} {n} atoms x {k} steps")
+    return done_as / spent, f"{len(used)} jobs of the sample, one at a time: " + "; ".join(used)
+
+
+def run_served(args):
+    import fmd_gb300
+    from fmd_gb300 import serve
+    L = serve.bind(fmd_gb300.load())
+    eam = serve.eam_tables(L)
+    jobs = served_jobs(args)
+    n_atoms = sum(len(j["x"]) for j in jobs)
+    K, W = args.steps, max(args.warmup, 8)
+
+    # --- value: the whole sample resident in HBM, K fleet steps ----------
+    fleet = serve.Server(L, budget_bytes=200 << 30, max_jobs=len(jobs) + 1, chunk_steps=1, eam=eam)
+    for j in jobs:
+        fleet.submit(j["pot"], j["x"], j["v"], j["l"], W + K + 8, precision=serve.PREC_MIXED)
+    fleet.admit()
+    st = fleet.stats()
+    assert st.running == len(jobs), "the sample does not fit the fleet budget"
+    for _ in range(W):              # warm-up; the autotuner picks block sizes here
+        fleet.run_resident(1)
+    stop = threading.Event()
+    samples = []
+    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
+    th.start()
+    k0 = fleet.stats().kernels
+    ms = fleet.run_resident(K)
+    k1 = fleet.stats().kernels
+    stop.set()
+    th.join(timeout=5)
+    clocks = summarize_clocks(samples)
+    tuned = {p: fleet.stats().pack_fblk[serve.POTENTIALS[p]["cat"]][1] for p in serve.POT_NAMES}
+    phases = {}
+    for p in serve.POT_NAMES:
+        pm, atoms, members = fleet.profile_pack(p)
+        phases[p] = {"bin_ms": pm[0], "nlist_ms": pm[1], "density_ms": pm[2], "force_ms": pm[3],
+                     "atoms": atoms, "jobs": members, "threads_per_block": tuned[p]}
+    fleet.close()
+    value = n_atoms * K / (ms * 1e-3)
+    # peak of the binary32 FMA pipe (measured microkernel)
+    h = C.c_void_p()
+    serve.check(L, L.fmdg_create(C.byref(h), 0), "create")
+    peak32, peak64 = C.c_double(), C.c_double()
+    serve.check(L, L.fmdg_measure_fma_peak(h, 0, C.byref(peak32)), "peak")
+    serve.check(L, L.fmdg_measure_fma_peak(h, 1, C.byref(peak64)), "peak")
+    L.fmdg_destroy(h)
+    dom = max(serve.POT_NAMES, key=lambda p: phases[p]["force_ms"])
+    fl = SERVED_FORCE_FLOP[dom] * phases[dom]["atoms"]
+    achieved = fl / (phases[dom]["force_ms"] * 1e-3) / 1e12
+
+    # --- e2e: the sample streamed through the request loop ---------------
+    srv = serve.Server(L, budget_bytes=64 << 30, max_jobs=1024, chunk_steps=16, eam=eam)
+    ids = [None] * len(jobs)
+    nxt = 0
+    t0 = srv.now()
+    active = 0
+    while nxt < len(jobs) or active > 0:
+        now = srv.now() - t0
+        while nxt < len(jobs) and jobs[nxt]["arrival"] <= now:
+            j = jobs[nxt]
+            ids[nxt] = srv.submit(j["pot"], j["x"], j["v"], j["l"], j["steps"], precision=serve.PREC_MIXED)
+            nxt += 1
+        if active == 0 and nxt < len(jobs) and srv.stats().queued == 0:
+            wait_s = jobs[nxt]["arrival"] - (srv.now() - t0)
+            if wait_s > 0:
+                time.sleep(min(wait_s, 0.01))
+        active = srv.progress(wait=(nxt >= len(jobs)))
+    res = [srv.result(i) for i in ids]
+    sst = srv.stats()
+    srv.close()
+    assert all(r.state == 2 for r in res), "a served job failed"
+    errbits = int(np.bitwise_or.reduce([r.errbits for r in res]))
+    job_as = np.array([r.n * r.steps for r in res], dtype=np.float64)
+    arr = np.array([j["arrival"] for j in jobs]) + 0.0
+    done = np.array([r.t_done for r in res]) - t0
+    lat = done - arr
+    span = done.max() - arr.min()
+    e2e_value = job_as.sum() / span
+    total_steps = sum(j["steps"] for j in jobs)
+    h2d = sum(len(j["x"]) * (6 * 8 + 4) for j in jobs)
+    d2h = len(jobs) * 2 * 64
+
+    def drift(r):
+        e0 = r.first.kinetic + r.first.potential
+        e1 = r.last.kinetic + r.last.potential
+        return abs(e1 - e0) / abs(e0)
+
+    served_drift = float(np.median([drift(r) for r in res]))
+
+    # --- plain: the same jobs one at a time, binary64 single-system path -----
+    plain = {}
+    for name, prec in (("fp64", serve.PREC_FP64),):
+        t_start = time.perf_counter()
+        drifts = []
+        for j in jobs:
+            one = serve.Single(L, j["pot"], j["x"], j["v"], j["l"], precision=prec, eam=eam)
+            one.steps(j["steps"])
+            t = one.thermo()
+            e0 = one.th0.kinetic + one.th0.potential
+            drifts.append(abs(t.kinetic + t.potential - e0) / abs(e0))
+            one.close()
+        t_plain = time.perf_counter() - t_start
+        plain[name] = {"value": job_as.sum() / t_plain, "unit": "atom-steps/s", "seconds": t_plain,
+                       "median_rel_energy_drift": float(np.median(drifts))}
+
+    # --- force error of the mixed path against binary64 at identical
+    # positions (a thermalised state: 20 binary64 steps), one job per potential
+    ferr = {}
+    for p in serve.POT_NAMES:
+        j = next(j for j in jobs if j["pot"] == p)
+        one = serve.Single(L, p, j["x"], j["v"], j["l"], precision=serve.PREC_FP64, eam=eam)
+        one.steps(20)
+        serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
+        F64 = one.state()[2]
+        serve.check(L, L.fmdg_set_precision(one.h, serve.PREC_MIXED), "precision")
+        serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
+        F32 = one.state()[2]
+        one.close()
+        ferr[p] = float(np.abs(F32 - F64).max() / np.abs(F64).max())
+
+    cores = os.cpu_count() or 1
+    if args.skip_cpu:
+        cpu_value, cpu_sample = None, "skipped"
+    else:
+        cpu_value, cpu_sample = cpu_port_jobs(jobs, cores)
+    out = {
+        "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1,
+        "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-compute/f64-accumulate", "data": "synthetic",
+        "config": served_config(args),
+        "gpu_launches": int(k1 - k0),
+        "served": {"jobs": len(jobs), "atoms_resident": n_atoms,
+                   "throughput_e2e": e2e_value, "plain_fp64_e2e": plain["fp64"]["value"],
+                   "served_over_plain_fp64": e2e_value / plain["fp64"]["value"],
+                   "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                   "makespan_s": float(span), "median_rel_energy_drift": served_drift,
+                   "plain": plain, "max_rel_force_err_mixed_vs_fp64": ferr,
+                   "device_error_bits": errbits, "bytes_peak": sst.bytes_peak,
+                   "graph_rebuilds": int(sum(sst.pack_rebuilds[c][m] for c in range(4) for m in range(2))),
+                   "threads_per_block": tuned},
+        "phases": phases,
+        "roofline": {"bound": "fp32-issue", "kernel": f"k_force<LocPack> ({dom} pack: pair forces + finish step)",
+                     "achieved": achieved, "peak": peak32.value, "unit": "TFLOP/s",
+                     "frac": achieved / peak32.value,
+                     "peak_source": "measured FMA-chain microkernel (MEASURED_PEAKS.json has no CUDA-core peak)",
+                     "traffic": None},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s",
+                "h2d_bytes_per_step": h2d / total_steps, "d2h_bytes_per_step": d2h / total_steps,
+                "how": "fmdg_srv_* request loop: jobs submitted from host arrays at their arrival times, "
+                       "admitted by HBM budget, uploaded, stepped in packs, results read back; wall clock "
+                       "from the first arrival to the last completion; bytes per job-step"},
+        "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                         "sample": cpu_sample},
+    }
+    return out
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: the
     oracle port (the reference's own sources are not present on the GPU
     host), all threads, same workload, metric and unit."""
     cores = os.cpu_count() or 1
+    if args.workload == "served":
+        jobs = served_jobs(args)
+        vals, sample = [], ""
+        for _ in range(max(1, min(args.steps, 3))):
+            v, sample = cpu_port_jobs(jobs, cores, budget_s=8.0)
+            vals.append(v)
+        value = float(np.median(vals))
+        out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s",
+               "n_gpus": 0, "steps": len(vals), "warmup": 0, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": served_config(args),
+               "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                                "sample": f"median of {len(vals)} samples; each: {sample}"},
+               "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return
     vals = []
     for _ in range(max(1, min(args.steps, 3))):
         v, k = cpu_port_run(cores, target_s=8.0, max_steps=10)
@@ -306,6 +555,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
+    ap.add_argument("--workload", default="served", choices=["served", "eam256k"])
+    ap.add_argument("--jobs", type=int, default=SERVED_JOBS, help="served: jobs of the stream sample")
+    ap.add_argument("--step-scale", type=float, default=SERVED_STEP_SCALE,
+                    help="served: factor on step counts and arrival times")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -314,7 +567,7 @@ def main():
             return
         run_reference(args)
         return
-    out = run_ours(args)
+    out = run_served(args) if args.workload == "served" else run_ours(args)
     print(json.dumps(out))
 
 

@@ -44,11 +44,17 @@ __device__ __forceinline__ int cell_flat(const Geo &g, int x, int y, int z)
 // Explicit _rn intrinsics keep the reference's operation order with no
 // fused multiply-add, so positions and velocities match bit for bit given
 // the same forces.
-__global__ void k_bin_classify(Geo g, int mode, double dt, int group, int thermostat)
+template <class L>
+__global__ void k_bin_classify(__grid_constant__ const L loc, int mode)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const double dt = g.st.dt;
+    const int group = g.st.group, thermostat = g.st.thermostat;
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
@@ -152,8 +158,12 @@ __global__ void k_bin_classify(Geo g, int mode, double dt, int group, int thermo
 
 // Exclusive scans over cells (one block): arrival bases and the next side's
 // cell_start, plus the atom count after the refresh.
-__global__ void k_bin_scan(Geo g)
+template <class L>
+__global__ void k_bin_scan(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     Dyn *dyn = g.dyn;
     if (!dyn->any_move) return;
     const Side S = g.side[dyn->cur];
@@ -200,11 +210,15 @@ __global__ void k_bin_scan(Geo g)
 // cells.  Emits the departure rank of each leaving atom (and queues it in
 // its destination's bucket), the final slot of each stayer, and the slot of
 // each placeholder.
-__global__ void k_bin_cells(Geo g)
+template <class L>
+__global__ void k_bin_cells(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     Dyn *dyn = g.dyn;
     if (!dyn->any_move) return;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = bx * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
     const Side S = g.side[dyn->cur];
     const int start = S.cell_start[c];
@@ -246,11 +260,15 @@ __global__ void k_bin_cells(Geo g)
 }
 
 // Order the arrivals of each destination cell and give them new indexes.
-__global__ void k_bin_arrivals(Geo g)
+template <class L>
+__global__ void k_bin_arrivals(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     Dyn *dyn = g.dyn;
     if (!dyn->any_move) return;
-    const int D = blockIdx.x * blockDim.x + threadIdx.x;
+    const int D = bx * blockDim.x + threadIdx.x;
     if (D >= g.ncell) return;
     const int total = g.arr_total[D];
     if (total == 0) return;
@@ -281,11 +299,15 @@ __global__ void k_bin_arrivals(Geo g)
     }
 }
 
-__global__ void k_bin_scatter(Geo g)
+template <class L>
+__global__ void k_bin_scatter(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     Dyn *dyn = g.dyn;
     if (!dyn->any_move) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= dyn->n) return;
     const int d = g.bdest[i];
     if (d == -1) return;
@@ -323,16 +345,34 @@ __global__ void k_bin_scatter(Geo g)
 
 // swaps sides after a refresh that moved atoms; advances the device copy of
 // the simulation time by one step (src/integrators.c:203, :256)
-__global__ void k_bin_flip(Geo g, double advance)
+template <class L>
+__global__ void k_bin_flip(__grid_constant__ const L loc, int mode)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g) || threadIdx.x != 0) return;
     Dyn *dyn = g.dyn;
-    dyn->time += advance;
+    dyn->time += (mode == FMDG_REFRESH_ONLY) ? 0.0 : g.st.dt;
     if (dyn->any_move)
     {
         dyn->cur ^= 1;
         dyn->n = dyn->n_next;
         dyn->any_move = 0;
     }
+}
+
+// per-cell binning counters of every system of a pack
+__global__ void k_bin_clear(__grid_constant__ const LocPack loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const int c = bx * blockDim.x + threadIdx.x;
+    if (c >= g.ncell) return;
+    g.dep_count[c] = 0;
+    g.arr_lower[c] = 0;
+    g.arr_total[c] = 0;
+    g.bucket_fill[c] = 0;
 }
 
 } // namespace
@@ -343,15 +383,37 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
 {
     Geo &g = s->g;
     cudaStream_t st = s->stream;
+    g.st.dt = dt;
+    g.st.group = group;
+    g.st.thermostat = thermostat;
+    const LocOne L{g};
     // dep_count, arr_lower, arr_total, bucket_fill are contiguous
     FMDG_CK(cudaMemsetAsync(g.dep_count, 0, sizeof(int) * 4 * (size_t)g.ncell, st));
-    k_bin_classify<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(g, mode, dt, group, thermostat);
-    k_bin_scan<<<1, 1024, 0, st>>>(g);
-    k_bin_cells<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(g);
-    k_bin_arrivals<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(g);
-    k_bin_scatter<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(g);
-    k_bin_flip<<<1, 1, 0, st>>>(g, mode == FMDG_REFRESH_ONLY ? 0.0 : dt);
+    k_bin_classify<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(L, mode);
+    k_bin_scan<<<1, 1024, 0, st>>>(L);
+    k_bin_cells<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(L);
+    k_bin_arrivals<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(L);
+    k_bin_scatter<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(L);
+    k_bin_flip<<<1, 32, 0, st>>>(L, mode);
     s->launches += 6;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
+}
+
+// The same refresh (velocity-Verlet start step) for every system of a pack.
+// Returns the kernels launched, or minus a status.
+int fmdg_pack_launch_refresh(const fmdg_pack_launch &P)
+{
+    cudaStream_t st = P.stream;
+    const LocPack La{P.geos, P.amap}, Lc{P.geos, P.cmap}, Ls{P.geos, nullptr};
+    k_bin_clear<<<P.ncb, 128, 0, st>>>(Lc);
+    k_bin_classify<<<P.nab, 128, 0, st>>>(La, FMDG_REFRESH_VV);
+    k_bin_scan<<<P.nsys, 1024, 0, st>>>(Ls);
+    k_bin_cells<<<P.ncb, 128, 0, st>>>(Lc);
+    k_bin_arrivals<<<P.ncb, 128, 0, st>>>(Lc);
+    k_bin_scatter<<<P.nab, 128, 0, st>>>(La);
+    k_bin_flip<<<P.nsys, 32, 0, st>>>(Ls, FMDG_REFRESH_VV);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -fmdg_fail("pack refresh", e);
+    return 7;
 }

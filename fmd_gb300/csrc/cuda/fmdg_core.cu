@@ -36,16 +36,22 @@ extern "C" int fmdg_device_count(int *count)
 
 namespace {
 
+// Device buffers are stream-ordered allocations on the system's stream from
+// the device's default pool (kept cached), so creating and retiring
+// systems never synchronises the device; the allocating call waits for its
+// own stream only.
 template <typename T>
-int dalloc(T **p, size_t n)
+int dalloc(fmdg_sys_t *s, T **p, size_t n)
 {
     if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
-    if (e != cudaSuccess) return fmdg_fail("cudaMalloc", e);
+    cudaError_t e = cudaMallocAsync((void **)p, n * sizeof(T), s->stream);
+    if (e != cudaSuccess) return fmdg_fail("cudaMallocAsync", e);
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) return fmdg_fail("cudaStreamSynchronize", e);
     return FMDG_OK;
 }
 
-void dfree(void *p) { if (p) cudaFree(p); }
+void dfree(fmdg_sys_t *s, void *p) { if (p) cudaFreeAsync(p, s->stream); }
 
 void free_atoms(fmdg_sys_t *s)
 {
@@ -53,16 +59,16 @@ void free_atoms(fmdg_sys_t *s)
     for (int k = 0; k < 2; k++)
     {
         Side &S = g.side[k];
-        dfree(S.x); dfree(S.v); dfree(S.kind); dfree(S.group); dfree(S.atomid);
-        dfree(S.cell_of); dfree(S.cell_start);
+        dfree(s, S.x); dfree(s, S.v); dfree(s, S.kind); dfree(s, S.group); dfree(s, S.atomid);
+        dfree(s, S.cell_of); dfree(s, S.cell_start);
         memset(&S, 0, sizeof S);
     }
-    dfree(g.F); dfree(g.vaream);
-    dfree(g.xf4); dfree(g.nbr); dfree(g.nbr_count);
+    dfree(s, g.F); dfree(s, g.vaream);
+    dfree(s, g.xf4); dfree(s, g.nbr); dfree(s, g.nbr_count);
     g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr;
-    dfree(g.bdest); dfree(g.bpath); dfree(g.bslot); dfree(g.brank); dfree(g.bnewidx);
-    dfree(g.dep_count); dfree(g.arr_base); dfree(g.bucket); dfree(g.arr_slot);
-    dfree(g.partials);
+    dfree(s, g.bdest); dfree(s, g.bpath); dfree(s, g.bslot); dfree(s, g.brank); dfree(s, g.bnewidx);
+    dfree(s, g.dep_count); dfree(s, g.arr_base); dfree(s, g.bucket); dfree(s, g.arr_slot);
+    dfree(s, g.partials);
     g.F = g.vaream = nullptr;
     g.bdest = g.bpath = g.bslot = g.brank = g.bnewidx = nullptr;
     g.dep_count = g.arr_lower = g.arr_total = g.bucket_fill = g.arr_base = nullptr;
@@ -71,6 +77,16 @@ void free_atoms(fmdg_sys_t *s)
     g.cap = 0;
     s->atoms = false;
     if (s->graph_key_valid) { cudaGraphExecDestroy(s->graph); s->graph_key_valid = 0; }
+}
+
+// forget EAM tables that belong to another system
+void drop_eam(fmdg_sys_t *s)
+{
+    Geo &g = s->g;
+    g.eF = g.eFDD = g.erho = g.erhoDD = g.ephi = g.ephiDD = nullptr;
+    g.pk_rho = g.pk_phi = g.pk_F = nullptr;
+    g.pkf_rho = g.pkf_phi = g.pkf_F = nullptr;
+    s->eam_borrowed = false;
 }
 
 void invalidate_graph(fmdg_sys_t *s)
@@ -159,6 +175,18 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
 {
     *out = nullptr;
     FMDG_CK(cudaSetDevice(device));
+    static bool pool_kept[64];
+    if (device >= 0 && device < 64 && !pool_kept[device])
+    {
+        // freed system buffers stay in this process's pool for the next system
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess)
+        {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool_kept[device] = true;
+    }
     fmdg_sys_t *s = (fmdg_sys_t *)calloc(1, sizeof(fmdg_sys_t));
     if (!s) return FMDG_E_NOMEM;
     s->device = device;
@@ -167,13 +195,14 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     FMDG_CK(cudaEventCreate(&s->ev0));
     FMDG_CK(cudaEventCreate(&s->ev1));
     for (int k = 0; k < 6; k++) FMDG_CK(cudaEventCreate(&s->pev[k]));
-    int rc = dalloc(&s->g.dyn, 1);
+    int rc = dalloc(s, &s->g.dyn, 1);
     if (rc) return rc;
-    rc = dalloc(&s->g.thermo, 1);
+    rc = dalloc(s, &s->g.thermo, 1);
     if (rc) return rc;
     FMDG_CK(cudaMemset(s->g.dyn, 0, sizeof(Dyn)));
     FMDG_CK(cudaMemset(s->g.thermo, 0, sizeof(fmdg_thermo_t)));
     s->ttm_turi = -1;
+    s->fblk = 128;
     *out = s;
     return FMDG_OK;
 }
@@ -184,22 +213,23 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     cudaSetDevice(s->device);
     cudaStreamSynchronize(s->stream);
     free_atoms(s);
-    dfree((void *)s->g.pairs); dfree((void *)s->g.mass); dfree((void *)s->g.eam_elem);
-    dfree((void *)s->g.eF); dfree((void *)s->g.eFDD); dfree((void *)s->g.erho);
-    dfree((void *)s->g.erhoDD); dfree((void *)s->g.ephi); dfree((void *)s->g.ephiDD);
-    dfree((void *)s->g.pk_rho); dfree((void *)s->g.pk_phi); dfree((void *)s->g.pk_F);
-    dfree((void *)s->g.pkf_rho); dfree((void *)s->g.pkf_phi); dfree((void *)s->g.pkf_F);
+    if (s->eam_borrowed) drop_eam(s);
+    dfree(s, (void *)s->g.pairs); dfree(s, (void *)s->g.mass); dfree(s, (void *)s->g.eam_elem);
+    dfree(s, (void *)s->g.eF); dfree(s, (void *)s->g.eFDD); dfree(s, (void *)s->g.erho);
+    dfree(s, (void *)s->g.erhoDD); dfree(s, (void *)s->g.ephi); dfree(s, (void *)s->g.ephiDD);
+    dfree(s, (void *)s->g.pk_rho); dfree(s, (void *)s->g.pk_phi); dfree(s, (void *)s->g.pk_F);
+    dfree(s, (void *)s->g.pkf_rho); dfree(s, (void *)s->g.pkf_phi); dfree(s, (void *)s->g.pkf_F);
     for (int k = 0; k < s->nturi; k++)
     {
         DTuri &t = s->turi[k];
-        dfree(t.acc); dfree(t.tacc); dfree(t.mass); dfree(t.vcm); dfree(t.Ti); dfree(t.num);
-        dfree(t.Te); dfree(t.Te2); dfree(t.xi); dfree(t.Ke); dfree(t.Ce); dfree(t.Gc); dfree(t.srcz);
-        dfree(t.Te_pre);
-        dfree((void *)t.p.T_C); dfree((void *)t.p.Ct); dfree((void *)t.p.C_DD);
-        dfree((void *)t.p.T_G); dfree((void *)t.p.Gt); dfree((void *)t.p.G_DD);
+        dfree(s, t.acc); dfree(s, t.tacc); dfree(s, t.mass); dfree(s, t.vcm); dfree(s, t.Ti); dfree(s, t.num);
+        dfree(s, t.Te); dfree(s, t.Te2); dfree(s, t.xi); dfree(s, t.Ke); dfree(s, t.Ce); dfree(s, t.Gc); dfree(s, t.srcz);
+        dfree(s, t.Te_pre);
+        dfree(s, (void *)t.p.T_C); dfree(s, (void *)t.p.Ct); dfree(s, (void *)t.p.C_DD);
+        dfree(s, (void *)t.p.T_G); dfree(s, (void *)t.p.Gt); dfree(s, (void *)t.p.G_DD);
     }
-    dfree(s->g.dyn); dfree(s->g.thermo);
-    dfree(s->l2buf);
+    dfree(s, s->g.dyn); dfree(s, s->g.thermo);
+    dfree(s, s->l2buf);
     cudaEventDestroy(s->ev0);
     cudaEventDestroy(s->ev1);
     for (int k = 0; k < 6; k++) cudaEventDestroy(s->pev[k]);
@@ -239,11 +269,11 @@ extern "C" int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, con
     }
     if (!s->g.mass)
     {
-        int rc = dalloc((double **)&s->g.mass, FMDG_MAXK);
+        int rc = dalloc(s, (double **)&s->g.mass, FMDG_MAXK);
         if (rc) return rc;
-        rc = dalloc((int **)&s->g.eam_elem, FMDG_MAXK);
+        rc = dalloc(s, (int **)&s->g.eam_elem, FMDG_MAXK);
         if (rc) return rc;
-        rc = dalloc((fmdg_pair_t **)&s->g.pairs, FMDG_MAXK * FMDG_MAXK);
+        rc = dalloc(s, (fmdg_pair_t **)&s->g.pairs, FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
     }
     FMDG_CK(cudaMemcpy((void *)s->g.mass, s->h_mass, sizeof(double) * nkinds, cudaMemcpyHostToDevice));
@@ -277,13 +307,14 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
 {
     if (nelem < 1 || nelem > FMDG_MAXE || Nrho < 3 || Nr2 < 3) return fmdg_set_error("fmdg_set_eam: bad sizes");
     Geo &g = s->g;
-    dfree((void *)g.eF); dfree((void *)g.eFDD); dfree((void *)g.erho);
-    dfree((void *)g.erhoDD); dfree((void *)g.ephi); dfree((void *)g.ephiDD);
+    if (s->eam_borrowed) drop_eam(s);
+    dfree(s, (void *)g.eF); dfree(s, (void *)g.eFDD); dfree(s, (void *)g.erho);
+    dfree(s, (void *)g.erhoDD); dfree(s, (void *)g.ephi); dfree(s, (void *)g.ephiDD);
     const size_t nF = (size_t)nelem * Nrho, nR = (size_t)nelem * Nr2, nP = (size_t)nelem * nelem * Nr2;
     int rc;
-    if ((rc = dalloc((double **)&g.eF, nF)) || (rc = dalloc((double **)&g.eFDD, nF)) ||
-        (rc = dalloc((double **)&g.erho, nR)) || (rc = dalloc((double **)&g.erhoDD, nR)) ||
-        (rc = dalloc((double **)&g.ephi, nP)) || (rc = dalloc((double **)&g.ephiDD, nP)))
+    if ((rc = dalloc(s, (double **)&g.eF, nF)) || (rc = dalloc(s, (double **)&g.eFDD, nF)) ||
+        (rc = dalloc(s, (double **)&g.erho, nR)) || (rc = dalloc(s, (double **)&g.erhoDD, nR)) ||
+        (rc = dalloc(s, (double **)&g.ephi, nP)) || (rc = dalloc(s, (double **)&g.ephiDD, nP)))
         return rc;
     FMDG_CK(cudaMemcpy((void *)g.eF, F, nF * 8, cudaMemcpyHostToDevice));
     FMDG_CK(cudaMemcpy((void *)g.eFDD, F_DD, nF * 8, cudaMemcpyHostToDevice));
@@ -302,8 +333,8 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     // algebraically the reference's a/b form (a = 1-b).  Computed in binary64;
     // the binary32 copy keeps k1 (the per-interval increment) to full relative
     // precision, which the two-sample difference y_k+1 - y_k would not.
-    dfree((void *)g.pk_rho); dfree((void *)g.pk_phi); dfree((void *)g.pk_F);
-    dfree((void *)g.pkf_rho); dfree((void *)g.pkf_phi); dfree((void *)g.pkf_F);
+    dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
+    dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
     auto pack = [&](const double *y, const double *ydd, double h, int npts, int nfun, const double4_32a **d64,
                     const float4 **d32) -> int {
         const size_t nint = (size_t)npts - 1;
@@ -320,7 +351,7 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
                 h32[f * nint + k] = make_float4((float)k0, (float)k1, (float)k2, (float)k3);
             }
         int rc2;
-        if ((rc2 = dalloc((double4_32a **)d64, h64.size())) || (rc2 = dalloc((float4 **)d32, h32.size()))) return rc2;
+        if ((rc2 = dalloc(s, (double4_32a **)d64, h64.size())) || (rc2 = dalloc(s, (float4 **)d32, h32.size()))) return rc2;
         FMDG_CK(cudaMemcpy((void *)*d64, h64.data(), h64.size() * sizeof(double4_32a), cudaMemcpyHostToDevice));
         FMDG_CK(cudaMemcpy((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
         return FMDG_OK;
@@ -336,6 +367,76 @@ extern "C" int fmdg_set_precision(fmdg_sys_t *s, int mode)
 {
     if (mode != FMDG_PREC_FP64 && mode != FMDG_PREC_MIXED) return fmdg_set_error("fmdg_set_precision: bad mode");
     s->g.prec = mode;
+    invalidate_graph(s);
+    return FMDG_OK;
+}
+
+// Neighbour-list entries per atom: 1.3x the pairs an atom of the densest
+// cell has within the list radius (largest cutoff + 0.01), at least 32.
+int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
+{
+    const Geo &g = s->g;
+    double rc2max = 0.0;
+    for (int k = 0; k < s->nkinds * s->nkinds; k++)
+    {
+        const fmdg_pair_t &pp = s->h_pairs[k];
+        const double r2 = pp.cat == FMDG_POT_MORSE ? pp.p[3] : pp.p[2];
+        if (r2 > rc2max) rc2max = r2;
+    }
+    if (!(rc2max > 0.0))
+    {
+        const double hmin = fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
+        rc2max = hmin * hmin;
+    }
+    const double rlist = sqrt(rc2max) + 1e-2;
+    int maxcell = 0;
+    for (int c = 0; c < ncell; c++) maxcell = cell_count[c] > maxcell ? cell_count[c] : maxcell;
+    const double nmax = maxcell / (g.cellh[0] * g.cellh[1] * g.cellh[2]);
+    const double est = 4.0 / 3.0 * 3.14159265358979 * rlist * rlist * rlist * nmax;
+    int maxnb = (int)(1.3 * est + 16);
+    maxnb = (maxnb + 7) & ~7;
+    if (maxnb < 32) maxnb = 32;
+    if (maxnb > 1024) maxnb = 1024;
+    return maxnb;
+}
+
+// device bytes of a system with n atoms, ncell cells and list capacity maxnb
+size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
+{
+    const size_t cap = n > 0 ? n : 1;
+    const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8;
+    const size_t per_cell = 2 * 4 + 5 * 4;
+    return cap * per_atom + (size_t)ncell * per_cell + 64 * 1024;
+}
+
+// packed launches: steps the system still takes
+int fmdg_set_steps_left(fmdg_sys_t *s, int steps)
+{
+    FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, steps_left), &steps, sizeof steps, cudaMemcpyHostToDevice));
+    return FMDG_OK;
+}
+
+// Use the EAM tables of another system on the same device without a copy;
+// the owner must outlive every borrower.
+extern "C" int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner)
+{
+    if (!owner || !owner->g.pk_rho) return fmdg_set_error("fmdg_share_eam: the owner has no EAM tables");
+    if (owner->device != s->device) return fmdg_set_error("fmdg_share_eam: different devices");
+    Geo &g = s->g;
+    if (!s->eam_borrowed)
+    {
+        dfree(s, (void *)g.eF); dfree(s, (void *)g.eFDD); dfree(s, (void *)g.erho);
+        dfree(s, (void *)g.erhoDD); dfree(s, (void *)g.ephi); dfree(s, (void *)g.ephiDD);
+        dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
+        dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
+    }
+    const Geo &o = owner->g;
+    g.eF = o.eF; g.eFDD = o.eFDD; g.erho = o.erho; g.erhoDD = o.erhoDD; g.ephi = o.ephi; g.ephiDD = o.ephiDD;
+    g.pk_rho = o.pk_rho; g.pk_phi = o.pk_phi; g.pk_F = o.pk_F;
+    g.pkf_rho = o.pkf_rho; g.pkf_phi = o.pkf_phi; g.pkf_F = o.pkf_F;
+    g.nelem = o.nelem; g.Nrho = o.Nrho; g.Nr2 = o.Nr2; g.drho = o.drho; g.dr2 = o.dr2;
+    g.inv_dr2 = o.inv_dr2; g.inv_drho = o.inv_drho;
+    s->eam_borrowed = true;
     invalidate_graph(s);
     return FMDG_OK;
 }
@@ -367,16 +468,16 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     for (int k = 0; k < 2; k++)
     {
         Side &S = g.side[k];
-        if ((rc = dalloc(&S.x, 3 * (size_t)cap)) || (rc = dalloc(&S.v, 3 * (size_t)cap)) ||
-            (rc = dalloc(&S.kind, cap)) || (rc = dalloc(&S.group, cap)) || (rc = dalloc(&S.atomid, cap)) ||
-            (rc = dalloc(&S.cell_of, cap)) || (rc = dalloc(&S.cell_start, (size_t)ncell + 1)))
+        if ((rc = dalloc(s, &S.x, 3 * (size_t)cap)) || (rc = dalloc(s, &S.v, 3 * (size_t)cap)) ||
+            (rc = dalloc(s, &S.kind, cap)) || (rc = dalloc(s, &S.group, cap)) || (rc = dalloc(s, &S.atomid, cap)) ||
+            (rc = dalloc(s, &S.cell_of, cap)) || (rc = dalloc(s, &S.cell_start, (size_t)ncell + 1)))
             return rc;
     }
-    if ((rc = dalloc(&g.F, 3 * (size_t)cap)) || (rc = dalloc(&g.vaream, cap)) ||
-        (rc = dalloc(&g.bdest, cap)) || (rc = dalloc(&g.bpath, cap)) || (rc = dalloc(&g.bslot, cap)) ||
-        (rc = dalloc(&g.brank, cap)) || (rc = dalloc(&g.bnewidx, cap)) ||
-        (rc = dalloc(&g.dep_count, 4 * (size_t)ncell)) || (rc = dalloc(&g.arr_base, (size_t)ncell + 1)) ||
-        (rc = dalloc(&g.bucket, cap)) || (rc = dalloc(&g.arr_slot, cap)))
+    if ((rc = dalloc(s, &g.F, 3 * (size_t)cap)) || (rc = dalloc(s, &g.vaream, cap)) ||
+        (rc = dalloc(s, &g.bdest, cap)) || (rc = dalloc(s, &g.bpath, cap)) || (rc = dalloc(s, &g.bslot, cap)) ||
+        (rc = dalloc(s, &g.brank, cap)) || (rc = dalloc(s, &g.bnewidx, cap)) ||
+        (rc = dalloc(s, &g.dep_count, 4 * (size_t)ncell)) || (rc = dalloc(s, &g.arr_base, (size_t)ncell + 1)) ||
+        (rc = dalloc(s, &g.bucket, cap)) || (rc = dalloc(s, &g.arr_slot, cap)))
         return rc;
     // neighbour list: size from the densest cell (an atom with more
     // candidates falls back to a direct stencil scan)
@@ -394,23 +495,17 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     }
     const double rlist = sqrt(rc2max) + 1e-2;
     g.rlist2 = (float)(rlist * rlist);
-    int maxcell = 0;
-    for (int c = 0; c < ncell; c++) maxcell = cell_count[c] > maxcell ? cell_count[c] : maxcell;
-    const double nmax = maxcell / (g.cellh[0] * g.cellh[1] * g.cellh[2]);
-    double est = 4.0 / 3.0 * 3.14159265358979 * rlist * rlist * rlist * nmax;
-    int maxnb = (int)(1.3 * est + 16);
-    maxnb = (maxnb + 7) & ~7;
-    if (maxnb < 32) maxnb = 32;
-    if (maxnb > 1024) maxnb = 1024;
+    const int maxnb = fmdg_list_capacity(s, cell_count, ncell);
     g.maxnb = maxnb;
     for (int d = 0; d < 3; d++) g.cellh_f[d] = (float)g.cellh[d];
-    if ((rc = dalloc(&g.xf4, cap)) || (rc = dalloc(&g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(&g.nbr_count, cap)))
+    if ((rc = dalloc(s, &g.xf4, cap)) || (rc = dalloc(s, &g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(s, &g.nbr_count, cap)))
         return rc;
     g.arr_lower = g.dep_count + ncell;
     g.arr_total = g.dep_count + 2 * ncell;
     g.bucket_fill = g.dep_count + 3 * ncell;
-    const int nb = fmdg_grid(cap, 128);
-    if ((rc = dalloc(&g.partials, (size_t)nb * 9 + 8))) return rc;
+    // partials for the smallest block size the tuner may pick (64)
+    const int nb = fmdg_grid(cap, 64);
+    if ((rc = dalloc(s, &g.partials, (size_t)nb * 9 + 8))) return rc;
     // host SoA staging
     std::vector<double> hx(3 * (size_t)cap, 0.0), hv(3 * (size_t)cap, 0.0);
     for (int i = 0; i < n; i++)
@@ -699,8 +794,8 @@ extern "C" int fmdg_turi_add(fmdg_sys_t *s, const int dims_local[3], const int g
     t.starttime = starttime;
     t.stoptime = stoptime;
     int rc;
-    if ((rc = dalloc(&t.acc, 5 * nc)) || (rc = dalloc(&t.tacc, nc)) || (rc = dalloc(&t.mass, nc)) ||
-        (rc = dalloc(&t.vcm, 3 * nc)) || (rc = dalloc(&t.Ti, nc)) || (rc = dalloc(&t.num, nc)))
+    if ((rc = dalloc(s, &t.acc, 5 * nc)) || (rc = dalloc(s, &t.tacc, nc)) || (rc = dalloc(s, &t.mass, nc)) ||
+        (rc = dalloc(s, &t.vcm, 3 * nc)) || (rc = dalloc(s, &t.Ti, nc)) || (rc = dalloc(s, &t.num, nc)))
         return rc;
     FMDG_CK(cudaMemset(t.num, 0, nc * sizeof(unsigned)));
     FMDG_CK(cudaMemset(t.mass, 0, nc * sizeof(double)));
@@ -723,9 +818,9 @@ extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, c
     int rc;
     if (!t.Te)
     {
-        if ((rc = dalloc(&t.Te, nz)) || (rc = dalloc(&t.Te2, nz)) || (rc = dalloc(&t.xi, nz)) ||
-            (rc = dalloc(&t.Ke, nz)) || (rc = dalloc(&t.Ce, nz)) || (rc = dalloc(&t.Gc, nz)) ||
-            (rc = dalloc(&t.srcz, nz)) || (rc = dalloc(&t.Te_pre, nz)))
+        if ((rc = dalloc(s, &t.Te, nz)) || (rc = dalloc(s, &t.Te2, nz)) || (rc = dalloc(s, &t.xi, nz)) ||
+            (rc = dalloc(s, &t.Ke, nz)) || (rc = dalloc(s, &t.Ce, nz)) || (rc = dalloc(s, &t.Gc, nz)) ||
+            (rc = dalloc(s, &t.srcz, nz)) || (rc = dalloc(s, &t.Te_pre, nz)))
             return rc;
         std::vector<double> m1(nz, -1.0), z0(nz, 0.0);
         FMDG_CK(cudaMemcpy(t.Te, m1.data(), nz * 8, cudaMemcpyHostToDevice));
@@ -736,8 +831,8 @@ extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, c
         FMDG_CK(cudaMemcpy(t.Ce, z0.data(), nz * 8, cudaMemcpyHostToDevice));
         FMDG_CK(cudaMemcpy(t.Gc, z0.data(), nz * 8, cudaMemcpyHostToDevice));
     }
-    dfree((void *)t.p.T_C); dfree((void *)t.p.Ct); dfree((void *)t.p.C_DD);
-    dfree((void *)t.p.T_G); dfree((void *)t.p.Gt); dfree((void *)t.p.G_DD);
+    dfree(s, (void *)t.p.T_C); dfree(s, (void *)t.p.Ct); dfree(s, (void *)t.p.C_DD);
+    dfree(s, (void *)t.p.T_G); dfree(s, (void *)t.p.Gt); dfree(s, (void *)t.p.G_DD);
     TtmParams q;
     memset(&q, 0, sizeof q);
     q.type = p->type; q.ratio = p->ratio; q.min_atoms = p->min_atoms; q.nC = p->nC; q.nG = p->nG;
@@ -750,7 +845,7 @@ extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, c
         if (p->nC < 2 || p->nG < 2 || !p->T_C || !p->Ct || !p->C_DD || !p->T_G || !p->Gt || !p->G_DD)
             return fmdg_set_error("fmdg_ttm_setup: type 2 needs C(Te) and G(Te) tables");
         auto up = [&](const double *h, int n, const double **d) -> int {
-            int r = dalloc((double **)d, n);
+            int r = dalloc(s, (double **)d, n);
             if (r) return r;
             FMDG_CK(cudaMemcpy((void *)*d, h, (size_t)n * 8, cudaMemcpyHostToDevice));
             return FMDG_OK;
@@ -963,7 +1058,8 @@ extern "C" int fmdg_flush_l2(fmdg_sys_t *s)
     if (!s->l2buf)
     {
         s->l2bytes = (size_t)256 << 20;
-        FMDG_CK(cudaMalloc(&s->l2buf, s->l2bytes));
+        int rc = dalloc(s, (char **)&s->l2buf, s->l2bytes);
+        if (rc) return rc;
         FMDG_CK(cudaMemset(s->l2buf, 0, s->l2bytes));
     }
     k_flush<<<1216, 256, 0, s->stream>>>((unsigned *)s->l2buf, s->l2bytes / 4);

@@ -122,17 +122,31 @@ __device__ __forceinline__ void scan_stencil(const Geo &g, const Side &S, int i,
     }
 }
 
-// list walk with stencil fallback
-template <typename F>
+// list walk with stencil fallback; UNROLL: four entries per round, their
+// index and coordinate loads independent and in flight together (the walk
+// is latency bound; pays where registers do not limit occupancy further)
+template <bool UNROLL, typename F>
 __device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i, CellXYZ ci, F &&f)
 {
     const int cnt = g.nbr_count[i];
     if (cnt <= g.maxnb)
     {
         const int cap = g.cap;
-        for (int k = 0; k < cnt; k++)
+        const int *col = g.nbr + i;
+        int k = 0;
+        if (UNROLL)
+            for (; k + 4 <= cnt; k += 4)
+            {
+                const int e0 = __ldg(col + (size_t)k * cap), e1 = __ldg(col + (size_t)(k + 1) * cap);
+                const int e2 = __ldg(col + (size_t)(k + 2) * cap), e3 = __ldg(col + (size_t)(k + 3) * cap);
+                f(e0 & 0x3ffffff, e0 >> 26);
+                f(e1 & 0x3ffffff, e1 >> 26);
+                f(e2 & 0x3ffffff, e2 >> 26);
+                f(e3 & 0x3ffffff, e3 >> 26);
+            }
+        for (; k < cnt; k++)
         {
-            const int e = g.nbr[(size_t)k * cap + i];
+            const int e = __ldg(col + (size_t)k * cap);
             f(e & 0x3ffffff, e >> 26);
         }
     }
@@ -249,10 +263,14 @@ struct Acc32
 
 // ---------------------------------------------------------------- kernels
 
-__global__ void k_prep_local(Geo g)
+template <class L>
+__global__ void k_prep_local(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     const Dyn *dyn = g.dyn;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= dyn->n) return;
     const Side S = g.side[dyn->cur];
     const CellXYZ c = cell_xyz(g, S.cell_of[i]);
@@ -263,10 +281,14 @@ __global__ void k_prep_local(Geo g)
     g.xf4[i] = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
 }
 
-__global__ void __launch_bounds__(128) k_nlist(Geo g)
+template <class L>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
     const Dyn *dyn = g.dyn;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     if (i >= dyn->n) return;
     const Side S = g.side[dyn->cur];
     const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
@@ -304,16 +326,20 @@ __global__ void __launch_bounds__(128) k_nlist(Geo g)
 
 // EAM pass 1 + embedding: rho_i = sum_j f_{elem(j)}(r_ij^2) (src/eam.h:270-406),
 // vaream_i = F'(rho_i), energy F(rho_i) (src/eam.c:160-179).
-template <bool MIXED, bool HYBRID>
-__global__ void __launch_bounds__(128) k_density(Geo g, int group)
+template <class L, bool MIXED, bool HYBRID>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__grid_constant__ const L loc)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const int group = g.st.group;
     __shared__ SmemPot sp;
     load_pot(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     double acc[1] = {0.0};
     if (i < n)
     {
@@ -330,7 +356,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double inv_h = g.inv_dr2;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
@@ -348,7 +374,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
                 const float4 xi = g.xf4[i];
                 const float inv_h = (float)g.inv_dr2;
                 Acc32<1> ac;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const float4 xj = g.xf4[j];
                     const int kj = __float_as_int(xj.w);
@@ -394,7 +420,7 @@ __global__ void __launch_bounds__(128) k_density(Geo g, int group)
         else
             g.vaream[i] = 0.0;
     }
-    block_reduce_store<1>(acc, g.partials + (size_t)gridDim.x * 8 + blockIdx.x);
+    block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
 }
 
 // Second level: sums the per-block partials in a fixed order, writes the
@@ -443,25 +469,23 @@ __global__ void k_reduce_final(Geo g, int nblocks, int keep_pe, int with_emb, in
     final_reduce(g, nblocks, keep_pe, with_emb, thermostat, dt, tau, T0);
 }
 
-// thermo-record arguments of the fused last-block reduction
-struct RedArgs
-{
-    int with_emb, thermostat;
-    double tau, T0;
-};
-
 // Pair forces + per-atom half energies; with finish=1 also the
 // velocity-Verlet finishStep (src/integrators.c:94-126) and its reductions.
-template <int CAT, bool MIXED>
-__global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, double dt, RedArgs ra)
+template <class L, int CAT, bool MIXED>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_constant__ const L loc, int finish)
 {
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const int group = g.st.group;
+    const double dt = g.st.dt;
     __shared__ SmemPot sp;
     load_pot(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = bx * blockDim.x + threadIdx.x;
     // pe, m v^2, m v (3), count
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (i < n)
@@ -481,7 +505,7 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
                 const double inv_h = g.inv_dr2;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
@@ -538,7 +562,7 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
                 const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? (float)g.vaream[i] : 0.f;
                 const float inv_h = (float)g.inv_dr2;
                 Acc32<4> ac;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const float4 xj = g.xf4[j];
                     const int kj = __float_as_int(xj.w);
@@ -655,17 +679,21 @@ __global__ void __launch_bounds__(128) k_force(Geo g, int group, int finish, dou
     block_reduce_store<6>(acc, blk);
     if (threadIdx.x == 0)
     {
-        for (int k = 0; k < 6; k++) g.partials[(size_t)k * gridDim.x + blockIdx.x] = blk[k];
+        for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
         __threadfence();
         ticket = atomicAdd(&g.dyn->blocks_done, 1u);
     }
     __syncthreads();
     // the last block to finish sums every block's partials in a fixed order
-    if (ticket == gridDim.x - 1)
+    if (ticket == (unsigned)nb - 1)
     {
         __threadfence();
-        final_reduce(g, gridDim.x, 0, ra.with_emb, ra.thermostat, dt, ra.tau, ra.T0);
-        if (threadIdx.x == 0) g.dyn->blocks_done = 0;
+        final_reduce(g, nb, 0, g.has_eam, g.st.thermostat, dt, g.st.tau, g.st.T0);
+        if (threadIdx.x == 0)
+        {
+            g.dyn->blocks_done = 0;
+            if (finish && g.dyn->steps_left > 0) g.dyn->steps_left--;
+        }
     }
 }
 
@@ -697,13 +725,47 @@ __global__ void __launch_bounds__(128) k_thermo(Geo g, int group)
 
 } // namespace
 
-int fmdg_force_blocks(const fmdg_sys_t *s) { return fmdg_grid(s->g.cap > 0 ? s->g.cap : 1, 128); }
+int fmdg_force_blocks(const fmdg_sys_t *s) { return fmdg_grid(s->g.cap > 0 ? s->g.cap : 1, s->fblk); }
+
+namespace {
+
+template <class L>
+void launch_nlist_t(const L &loc, int n_prep, int prep_threads, int nb, int blk, cudaStream_t st)
+{
+    k_prep_local<<<n_prep, prep_threads, 0, st>>>(loc);
+    k_nlist<<<nb, blk, 0, st>>>(loc);
+}
+
+template <class L>
+void launch_density_t(const L &loc, bool mixed, bool hyb, int nb, int blk, cudaStream_t st)
+{
+    if (mixed)
+    {
+        if (hyb) k_density<L, true, true><<<nb, blk, 0, st>>>(loc);
+        else k_density<L, true, false><<<nb, blk, 0, st>>>(loc);
+    }
+    else
+    {
+        if (hyb) k_density<L, false, true><<<nb, blk, 0, st>>>(loc);
+        else k_density<L, false, false><<<nb, blk, 0, st>>>(loc);
+    }
+}
+
+template <class L, bool MIXED>
+void launch_force_t(const L &loc, int cats, int finish, int nb, int blk, cudaStream_t st)
+{
+    const int ncat = __builtin_popcount(cats);
+    if (ncat > 1) k_force<L, CAT_HYBRID, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else if (cats == (1 << FMDG_POT_LJ)) k_force<L, CAT_LJ, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else if (cats == (1 << FMDG_POT_MORSE)) k_force<L, CAT_MORSE, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else k_force<L, CAT_EAM, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+}
+
+} // namespace
 
 int fmdg_launch_nlist(fmdg_sys_t *s)
 {
-    const int nb = fmdg_force_blocks(s);
-    k_prep_local<<<fmdg_grid(s->g.cap, 256), 256, 0, s->stream>>>(s->g);
-    k_nlist<<<nb, 128, 0, s->stream>>>(s->g);
+    launch_nlist_t(LocOne{s->g}, fmdg_grid(s->g.cap, 256), 256, fmdg_force_blocks(s), s->fblk, s->stream);
     s->launches += 2;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
@@ -713,49 +775,28 @@ int fmdg_launch_density(fmdg_sys_t *s, int group)
 {
     const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
     if (!eam) return FMDG_OK;
-    const int nb = fmdg_force_blocks(s);
-    const bool hyb = __builtin_popcount(s->cats) > 1;
-    const bool mixed = s->g.prec == FMDG_PREC_MIXED;
-    cudaStream_t st = s->stream;
-    if (mixed)
-    {
-        if (hyb) k_density<true, true><<<nb, 128, 0, st>>>(s->g, group);
-        else k_density<true, false><<<nb, 128, 0, st>>>(s->g, group);
-    }
-    else
-    {
-        if (hyb) k_density<false, true><<<nb, 128, 0, st>>>(s->g, group);
-        else k_density<false, false><<<nb, 128, 0, st>>>(s->g, group);
-    }
+    s->g.st.group = group;
+    launch_density_t(LocOne{s->g}, s->g.prec == FMDG_PREC_MIXED, __builtin_popcount(s->cats) > 1,
+                     fmdg_force_blocks(s), s->fblk, s->stream);
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
-}
-
-template <bool MIXED>
-static void launch_force_t(fmdg_sys_t *s, int nb, int group, int finish, double dt, RedArgs ra)
-{
-    Geo &g = s->g;
-    cudaStream_t st = s->stream;
-    const int ncat = __builtin_popcount(s->cats);
-    if (ncat > 1) k_force<CAT_HYBRID, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
-    else if (s->cats == (1 << FMDG_POT_LJ)) k_force<CAT_LJ, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
-    else if (s->cats == (1 << FMDG_POT_MORSE)) k_force<CAT_MORSE, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
-    else k_force<CAT_EAM, MIXED><<<nb, 128, 0, st>>>(g, group, finish, dt, ra);
 }
 
 // pair forces; the kernel's last block also writes the thermo record
 int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau,
                             double T0)
 {
+    StepArgs &a = s->g.st;
+    a.group = group;
+    a.dt = dt;
+    a.thermostat = thermostat;
+    a.tau = tau;
+    a.T0 = T0;
+    const LocOne L{s->g};
     const int nb = fmdg_force_blocks(s);
-    RedArgs ra;
-    ra.with_emb = (s->cats & (1 << FMDG_POT_EAM)) != 0;
-    ra.thermostat = thermostat;
-    ra.tau = tau;
-    ra.T0 = T0;
-    if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<true>(s, nb, group, finish, dt, ra);
-    else launch_force_t<false>(s, nb, group, finish, dt, ra);
+    if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<LocOne, true>(L, s->cats, finish, nb, s->fblk, s->stream);
+    else launch_force_t<LocOne, false>(L, s->cats, finish, nb, s->fblk, s->stream);
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
@@ -767,6 +808,38 @@ int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int ther
     if (rc) return rc;
     if ((rc = fmdg_launch_density(s, group))) return rc;
     return fmdg_launch_pair_forces(s, group, finish, dt, thermostat, tau, T0);
+}
+
+// Neighbour lists, EAM density and pair forces + finish step for every
+// system of a pack (one launch per kernel).
+// phases: bit 0 neighbour lists, bit 1 EAM density, bit 2 pair forces +
+// finish step (all three for a step).  Returns the kernels launched.
+int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
+{
+    const LocPack La{P.geos, P.amap}, Lf{P.geos, P.fmap};
+    cudaStream_t st = P.stream;
+    int n = 0;
+    if (phases & 1)
+    {
+        k_prep_local<<<P.nab, 128, 0, st>>>(La);
+        k_nlist<<<P.nfb, P.fblk, 0, st>>>(Lf);
+        n += 2;
+    }
+    const int cats = 1 << P.cat;
+    if ((phases & 2) && P.cat == FMDG_POT_EAM)
+    {
+        launch_density_t(Lf, P.mixed != 0, false, P.nfb, P.fblk, st);
+        n++;
+    }
+    if (phases & 4)
+    {
+        if (P.mixed) launch_force_t<LocPack, true>(Lf, cats, 1, P.nfb, P.fblk, st);
+        else launch_force_t<LocPack, false>(Lf, cats, 1, P.nfb, P.fblk, st);
+        n++;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -fmdg_fail("pack forces", e);
+    return n;
 }
 
 // thermo-only reduction (no force evaluation); keeps the potential energy

@@ -31,6 +31,8 @@ struct Dyn
     int any_move;       // a refresh moved at least one atom
     unsigned err;       // sticky error bits (FMDG_ERRBIT_*)
     unsigned blocks_done;   // ticket of the force kernel's last-block reduction
+    int steps_left;     // packed launches: steps this system still takes
+    int pad;
     double lambda;      // Berendsen scale for the next start step
     double time;        // simulation time (advanced by every step)
     double dt;          // time step of the current run (turi windows)
@@ -46,8 +48,17 @@ struct Side
     int *cell_start;
 };
 
+// integrator arguments of the step in flight (set by the host before a
+// launch or a capture; per system in packed launches)
+struct StepArgs
+{
+    double dt, tau, T0;
+    int group, thermostat;
+};
+
 struct Geo   // passed by value to kernels
 {
+    StepArgs st;
     int cap, ncell;
     int nc[3];
     int pbc[3];
@@ -126,7 +137,79 @@ struct fmdg_sys
     int nturi;
     int ttm_turi;                 // index of the TTM turi or -1
     int graph_mode;               // 0 velocity Verlet, 1 symplectic Euler
+    int fblk;                     // threads per block of the list/density/force kernels
+    bool eam_borrowed;            // EAM tables belong to another system
 };
+
+// ---- which system a thread block works on ------------------------------------
+// The step kernels are templates over a locator.
+//   LocOne : one system, its Geo in kernel parameter space.
+//   LocPack: many systems of one pair category and precision in one launch.
+//            map[b] = (system, block within the system, that system's block
+//            count); without a map, block b is system b.  The block copies
+//            its system's Geo into shared memory.  A system whose
+//            steps_left reached zero is skipped by every kernel.
+struct LocOne
+{
+    static constexpr int max_threads = 128;
+    static constexpr int min_blocks = 0;      // 0: register count left to the compiler
+    static constexpr bool unroll = false;
+    Geo g;
+};
+
+struct LocPack
+{
+    // the Geo copy in shared memory invites the compiler to keep its fields
+    // in registers; two 256-thread blocks per SM cap them at 128 (lower caps
+    // spill in the force kernels)
+    static constexpr int max_threads = 256;
+    static constexpr int min_blocks = 2;
+    static constexpr bool unroll = true;    // list walk four entries per round
+    const Geo *geos;
+    const int4 *map;
+};
+
+__device__ __forceinline__ const Geo &loc_geo(const LocOne &L, int &bx, int &nb)
+{
+    bx = blockIdx.x;
+    nb = gridDim.x;
+    return L.g;
+}
+
+__device__ __forceinline__ const Geo &loc_geo(const LocPack &L, int &bx, int &nb)
+{
+    __shared__ Geo sg;
+    __shared__ int4 sm;
+    if (threadIdx.x == 0) sm = L.map ? L.map[blockIdx.x] : make_int4((int)blockIdx.x, 0, 1, 0);
+    __syncthreads();
+    const int *src = (const int *)(L.geos + sm.x);
+    int *dst = (int *)&sg;
+    for (int k = threadIdx.x; k < (int)(sizeof(Geo) / 4); k += blockDim.x) dst[k] = src[k];
+    __syncthreads();
+    bx = sm.y;
+    nb = sm.z;
+    return sg;
+}
+
+__device__ __forceinline__ bool loc_idle(const LocOne &, const Geo &) { return false; }
+__device__ __forceinline__ bool loc_idle(const LocPack &, const Geo &g) { return g.dyn->steps_left <= 0; }
+
+// A pack: systems of one pair category and precision stepped together.
+struct fmdg_pack_launch
+{
+    cudaStream_t stream;
+    int nsys;
+    int cat;                    // FMDG_POT_* (single category)
+    int mixed;
+    const Geo *geos;            // device, nsys
+    const int4 *amap; int nab;  // 128-thread atom blocks
+    const int4 *cmap; int ncb;  // 128-thread cell blocks
+    const int4 *fmap; int nfb;  // force blocks of fblk threads
+    int fblk;
+};
+// both return the number of kernels launched, or minus a status
+int fmdg_pack_launch_refresh(const fmdg_pack_launch &P);
+int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases);
 
 // ---- helpers shared by the translation units --------------------------------
 int fmdg_fail(const char *where, cudaError_t e);
@@ -148,6 +231,9 @@ int fmdg_pack_tables(fmdg_sys_t *s);
 int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0);
 int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0);
 int fmdg_force_blocks(const fmdg_sys_t *s);
+int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell);
+size_t fmdg_bytes_estimate(int n, int ncell, int maxnb);
+int fmdg_set_steps_left(fmdg_sys_t *s, int steps);
 
 // refresh modes
 #define FMDG_REFRESH_ONLY  0     // positions already updated

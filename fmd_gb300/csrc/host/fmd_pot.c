@@ -378,6 +378,27 @@ bool _fmdh_pots_ready(fmd_t *md)
 
 /* Pair table, masses and EAM tables to the device (replaces the per-pair
    pointer chasing of the reference's pottable). */
+/* EAM tables of all elements as contiguous arrays in the device engine's
+   layout: F, F_DD [nelem*Nrho]; rho, rhoDD [nelem*Nr2]; phi, phiDD
+   [nelem*nelem*Nr2] */
+void _fmdh_eam_flatten(const eam_t *e, double *F, double *FDD, double *rho, double *rhoDD, double *phi,
+                       double *phiDD)
+{
+    const int ne = e->nelem;
+    for (int i = 0; i < ne; i++)
+    {
+        memcpy(F + (size_t)i * e->Nrho, e->el[i].F, sizeof(double) * e->Nrho);
+        memcpy(FDD + (size_t)i * e->Nrho, e->el[i].F_DD, sizeof(double) * e->Nrho);
+        memcpy(rho + (size_t)i * e->Nr2, e->el[i].rho, sizeof(double) * e->Nr2);
+        memcpy(rhoDD + (size_t)i * e->Nr2, e->el[i].rhoDD, sizeof(double) * e->Nr2);
+        for (int j = 0; j < ne; j++)
+        {
+            memcpy(phi + ((size_t)i * ne + j) * e->Nr2, e->phi[i * ne + j], sizeof(double) * e->Nr2);
+            memcpy(phiDD + ((size_t)i * ne + j) * e->Nr2, e->phiDD[i * ne + j], sizeof(double) * e->Nr2);
+        }
+    }
+}
+
 int _fmdh_upload_tables(fmd_t *md)
 {
     if (md->dev_tables_ok) return FMDG_OK;
@@ -427,18 +448,7 @@ int _fmdh_upload_tables(fmd_t *md)
         double *rhoDD = (double *)malloc(sizeof(double) * ne * e->Nr2);
         double *phi = (double *)malloc(sizeof(double) * ne * ne * e->Nr2);
         double *phiDD = (double *)malloc(sizeof(double) * ne * ne * e->Nr2);
-        for (int i = 0; i < ne; i++)
-        {
-            memcpy(F + (size_t)i * e->Nrho, e->el[i].F, sizeof(double) * e->Nrho);
-            memcpy(FDD + (size_t)i * e->Nrho, e->el[i].F_DD, sizeof(double) * e->Nrho);
-            memcpy(rho + (size_t)i * e->Nr2, e->el[i].rho, sizeof(double) * e->Nr2);
-            memcpy(rhoDD + (size_t)i * e->Nr2, e->el[i].rhoDD, sizeof(double) * e->Nr2);
-            for (int j = 0; j < ne; j++)
-            {
-                memcpy(phi + ((size_t)i * ne + j) * e->Nr2, e->phi[i * ne + j], sizeof(double) * e->Nr2);
-                memcpy(phiDD + ((size_t)i * ne + j) * e->Nr2, e->phiDD[i * ne + j], sizeof(double) * e->Nr2);
-            }
-        }
+        _fmdh_eam_flatten(e, F, FDD, rho, rhoDD, phi, phiDD);
         rc = fmdg_set_eam(md->dev, ne, e->Nrho, e->drho, e->Nr2, e->dr2, F, FDD, rho, rhoDD, phi, phiDD);
         free(F); free(FDD); free(rho); free(rhoDD); free(phi); free(phiDD);
         if (rc) return rc;

@@ -160,6 +160,8 @@ bool _fmdh_dev_ok(fmd_t *md, int rc, const char *what);
 double _fmdh_largest_cutoff(fmd_t *md);
 bool _fmdh_pots_ready(fmd_t *md);
 int _fmdh_upload_tables(fmd_t *md);
+void _fmdh_eam_flatten(const eam_t *e, double *F, double *FDD, double *rho, double *rhoDD, double *phi,
+                       double *phiDD);
 void _fmdh_pots_free(fmd_t *md);
 void _fmdh_spline_prepare(double h, const double *y, int n, double *yDD);
 void _fmdh_spline_prepare_adv(const double *x, const double *y, int n, double *yDD);

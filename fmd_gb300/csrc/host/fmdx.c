@@ -78,3 +78,23 @@ void fmdx_set_precision(fmd_t *md, int mode)
 /* distribute the atoms to the device without running (first half of
    fmd_dync_integrate) */
 int fmdx_distribute(fmd_t *md) { return _fmdh_distribute(md) ? 0 : -1; }
+
+/* Tables of an EAM potential loaded with fmd_pot_eam_alloy_load in the
+   layout of fmdg_set_eam (for callers that drive the device engine or the
+   served mode directly).  Sizes only when F is NULL.  Returns 0, or -1
+   when pot is not an EAM potential. */
+int fmdx_eam_tables(fmd_pot_t *pot, int *nelem, int *Nrho, double *drho, int *Nr2, double *dr2,
+                    double *cutoff_sqr, double *F, double *F_DD, double *rho, double *rhoDD, double *phi,
+                    double *phiDD)
+{
+    if (pot == NULL || pot->cat != POTCAT_EAM) return -1;
+    const eam_t *e = (const eam_t *)pot->data;
+    *nelem = e->nelem;
+    *Nrho = e->Nrho;
+    *drho = e->drho;
+    *Nr2 = e->Nr2;
+    *dr2 = e->dr2;
+    *cutoff_sqr = e->cutoff_sqr;
+    if (F != NULL) _fmdh_eam_flatten(e, F, F_DD, rho, rhoDD, phi, phiDD);
+    return 0;
+}

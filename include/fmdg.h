@@ -229,6 +229,94 @@ int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops);
 /* write a buffer larger than L2 so the next kernel starts cold */
 int fmdg_flush_l2(fmdg_sys_t *s);
 
+/* --- shared EAM tables ---------------------------------------------- */
+/* Use the EAM tables of `owner` (same device) without copying them; the
+   owner must outlive `s`.  Many systems with one potential then read one
+   copy of the tables (one L2 footprint). */
+int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner);
+
+/* --- served mode: continuous batching of independent jobs --------------
+   No counterpart in the reference, which runs one simulation per process
+   (one fmd_t, src/integrators.c:227-264).  Jobs wait in a FIFO queue until
+   the device bytes they need fit the HBM budget; admitted jobs of one pair
+   category and precision are stepped together by one launch per kernel
+   (velocity Verlet, NVE), chunk_steps steps per captured CUDA graph; the
+   threads per block of the list/density/force kernels are autotuned per
+   pack unless fixed with fmdg_srv_set_tuning.  A job's per-atom arithmetic
+   is the single-system arithmetic, independent of the other jobs. */
+typedef struct fmdg_server fmdg_server_t;
+
+typedef struct
+{
+    double l[3];              /* box lengths (A) */
+    int pbc[3];               /* periodic axes */
+    int nkinds;               /* 1..8 */
+    const double *mass;       /* [nkinds], internal units (src/potential.c:47) */
+    const int *eam_elem;      /* [nkinds] element in the EAM tables, or NULL */
+    const fmdg_pair_t *pairs; /* [nkinds*nkinds], one category for all pairs */
+    int eam_key;              /* EAM jobs: tables registered with fmdg_srv_set_eam */
+    int n;                    /* atoms */
+    const double *x, *v;      /* n*3 interleaved, positions inside [0, l) */
+    const unsigned *kind;     /* [n] */
+    int steps;                /* velocity-Verlet steps */
+    double dt;                /* time step (ps) */
+    int precision;            /* FMDG_PREC_* */
+    int keep_state;           /* keep the final positions/velocities/forces */
+} fmdg_job_desc_t;
+
+typedef struct
+{
+    int state;                /* 0 queued, 1 running, 2 done, 3 failed */
+    int error;                /* FMDG_E_* of a failed job */
+    int n, steps;
+    double t_submit, t_start, t_done;   /* seconds on the server clock */
+    fmdg_thermo_t first, last;          /* before the first step, after the last */
+    unsigned errbits;                   /* sticky device error bits */
+    unsigned pad;
+    double device_bytes;                /* admission estimate */
+} fmdg_job_result_t;
+
+typedef struct
+{
+    int queued, running;
+    long long admitted, finished, failed;
+    double atom_steps;                  /* completed atom-steps */
+    long long kernels;                  /* kernels launched (graph replays included) */
+    double bytes_in_use, bytes_peak;    /* admission accounting */
+    int pack_fblk[4][2];                /* tuned threads per block [category][mixed], 0 = not yet */
+    long long pack_chunks[4][2], pack_rebuilds[4][2];
+} fmdg_srv_stats_t;
+
+int  fmdg_srv_create(fmdg_server_t **out, int device, size_t hbm_budget, int max_jobs, int chunk_steps);
+void fmdg_srv_destroy(fmdg_server_t *srv);
+/* EAM tables shared by every job that names `key` (arguments as fmdg_set_eam) */
+int  fmdg_srv_set_eam(fmdg_server_t *srv, int key, int nelem, int Nrho, double drho, int Nr2, double dr2,
+                      const double *F, const double *F_DD, const double *rho, const double *rhoDD,
+                      const double *phi, const double *phiDD);
+/* 0: autotune (default); 64, 128 or 256: fixed threads per block */
+int  fmdg_srv_set_tuning(fmdg_server_t *srv, int fblk);
+/* queue a job (the description is copied) */
+int  fmdg_srv_submit(fmdg_server_t *srv, const fmdg_job_desc_t *job, long long *id);
+/* one turn of the serving loop (reap finished chunks, admit, launch);
+   wait=1 blocks on the oldest chunk when nothing new could be launched;
+   *active = queued + running jobs */
+int  fmdg_srv_progress(fmdg_server_t *srv, int wait, int *active);
+int  fmdg_srv_result(fmdg_server_t *srv, long long id, fmdg_job_result_t *out);
+/* final state of a finished keep_state job, cell order (n*3 interleaved) */
+int  fmdg_srv_state(fmdg_server_t *srv, long long id, double *x, double *v, double *F, unsigned *atomid);
+/* forget a finished job */
+int  fmdg_srv_release(fmdg_server_t *srv, long long id);
+int  fmdg_srv_now(fmdg_server_t *srv, double *seconds);
+int  fmdg_srv_stats(fmdg_server_t *srv, fmdg_srv_stats_t *out);
+/* benchmark helpers: admit every queued job that fits (no steps);
+   advance every admitted job by k chunks and return the device time;
+   one un-captured step of one pack timed phase by phase (ms[0] refresh,
+   ms[1] neighbour lists, ms[2] EAM density, ms[3] forces + finish step) */
+int  fmdg_srv_admit(fmdg_server_t *srv);
+int  fmdg_srv_run_resident(fmdg_server_t *srv, int k, float *ms);
+int  fmdg_srv_profile_pack(fmdg_server_t *srv, int category, int mixed, float ms[4], double *atoms,
+                           int *members);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,7 +62,18 @@ def _hybrid():
                 group=np.zeros(len(xc) + len(xa), np.int32), dt=0.001)
 
 
-SPECS = {"lj32k": _lj32k, "eam16k": _eam16k, "morse_slab": _morse_slab, "hybrid": _hybrid}
+def _morse_nc2():
+    """Smallest Morse cube of the served stream: l = 18.075 A, two cells per
+    axis (each cell is its own upper and lower neighbour, with two images)."""
+    x, v = workloads.fcc_state(5, 5, 5, 3.615, 600.0, 63.546, seed=36, disp=0.05)
+    x = np.mod(x, 18.075)
+    return dict(box=(18.075,) * 3, pbc=(1, 1, 1), kinds=[("Cu", 63.546)],
+                pots=[("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)], x=x, v=v,
+                kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), dt=0.001)
+
+
+SPECS = {"lj32k": _lj32k, "eam16k": _eam16k, "morse_slab": _morse_slab, "hybrid": _hybrid,
+         "morse_nc2": _morse_nc2}
 
 
 def build_both(lib, spec, work, precision=0):

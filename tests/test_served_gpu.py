@@ -1,0 +1,150 @@
+"""Served mode (fmdg_srv_*): packed multi-job stepping against the plain
+single-system path, and a job alone against the same job in a mix.
+
+A job's per-atom arithmetic in a pack is the single-system arithmetic, so
+positions, velocities and forces must be bit-identical (alone vs mix and
+pack vs single); the thermo record may differ in the grouping of block
+partial sums: kinetic and potential energy within 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+from fmd_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def L(gpu_lib):
+    return serve.bind(gpu_lib.L)
+
+
+@pytest.fixture(scope="module")
+def eam(L):
+    return serve.eam_tables(L)
+
+
+def _job(pot, n, T, seed):
+    j = dict(pot=pot, ncell=n, T=T, seed=seed)
+    x, v, l = serve.job_atoms(j)
+    return x, v, l
+
+
+def _thermo_close(a, b):
+    for f in ("kinetic", "potential"):
+        x, y = getattr(a, f), getattr(b, f)
+        assert abs(x - y) <= 1e-12 * max(abs(x), abs(y), 1e-30), (f, x, y)
+
+
+@pytest.mark.parametrize("pot", ["lj", "morse", "eam"])
+@pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
+def test_pack_equals_single(L, eam, pot, precision):
+    x, v, l = _job(pot, 6, 700.0, 11)
+    steps = 25
+    one = serve.Single(L, pot, x, v, l, precision=precision, eam=eam)
+    one.steps(steps)
+    xs, vs, Fs, ids = one.state()
+    ts = one.thermo()
+    one.close()
+    srv = serve.Server(L, chunk_steps=8, eam=eam)
+    srv.set_tuning(128)
+    jid = srv.submit(pot, x, v, l, steps, precision=precision, keep_state=True)
+    srv.drain()
+    r = srv.result(jid)
+    assert r.state == 2 and r.errbits == 0
+    xp, vp, Fp, idp = srv.state(jid, len(x))
+    srv.close()
+    np.testing.assert_array_equal(ids, idp)
+    np.testing.assert_array_equal(xs, xp)
+    np.testing.assert_array_equal(vs, vp)
+    np.testing.assert_array_equal(Fs, Fp)
+    _thermo_close(ts, r.last)
+
+
+def test_alone_vs_mix(L, eam):
+    """Each job alone and in a mix of 9 jobs of three potentials and both
+    precisions, uneven sizes and step counts, chunk boundaries falling
+    inside jobs, the autotuner switching block sizes between chunks."""
+    specs = [("eam", 6, 900.0, 21, 37, 1), ("lj", 5, 80.0, 22, 50, 1), ("morse", 5, 500.0, 23, 19, 1),
+             ("eam", 9, 300.0, 24, 44, 1), ("lj", 7, 120.0, 25, 9, 0), ("morse", 7, 1100.0, 26, 31, 0),
+             ("eam", 5, 1200.0, 27, 23, 0), ("lj", 6, 60.0, 28, 40, 1), ("morse", 6, 250.0, 29, 28, 1)]
+    jobs = [(_job(p, n, T, s), st, pr, p) for (p, n, T, s, st, pr) in specs]
+    alone = []
+    for (x, v, l), st, pr, p in jobs:
+        srv = serve.Server(L, chunk_steps=8, eam=eam)
+        jid = srv.submit(p, x, v, l, st, precision=pr, keep_state=True)
+        srv.drain()
+        alone.append((srv.result(jid), srv.state(jid, len(x))))
+        srv.close()
+    srv = serve.Server(L, chunk_steps=8, eam=eam)
+    ids = [srv.submit(p, x, v, l, st, precision=pr, keep_state=True) for (x, v, l), st, pr, p in jobs]
+    srv.drain()
+    st = srv.stats()
+    assert st.finished == len(jobs) and st.failed == 0
+    for k, jid in enumerate(ids):
+        r = srv.result(jid)
+        assert r.state == 2 and r.errbits == 0
+        ra, (xa, va, Fa, ia) = alone[k]
+        xm, vm, Fm, im = srv.state(jid, len(xa))
+        np.testing.assert_array_equal(ia, im)
+        np.testing.assert_array_equal(xa, xm)
+        np.testing.assert_array_equal(va, vm)
+        np.testing.assert_array_equal(Fa, Fm)
+        _thermo_close(ra.last, r.last)
+        _thermo_close(ra.first, r.first)
+    srv.close()
+
+
+def test_admission_budget(L, eam):
+    """A budget that holds about two jobs: every job still finishes, the
+    admission accounting never exceeds the budget, results equal an
+    unconstrained run's."""
+    specs = [("lj", 6, 100.0, 41, 20), ("morse", 6, 300.0, 42, 12), ("eam", 7, 600.0, 43, 17),
+             ("lj", 5, 90.0, 44, 30), ("eam", 6, 900.0, 45, 8), ("morse", 5, 700.0, 46, 25)]
+    jobs = [(_job(p, n, T, s), st, p) for (p, n, T, s, st) in specs]
+    free = serve.Server(L, chunk_steps=4, eam=eam)
+    fids = [free.submit(p, x, v, l, st, keep_state=True) for (x, v, l), st, p in jobs]
+    free.drain()
+    sizes = [free.result(j).device_bytes for j in fids]
+    budget = int(2.2 * max(sizes))
+    tight = serve.Server(L, budget_bytes=budget, chunk_steps=4, eam=eam)
+    tids = [tight.submit(p, x, v, l, st, keep_state=True) for (x, v, l), st, p in jobs]
+    tight.drain()
+    s = tight.stats()
+    assert s.finished == len(jobs) and s.failed == 0
+    assert s.bytes_peak <= budget
+    for a, b, ((x, v, l), st, p) in zip(fids, tids, jobs):
+        xa = free.state(a, len(x))
+        xb = tight.state(b, len(x))
+        for u, w in zip(xa, xb):
+            np.testing.assert_array_equal(u, w)
+    free.close()
+    tight.close()
+
+
+def test_oversize_job_fails_cleanly(L, eam):
+    srv = serve.Server(L, budget_bytes=100000, chunk_steps=4, eam=eam)
+    x, v, l = _job("lj", 6, 100.0, 51)
+    jid = srv.submit("lj", x, v, l, 5)
+    srv.drain()
+    r = srv.result(jid)
+    assert r.state == 3 and r.error == 3
+    srv.close()
+
+
+@pytest.mark.parametrize("pot", ["lj", "morse", "eam"])
+def test_mixed_force_error_bound(L, eam, pot):
+    """Mixed precision against binary64 at identical positions of a
+    thermalised cube (1200 K, 20 binary64 steps): max |F32 - F64| <= 1e-5
+    max |F64|."""
+    x, v, l = _job(pot, 7, 1200.0, 61)
+    one = serve.Single(L, pot, x, v, l, precision=serve.PREC_FP64, eam=eam)
+    one.steps(20)
+    serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
+    F64 = one.state()[2]
+    serve.check(L, L.fmdg_set_precision(one.h, serve.PREC_MIXED), "precision")
+    serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
+    F32 = one.state()[2]
+    one.close()
+    err = np.abs(F32 - F64).max() / np.abs(F64).max()
+    assert err <= 1e-5, err
