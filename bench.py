@@ -391,6 +391,10 @@ def run_served(args):
                      "atoms": atoms, "jobs": members, "threads_per_block": tuned[p]}
     fleet.close()
     value = n_atoms * K / (ms * 1e-3)
+    if args.only == "fleet":
+        return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1, "steps": K,
+                "warmup": W, "ms_per_step": ms / K, "config": served_config(args), "gpu_launches": int(k1 - k0),
+                "phases": phases, "clocks": clocks, "note": "resident fleet only (--only fleet)"}
     # peak of the binary32 FMA pipe (measured microkernel)
     h = C.c_void_p()
     serve.check(L, L.fmdg_create(C.byref(h), 0), "create")
@@ -556,6 +560,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
     ap.add_argument("--workload", default="served", choices=["served", "eam256k"])
+    ap.add_argument("--only", default="all", choices=["all", "fleet"],
+                    help="served: 'fleet' times the resident fleet only (profiling runs)")
     ap.add_argument("--jobs", type=int, default=SERVED_JOBS, help="served: jobs of the stream sample")
     ap.add_argument("--step-scale", type=float, default=SERVED_STEP_SCALE,
                     help="served: factor on step counts and arrival times")

@@ -405,14 +405,14 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
 int fmdg_pack_launch_refresh(const fmdg_pack_launch &P)
 {
     cudaStream_t st = P.stream;
-    const LocPack La{P.geos, P.amap}, Lc{P.geos, P.cmap}, Ls{P.geos, nullptr};
-    k_bin_clear<<<P.ncb, 128, 0, st>>>(Lc);
-    k_bin_classify<<<P.nab, 128, 0, st>>>(La, FMDG_REFRESH_VV);
-    k_bin_scan<<<P.nsys, 1024, 0, st>>>(Ls);
-    k_bin_cells<<<P.ncb, 128, 0, st>>>(Lc);
-    k_bin_arrivals<<<P.ncb, 128, 0, st>>>(Lc);
-    k_bin_scatter<<<P.nab, 128, 0, st>>>(La);
-    k_bin_flip<<<P.nsys, 32, 0, st>>>(Ls, FMDG_REFRESH_VV);
+    const int nab = P.la.bstart[P.nsys], ncb = P.lc.bstart[P.nsys];
+    k_bin_clear<<<ncb, 128, 0, st>>>(P.lc);
+    k_bin_classify<<<nab, 128, 0, st>>>(P.la, FMDG_REFRESH_VV);
+    k_bin_scan<<<P.nsys, 1024, 0, st>>>(P.ls);
+    k_bin_cells<<<ncb, 128, 0, st>>>(P.lc);
+    k_bin_arrivals<<<ncb, 128, 0, st>>>(P.lc);
+    k_bin_scatter<<<nab, 128, 0, st>>>(P.la);
+    k_bin_flip<<<P.nsys, 32, 0, st>>>(P.ls, FMDG_REFRESH_VV);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return -fmdg_fail("pack refresh", e);
     return 7;

@@ -64,8 +64,8 @@ void free_atoms(fmdg_sys_t *s)
         memset(&S, 0, sizeof S);
     }
     dfree(s, g.F); dfree(s, g.vaream);
-    dfree(s, g.xf4); dfree(s, g.nbr); dfree(s, g.nbr_count);
-    g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr;
+    dfree(s, g.xf4); dfree(s, g.nbr); dfree(s, g.nbr_count); dfree(s, g.fpf);
+    g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr; g.fpf = nullptr;
     dfree(s, g.bdest); dfree(s, g.bpath); dfree(s, g.bslot); dfree(s, g.brank); dfree(s, g.bnewidx);
     dfree(s, g.dep_count); dfree(s, g.arr_base); dfree(s, g.bucket); dfree(s, g.arr_slot);
     dfree(s, g.partials);
@@ -498,7 +498,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     const int maxnb = fmdg_list_capacity(s, cell_count, ncell);
     g.maxnb = maxnb;
     for (int d = 0; d < 3; d++) g.cellh_f[d] = (float)g.cellh[d];
-    if ((rc = dalloc(s, &g.xf4, cap)) || (rc = dalloc(s, &g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(s, &g.nbr_count, cap)))
+    if ((rc = dalloc(s, &g.fpf, cap)) || (rc = dalloc(s, &g.xf4, cap)) || (rc = dalloc(s, &g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(s, &g.nbr_count, cap)))
         return rc;
     g.arr_lower = g.dep_count + ncell;
     g.arr_total = g.dep_count + 2 * ncell;

@@ -45,6 +45,7 @@ struct SmemPot
     float pf[FMDG_MAXK * FMDG_MAXK][4];
     double mass[FMDG_MAXK];
     int elem[FMDG_MAXK];
+    float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
 };
 
 __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
@@ -60,6 +61,9 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
         sp.mass[k] = g.mass[k];
         sp.elem[k] = g.eam_elem[k];
     }
+    for (int c = threadIdx.x; c < 27; c += blockDim.x)
+        sp.off[c] = make_float4((float)(c / 9 - 1) * g.cellh_f[0], (float)((c / 3) % 3 - 1) * g.cellh_f[1],
+                                (float)(c % 3 - 1) * g.cellh_f[2], 0.f);
     __syncthreads();
 }
 
@@ -178,11 +182,21 @@ __device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const doub
 }
 
 // binary32 pair geometry from cell-local coordinates
-__device__ __forceinline__ float3 geom32(const Geo &g, float4 xi, float4 xj, int code)
+__device__ __forceinline__ float3 geom32(const SmemPot &sp, float4 xi, float4 xj, int code)
 {
-    return make_float3(xi.x - xj.x - (float)off_x(code) * g.cellh_f[0],
-                       xi.y - xj.y - (float)off_y(code) * g.cellh_f[1],
-                       xi.z - xj.z - (float)off_z(code) * g.cellh_f[2]);
+    const float4 o = sp.off[code];
+    return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
+}
+
+// interval index k = floor(q) (clamped to kmax) and fraction b = q - k of a
+// binary32 table coordinate 0 <= q < 2^23, without conversion instructions:
+// adding 2^23 rounding towards minus infinity leaves floor(q) in the
+// significand
+__device__ __forceinline__ int table_index(float q, float kmax, float &b)
+{
+    const float fl = fminf(__fadd_rd(q, 8388608.f) - 8388608.f, kmax);
+    b = q - fl;
+    return __float_as_int(fl + 8388608.f) - 0x4B000000;
 }
 
 // natural cubic spline on a uniform grid (src/cspline.h:26-27) as a cubic
@@ -207,9 +221,8 @@ __device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
 // is r2 (binary32) within rc2?  Near the cutoff the decision is taken in
 // binary64 from the absolute positions, as the reference does.
 __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i, CellXYZ ci, int j, int code,
-                                             float r2f, double rc2)
+                                             float r2f, float rc2f, double rc2)
 {
-    const float rc2f = (float)rc2;
     if (fabsf(r2f - rc2f) > 1e-4f * rc2f) return r2f < rc2f;
     const int cap = g.cap;
     const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
@@ -303,11 +316,12 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist(__grid_
         const int jy = nb_axis(g, 1, ci.y, off_y(code), &sdummy);
         const int jz = nb_axis(g, 2, ci.z, off_z(code), &sdummy);
         if (jx < 0 || jy < 0 || jz < 0) continue;
-        const int nb = jz + g.nc[2] * (jy + g.nc[1] * jx);
-        const int jb = S.cell_start[nb], je = S.cell_start[nb + 1];
-        const float ox = (float)off_x(code) * g.cellh_f[0];
-        const float oy = (float)off_y(code) * g.cellh_f[1];
-        const float oz = (float)off_z(code) * g.cellh_f[2];
+        const int cx = off_x(code), cy = off_y(code), cz = off_z(code);
+        const int c = jz + g.nc[2] * (jy + g.nc[1] * jx);
+        const int jb = S.cell_start[c], je = S.cell_start[c + 1];
+        const float ox = (float)cx * g.cellh_f[0];
+        const float oy = (float)cy * g.cellh_f[1];
+        const float oz = (float)cz * g.cellh_f[2];
         for (int j = jb; j < je; j++)
         {
             if (code == 13 && j == i) continue;
@@ -373,6 +387,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             {
                 const float4 xi = g.xf4[i];
                 const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
                 Acc32<1> ac;
                 for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
@@ -380,13 +395,13 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     const int kj = __float_as_int(xj.w);
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + kj];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                    const float3 rv = geom32(g, xi, xj, code);
+                    const float3 rv = geom32(sp, xi, xj, code);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                    if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                    if (within_cut32(g, S, i, ci, j, code, r2, sp.pf[ki * nk + kj][2], pp.p[2]))
                     {
-                        const float q = r2 * inv_h;
-                        const int ir2 = min((int)q, nint - 1);
-                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], q - (float)ir2);
+                        float b;
+                        const int ir2 = table_index(r2 * inv_h, kmax, b);
+                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], b);
                         ac.tick();
                     }
                 });
@@ -413,12 +428,17 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             {
                 const float b = (float)(qr - irho);
                 const float4 t = g.pkf_F[(size_t)ei * nrint + irho];
-                g.vaream[i] = (double)spl_der(t, b, (float)g.inv_drho);
+                const float fp = spl_der(t, b, (float)g.inv_drho);
+                g.vaream[i] = (double)fp;
+                g.fpf[i] = fp;
                 acc[0] = (double)spl_val(t, b);
             }
         }
         else
+        {
             g.vaream[i] = 0.0;
+            if (MIXED) g.fpf[i] = 0.f;
+        }
     }
     block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
 }
@@ -559,8 +579,9 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
             else
             {
                 const float4 xi = g.xf4[i];
-                const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? (float)g.vaream[i] : 0.f;
+                const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpf[i] : 0.f;
                 const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
                 Acc32<4> ac;
                 for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
@@ -569,13 +590,13 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     const int pidx = ki * nk + kj;
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
-                    const float3 rv = geom32(g, xi, xj, code);
+                    const float3 rv = geom32(sp, xi, xj, code);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     if (cat == FMDG_POT_LJ)
                     {
-                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                        if (within_cut32(g, S, i, ci, j, code, r2, sp.pf[pidx][2], pp.p[2]))
                         {
-                            const float inv_r2 = __frcp_rn(r2);
+                            const float inv_r2 = __fdividef(1.f, r2);
                             const float inv_rs2 = sp.pf[pidx][1] * inv_r2;
                             const float inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
                             const float inv_rs12 = inv_rs6 * inv_rs6;
@@ -590,11 +611,11 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     }
                     else if (cat == FMDG_POT_MORSE)
                     {
-                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[3]))
+                        if (within_cut32(g, S, i, ci, j, code, r2, sp.pf[pidx][3], pp.p[3]))
                         {
                             const float D0 = sp.pf[pidx][0], al = sp.pf[pidx][1], r0 = sp.pf[pidx][2];
-                            const float r = sqrtf(r2);
-                            const float inv_r = __frcp_rn(r);
+                            const float inv_r = rsqrtf(r2);
+                            const float r = r2 * inv_r;
                             const float e1 = expf(-al * (r - r0));
                             const float e2 = e1 * e1;
                             const float factor = 2.f * al * D0 * inv_r * (e2 - e1);
@@ -607,18 +628,17 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     }
                     else if (cat == FMDG_POT_EAM)
                     {
-                        if (within_cut32(g, S, i, ci, j, code, r2, pp.p[2]))
+                        if (within_cut32(g, S, i, ci, j, code, r2, sp.pf[pidx][2], pp.p[2]))
                         {
-                            const float q = r2 * inv_h;
-                            const int ir2 = min((int)q, nint - 1);
-                            const float b = q - (float)ir2;
+                            float b;
+                            const int ir2 = table_index(r2 * inv_h, kmax, b);
                             const int ei = pp.iloc, ej = pp.jloc;
                             const float4 tph = g.pkf_phi[((size_t)ei * ne + ej) * nint + ir2];
                             const float phi_d = spl_der(tph, b, inv_h);
                             const float rho_ip = spl_der(g.pkf_rho[(size_t)ei * nint + ir2], b, inv_h);
                             const float rho_jp = (ei == ej) ? rho_ip
                                                : spl_der(g.pkf_rho[(size_t)ej * nint + ir2], b, inv_h);
-                            const float mag = 2.f * (fpi * rho_jp + (float)g.vaream[j] * rho_ip + phi_d);
+                            const float mag = 2.f * (fpi * rho_jp + g.fpf[j] * rho_ip + phi_d);
                             ac.part[0] -= mag * rv.x;
                             ac.part[1] -= mag * rv.y;
                             ac.part[2] -= mag * rv.z;
@@ -816,25 +836,25 @@ int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int ther
 // finish step (all three for a step).  Returns the kernels launched.
 int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
 {
-    const LocPack La{P.geos, P.amap}, Lf{P.geos, P.fmap};
     cudaStream_t st = P.stream;
+    const int nab = P.la.bstart[P.nsys], nfb = P.lf.bstart[P.nsys];
     int n = 0;
     if (phases & 1)
     {
-        k_prep_local<<<P.nab, 128, 0, st>>>(La);
-        k_nlist<<<P.nfb, P.fblk, 0, st>>>(Lf);
+        k_prep_local<<<nab, 128, 0, st>>>(P.la);
+        k_nlist<<<nfb, P.fblk, 0, st>>>(P.lf);
         n += 2;
     }
     const int cats = 1 << P.cat;
     if ((phases & 2) && P.cat == FMDG_POT_EAM)
     {
-        launch_density_t(Lf, P.mixed != 0, false, P.nfb, P.fblk, st);
+        launch_density_t(P.lf, P.mixed != 0, false, nfb, P.fblk, st);
         n++;
     }
     if (phases & 4)
     {
-        if (P.mixed) launch_force_t<LocPack, true>(Lf, cats, 1, P.nfb, P.fblk, st);
-        else launch_force_t<LocPack, false>(Lf, cats, 1, P.nfb, P.fblk, st);
+        if (P.mixed) launch_force_t<LocPack, true>(P.lf, cats, 1, nfb, P.fblk, st);
+        else launch_force_t<LocPack, false>(P.lf, cats, 1, nfb, P.fblk, st);
         n++;
     }
     cudaError_t e = cudaGetLastError();

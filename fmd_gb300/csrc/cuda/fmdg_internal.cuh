@@ -65,6 +65,7 @@ struct Geo   // passed by value to kernels
     double l[3], cellh[3], inv_cellh[3];
     Side side[2];
     double *F, *vaream;
+    float *fpf;        // binary32 copy of F'(rho) (mixed-precision EAM force pass)
     // per-step neighbour list (built after every refresh)
     float4 *xf4;       // cell-local coordinates (binary32) + kind bits, current order
     int *nbr;          // nbr[k*cap + i] = j | (stencil offset code << 26)
@@ -144,11 +145,16 @@ struct fmdg_sys
 // ---- which system a thread block works on ------------------------------------
 // The step kernels are templates over a locator.
 //   LocOne : one system, its Geo in kernel parameter space.
-//   LocPack: many systems of one pair category and precision in one launch.
-//            map[b] = (system, block within the system, that system's block
-//            count); without a map, block b is system b.  The block copies
-//            its system's Geo into shared memory.  A system whose
+//   LocPack: up to FMDG_PACK_MAX systems of one pair category and precision
+//            in one launch, their Geo copies in kernel parameter space too.
+//            bstart[s] is the first block of system s (bstart[nsys] = the
+//            grid); a block finds its system by bisection over bstart.  The
+//            index depends on blockIdx and parameters only, so the compiler
+//            reads the Geo fields as uniform constant-bank loads instead of
+//            holding them in per-thread registers.  A system whose
 //            steps_left reached zero is skipped by every kernel.
+#define FMDG_PACK_MAX 32
+
 struct LocOne
 {
     static constexpr int max_threads = 128;
@@ -159,15 +165,14 @@ struct LocOne
 
 struct LocPack
 {
-    // the Geo copy in shared memory invites the compiler to keep its fields
-    // in registers; two 256-thread blocks per SM cap them at 128 (lower caps
-    // spill in the force kernels)
     static constexpr int max_threads = 256;
-    static constexpr int min_blocks = 2;
-    static constexpr bool unroll = true;    // list walk four entries per round
-    const Geo *geos;
-    const int4 *map;
+    static constexpr int min_blocks = 0;
+    static constexpr bool unroll = true;      // list walk four entries per round
+    int nsys;
+    int bstart[FMDG_PACK_MAX + 1];
+    Geo geos[FMDG_PACK_MAX];
 };
+static_assert(sizeof(LocPack) < 32000, "a packed launch's parameters exceed the 32 KB limit");
 
 __device__ __forceinline__ const Geo &loc_geo(const LocOne &L, int &bx, int &nb)
 {
@@ -178,34 +183,35 @@ __device__ __forceinline__ const Geo &loc_geo(const LocOne &L, int &bx, int &nb)
 
 __device__ __forceinline__ const Geo &loc_geo(const LocPack &L, int &bx, int &nb)
 {
-    __shared__ Geo sg;
-    __shared__ int4 sm;
-    if (threadIdx.x == 0) sm = L.map ? L.map[blockIdx.x] : make_int4((int)blockIdx.x, 0, 1, 0);
-    __syncthreads();
-    const int *src = (const int *)(L.geos + sm.x);
-    int *dst = (int *)&sg;
-    for (int k = threadIdx.x; k < (int)(sizeof(Geo) / 4); k += blockDim.x) dst[k] = src[k];
-    __syncthreads();
-    bx = sm.y;
-    nb = sm.z;
-    return sg;
+    const int b = blockIdx.x;
+    int lo = 0, hi = L.nsys;
+    while (hi - lo > 1)
+    {
+        const int mid = (lo + hi) >> 1;
+        if (L.bstart[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    bx = b - L.bstart[lo];
+    nb = L.bstart[lo + 1] - L.bstart[lo];
+    return L.geos[lo];
 }
 
 __device__ __forceinline__ bool loc_idle(const LocOne &, const Geo &) { return false; }
 __device__ __forceinline__ bool loc_idle(const LocPack &, const Geo &g) { return g.dyn->steps_left <= 0; }
 
-// A pack: systems of one pair category and precision stepped together.
+// A pack: systems of one pair category and precision stepped together; one
+// locator per block shape (its grid is bstart[nsys]).
 struct fmdg_pack_launch
 {
     cudaStream_t stream;
     int nsys;
     int cat;                    // FMDG_POT_* (single category)
     int mixed;
-    const Geo *geos;            // device, nsys
-    const int4 *amap; int nab;  // 128-thread atom blocks
-    const int4 *cmap; int ncb;  // 128-thread cell blocks
-    const int4 *fmap; int nfb;  // force blocks of fblk threads
-    int fblk;
+    int fblk;                   // threads per block of the list/density/force kernels
+    LocPack la;                 // 128-thread atom blocks
+    LocPack lc;                 // 128-thread cell blocks
+    LocPack lf;                 // force blocks of fblk threads
+    LocPack ls;                 // one block per system
 };
 // both return the number of kernels launched, or minus a status
 int fmdg_pack_launch_refresh(const fmdg_pack_launch &P);

@@ -90,26 +90,38 @@ struct Chunk
     bool timed;         // counts for the tuner
 };
 
+// At most FMDG_PACK_MAX systems (their Geo travel as kernel parameters);
+// more systems of one category and precision form further packs, each on
+// its own stream.
 struct Pack
 {
     int cat = 0, mixed = 0;
     cudaStream_t stream = nullptr;
     std::vector<Job *> members;
     bool dirty = true;
-    char *dbuf = nullptr;          // Geo table + block maps of the membership
     fmdg_pack_launch P;
     cudaGraphExec_t exec = nullptr;
     int exec_fblk = 0;
     int exec_kernels = 0;          // kernels per replay of the chunk graph
     std::deque<Chunk> inflight;
     std::vector<std::pair<long long, cudaGraphExec_t>> old_execs;   // (last chunk seq, exec)
-    // autotuner
-    int fblk = 128;
-    bool tuned = false;
-    int tune_step = 0;
-    double tune_cost[3] = {1e300, 1e300, 1e300};
     long long chunks = 0, rebuilds = 0;
     double atom_steps = 0.0;
+    int active() const
+    {
+        int a = 0;
+        for (const Job *j : members) a += j->left > 0;
+        return a;
+    }
+};
+
+// block-size autotuner of one category and precision (shared by its packs)
+struct Tuner
+{
+    int fblk = 128;
+    bool tuned = false;
+    int step = 0;
+    double cost[3] = {1e300, 1e300, 1e300};
 };
 
 const int TUNE_BLK[3] = {64, 128, 256};
@@ -134,7 +146,8 @@ struct fmdg_server
     std::deque<Job *> queue;
     std::map<long long, Job *> jobs;
     int running = 0;
-    Pack packs[4][2];                 // [category][mixed]
+    std::vector<Pack *> packs[4][2];  // [category][mixed]
+    Tuner tuners[4][2];
     std::map<int, fmdg_sys_t *> eam_owner;   // shared EAM tables by key
     std::vector<cudaEvent_t> free_events;
     long long admitted = 0, finished = 0, failed = 0;
@@ -160,6 +173,38 @@ cudaEvent_t get_event(fmdg_server_t *S)
 }
 
 void put_event(fmdg_server_t *S, cudaEvent_t e) { if (e) S->free_events.push_back(e); }
+
+template <typename F>
+void each_pack(fmdg_server_t *S, F f)
+{
+    for (auto &row : S->packs)
+        for (auto &v : row)
+            for (Pack *p : v) f(*p);
+}
+
+int want_fblk(const fmdg_server_t *S, const Pack &p)
+{
+    if (S->fixed_fblk) return S->fixed_fblk;
+    const Tuner &t = S->tuners[p.cat][p.mixed];
+    return t.tuned ? t.fblk : TUNE_BLK[t.step % 3];
+}
+
+// a pack of (cat, mixed) with room for one more system
+Pack *pack_for(fmdg_server_t *S, int cat, int mixed)
+{
+    for (Pack *p : S->packs[cat][mixed])
+        if (p->active() < FMDG_PACK_MAX) return p;
+    Pack *p = new Pack();
+    p->cat = cat;
+    p->mixed = mixed;
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete p;
+        return nullptr;
+    }
+    S->packs[cat][mixed].push_back(p);
+    return p;
+}
 
 // admitted: the job's bytes and slot were counted
 int fail_job(fmdg_server_t *S, Job *j, int code, bool admitted)
@@ -265,9 +310,14 @@ int admit(fmdg_server_t *S)
             retire(S, j);
             continue;
         }
-        Pack &p = S->packs[j->cat][j->prec == FMDG_PREC_MIXED];
-        p.members.push_back(j);
-        p.dirty = true;
+        Pack *p = pack_for(S, j->cat, j->prec == FMDG_PREC_MIXED);
+        if (!p)
+        {
+            fail_job(S, j, fmdg_set_error("fmdg_srv: cannot create a pack stream"), true);
+            continue;
+        }
+        p->members.push_back(j);
+        p->dirty = true;
     }
     return FMDG_OK;
 }
@@ -285,50 +335,30 @@ int rebuild(fmdg_server_t *S, Pack &p)
         p.old_execs.push_back({S->seq, p.exec});   // freed once chunk S->seq-1 and older are done
         p.exec = nullptr;
     }
-    if (p.dbuf)
-    {
-        cudaFreeAsync(p.dbuf, p.stream);
-        p.dbuf = nullptr;
-    }
     if (p.members.empty()) return FMDG_OK;
-    const int fblk = S->fixed_fblk ? S->fixed_fblk : (p.tuned ? p.fblk : TUNE_BLK[p.tune_step % 3]);
-    std::vector<Geo> geos;
-    std::vector<int4> amap, cmap, fmap;
-    for (size_t k = 0; k < p.members.size(); k++)
-    {
-        fmdg_sys_t *s = p.members[k]->sys;
-        s->fblk = fblk;
-        geos.push_back(s->g);
-        const int ab = fmdg_grid(s->g.cap, 128), cb = fmdg_grid(s->g.ncell, 128), fb = fmdg_grid(s->g.cap, fblk);
-        for (int b = 0; b < ab; b++) amap.push_back(make_int4((int)k, b, ab, 0));
-        for (int b = 0; b < cb; b++) cmap.push_back(make_int4((int)k, b, cb, 0));
-        for (int b = 0; b < fb; b++) fmap.push_back(make_int4((int)k, b, fb, 0));
-    }
-    const size_t bg = (geos.size() * sizeof(Geo) + 255) & ~(size_t)255;
-    const size_t ba = (amap.size() * sizeof(int4) + 255) & ~(size_t)255;
-    const size_t bc = (cmap.size() * sizeof(int4) + 255) & ~(size_t)255;
-    const size_t bf = (fmap.size() * sizeof(int4) + 255) & ~(size_t)255;
-    FMDG_CK(cudaMallocAsync((void **)&p.dbuf, bg + ba + bc + bf, p.stream));
-    std::vector<char> h(bg + ba + bc + bf, 0);
-    memcpy(h.data(), geos.data(), geos.size() * sizeof(Geo));
-    memcpy(h.data() + bg, amap.data(), amap.size() * sizeof(int4));
-    memcpy(h.data() + bg + ba, cmap.data(), cmap.size() * sizeof(int4));
-    memcpy(h.data() + bg + ba + bc, fmap.data(), fmap.size() * sizeof(int4));
-    // pageable source: staged by the runtime before the call returns
-    FMDG_CK(cudaMemcpyAsync(p.dbuf, h.data(), h.size(), cudaMemcpyHostToDevice, p.stream));
+    const int fblk = want_fblk(S, p);
     fmdg_pack_launch &P = p.P;
     P.stream = p.stream;
     P.nsys = (int)p.members.size();
     P.cat = p.cat;
     P.mixed = p.mixed;
-    P.geos = (const Geo *)p.dbuf;
-    P.amap = (const int4 *)(p.dbuf + bg);
-    P.nab = (int)amap.size();
-    P.cmap = (const int4 *)(p.dbuf + bg + ba);
-    P.ncb = (int)cmap.size();
-    P.fmap = (const int4 *)(p.dbuf + bg + ba + bc);
-    P.nfb = (int)fmap.size();
     P.fblk = fblk;
+    LocPack *locs[4] = {&P.la, &P.lc, &P.lf, &P.ls};
+    for (LocPack *L : locs)
+    {
+        L->nsys = P.nsys;
+        L->bstart[0] = 0;
+    }
+    for (int k = 0; k < P.nsys; k++)
+    {
+        fmdg_sys_t *s = p.members[k]->sys;
+        s->fblk = fblk;
+        for (LocPack *L : locs) L->geos[k] = s->g;
+        P.la.bstart[k + 1] = P.la.bstart[k] + fmdg_grid(s->g.cap, 128);
+        P.lc.bstart[k + 1] = P.lc.bstart[k] + fmdg_grid(s->g.ncell, 128);
+        P.lf.bstart[k + 1] = P.lf.bstart[k] + fmdg_grid(s->g.cap, fblk);
+        P.ls.bstart[k + 1] = k + 1;
+    }
     // members set up on their own streams must be ready before the chunk
     for (Job *j : p.members)
         if (j->ready) FMDG_CK(cudaStreamWaitEvent(p.stream, j->ready, 0));
@@ -356,6 +386,7 @@ int rebuild(fmdg_server_t *S, Pack &p)
 
 int launch_chunk(fmdg_server_t *S, Pack &p)
 {
+    if (p.exec && p.exec_fblk != want_fblk(S, p)) p.dirty = true;
     if (p.dirty)
     {
         int rc = rebuild(S, p);
@@ -383,7 +414,7 @@ int launch_chunk(fmdg_server_t *S, Pack &p)
         c.atom_steps += (double)j->n * k;
         if (j->left == 0) p.dirty = true;
     }
-    c.timed = full && !p.tuned && !S->fixed_fblk;
+    c.timed = full && !S->tuners[p.cat][p.mixed].tuned && !S->fixed_fblk;
     p.inflight.push_back(c);
     p.chunks++;
     return FMDG_OK;
@@ -438,22 +469,24 @@ int reap(fmdg_server_t *S, Pack &p, bool block)
         const cudaError_t q = cudaEventQuery(c.ev1);
         if (q == cudaErrorNotReady) break;
         if (q != cudaSuccess) return fmdg_fail("chunk", q);
-        if (c.timed && !p.tuned && c.atom_steps > 0)
+        Tuner &t = S->tuners[p.cat][p.mixed];
+        if (c.timed && !t.tuned && c.atom_steps > 0)
         {
+            // device time per atom-step of this block size; the next chunks
+            // of the category try the next candidate (or keep the choice)
             float ms = 0.f;
             cudaEventElapsedTime(&ms, c.ev0, c.ev1);
             const int slot = (c.fblk == 64) ? 0 : (c.fblk == 128 ? 1 : 2);
-            p.tune_cost[slot] = std::min(p.tune_cost[slot], ms / c.atom_steps);
-            p.tune_step++;
-            if (p.tune_step >= TUNE_ROUNDS)
+            t.cost[slot] = std::min(t.cost[slot], ms / c.atom_steps);
+            t.step++;
+            if (t.step >= TUNE_ROUNDS)
             {
                 int best = 1;
                 for (int k = 0; k < 3; k++)
-                    if (p.tune_cost[k] < p.tune_cost[best]) best = k;
-                p.fblk = TUNE_BLK[best];
-                p.tuned = true;
+                    if (t.cost[k] < t.cost[best]) best = k;
+                t.fblk = TUNE_BLK[best];
+                t.tuned = true;
             }
-            p.dirty = true;   // next candidate (or the choice)
         }
         p.atom_steps += c.atom_steps;
         S->atom_steps_done += c.atom_steps;
@@ -497,15 +530,6 @@ extern "C" int fmdg_srv_create(fmdg_server_t **out, int device, size_t hbm_budge
     S->max_jobs = max_jobs;
     S->chunk = chunk_steps;
     S->t0 = wall_s();
-    for (int c = 0; c < 4; c++)
-        for (int m = 0; m < 2; m++)
-        {
-            Pack &p = S->packs[c][m];
-            p.cat = c;
-            p.mixed = m;
-            cudaError_t e = cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking);
-            if (e != cudaSuccess) return fmdg_fail("cudaStreamCreate", e);
-        }
     *out = S;
     return FMDG_OK;
 }
@@ -514,17 +538,16 @@ extern "C" void fmdg_srv_destroy(fmdg_server_t *S)
 {
     if (!S) return;
     cudaSetDevice(S->device);
+    each_pack(S, [&](Pack &p) {
+        cudaStreamSynchronize(p.stream);
+        for (Chunk &c : p.inflight) { cudaEventDestroy(c.ev0); cudaEventDestroy(c.ev1); }
+        if (p.exec) cudaGraphExecDestroy(p.exec);
+        for (auto &oe : p.old_execs) cudaGraphExecDestroy(oe.second);
+        cudaStreamDestroy(p.stream);
+    });
     for (auto &row : S->packs)
-        for (Pack &p : row)
-        {
-            cudaStreamSynchronize(p.stream);
-            for (Chunk &c : p.inflight) { cudaEventDestroy(c.ev0); cudaEventDestroy(c.ev1); }
-            if (p.exec) cudaGraphExecDestroy(p.exec);
-            for (auto &oe : p.old_execs) cudaGraphExecDestroy(oe.second);
-            if (p.dbuf) cudaFreeAsync(p.dbuf, p.stream);
-            cudaStreamSynchronize(p.stream);
-            cudaStreamDestroy(p.stream);
-        }
+        for (auto &v : row)
+            for (Pack *p : v) delete p;
     for (auto &kv : S->jobs)
     {
         Job *j = kv.second;
@@ -562,8 +585,7 @@ extern "C" int fmdg_srv_set_tuning(fmdg_server_t *S, int fblk)
     if (fblk != 0 && fblk != 64 && fblk != 128 && fblk != 256)
         return fmdg_set_error("fmdg_srv_set_tuning: 0 (autotune), 64, 128 or 256");
     S->fixed_fblk = fblk;
-    for (auto &row : S->packs)
-        for (Pack &p : row) p.dirty = true;
+    each_pack(S, [](Pack &p) { p.dirty = true; });
     return FMDG_OK;
 }
 
@@ -682,30 +704,25 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
 extern "C" int fmdg_srv_progress(fmdg_server_t *S, int wait, int *active)
 {
     FMDG_CK(cudaSetDevice(S->device));
-    int rc;
-    for (auto &row : S->packs)
-        for (Pack &p : row)
-            if ((rc = reap(S, p, false))) return rc;
+    int rc = FMDG_OK;
+    each_pack(S, [&](Pack &p) { if (!rc) rc = reap(S, p, false); });
+    if (rc) return rc;
     if ((rc = admit(S))) return rc;
     bool launched = false;
-    for (auto &row : S->packs)
-        for (Pack &p : row)
-        {
-            if (p.inflight.size() >= 2) continue;
-            bool work = false;
-            for (Job *j : p.members) work |= j->left > 0;
-            if (!work) continue;
-            if ((rc = launch_chunk(S, p))) return rc;
-            launched = true;
-        }
+    each_pack(S, [&](Pack &p) {
+        if (rc || p.inflight.size() >= 2 || p.active() == 0) return;
+        rc = launch_chunk(S, p);
+        launched = true;
+    });
+    if (rc) return rc;
     if (wait && !launched)
     {
         // the pack whose oldest chunk was launched first
         Pack *oldest = nullptr;
-        for (auto &row : S->packs)
-            for (Pack &p : row)
-                if (!p.inflight.empty() && (!oldest || p.inflight.front().seq < oldest->inflight.front().seq))
-                    oldest = &p;
+        each_pack(S, [&](Pack &p) {
+            if (!p.inflight.empty() && (!oldest || p.inflight.front().seq < oldest->inflight.front().seq))
+                oldest = &p;
+        });
         if (oldest && (rc = reap(S, *oldest, true))) return rc;
     }
     if (active) *active = (int)S->queue.size() + S->running;
@@ -778,10 +795,13 @@ extern "C" int fmdg_srv_stats(fmdg_server_t *S, fmdg_srv_stats_t *out)
     for (int c = 0; c < 4; c++)
         for (int m = 0; m < 2; m++)
         {
-            const Pack &p = S->packs[c][m];
-            out->pack_fblk[c][m] = p.tuned ? p.fblk : 0;
-            out->pack_chunks[c][m] = p.chunks;
-            out->pack_rebuilds[c][m] = p.rebuilds;
+            const Tuner &t = S->tuners[c][m];
+            out->pack_fblk[c][m] = S->fixed_fblk ? S->fixed_fblk : (t.tuned ? t.fblk : 0);
+            for (const Pack *p : S->packs[c][m])
+            {
+                out->pack_chunks[c][m] += p->chunks;
+                out->pack_rebuilds[c][m] += p->rebuilds;
+            }
         }
     return FMDG_OK;
 }
@@ -807,33 +827,29 @@ extern "C" int fmdg_srv_run_resident(fmdg_server_t *S, int k, float *ms)
         FMDG_CK(cudaEventCreate(&S->jev0));
         FMDG_CK(cudaEventCreate(&S->jev1));
     }
-    int rc;
-    for (auto &row : S->packs)
-        for (Pack &p : row)
-        {
-            for (Job *j : p.members)
-                if (j->left < k * S->chunk) return fmdg_set_error("fmdg_srv_run_resident: a job has too few steps left");
-            if (p.dirty && (rc = rebuild(S, p))) return rc;
-        }
+    int rc = FMDG_OK;
+    each_pack(S, [&](Pack &p) {
+        for (Job *j : p.members)
+            if (!rc && j->left < k * S->chunk) rc = fmdg_set_error("fmdg_srv_run_resident: a job has too few steps left");
+        if (p.exec && p.exec_fblk != want_fblk(S, p)) p.dirty = true;
+        if (!rc && p.dirty) rc = rebuild(S, p);
+    });
+    if (rc) return rc;
     FMDG_CK(cudaEventRecord(S->jev0, S->join));
     std::vector<cudaEvent_t> ends;
-    for (auto &row : S->packs)
-        for (Pack &p : row)
-        {
-            if (p.members.empty() || !p.exec) continue;
-            FMDG_CK(cudaStreamWaitEvent(p.stream, S->jev0, 0));
-            for (int q = 0; q < k; q++)
-                if ((rc = launch_chunk(S, p))) return rc;
-            ends.push_back(p.inflight.back().ev1);
-        }
+    each_pack(S, [&](Pack &p) {
+        if (rc || p.members.empty() || !p.exec) return;
+        if (cudaStreamWaitEvent(p.stream, S->jev0, 0) != cudaSuccess) rc = fmdg_set_error("stream wait");
+        for (int q = 0; q < k && !rc; q++) rc = launch_chunk(S, p);
+        if (!rc) ends.push_back(p.inflight.back().ev1);
+    });
+    if (rc) return rc;
     for (cudaEvent_t e : ends) FMDG_CK(cudaStreamWaitEvent(S->join, e, 0));
     FMDG_CK(cudaEventRecord(S->jev1, S->join));
     FMDG_CK(cudaEventSynchronize(S->jev1));
     FMDG_CK(cudaEventElapsedTime(ms, S->jev0, S->jev1));
-    for (auto &row : S->packs)
-        for (Pack &p : row)
-            if ((rc = reap(S, p, false))) return rc;
-    return FMDG_OK;
+    each_pack(S, [&](Pack &p) { if (!rc) rc = reap(S, p, false); });
+    return rc;
 }
 
 // One step of the pack (category, precision) launched phase by phase
@@ -845,41 +861,53 @@ extern "C" int fmdg_srv_profile_pack(fmdg_server_t *S, int cat, int mixed, float
 {
     FMDG_CK(cudaSetDevice(S->device));
     if (cat < 0 || cat > 3 || mixed < 0 || mixed > 1) return fmdg_set_error("fmdg_srv_profile_pack: bad pack");
-    Pack &p = S->packs[cat][mixed];
-    int rc;
-    if (p.dirty && (rc = rebuild(S, p))) return rc;
     *atoms = 0.0;
-    *members = (int)p.members.size();
+    *members = 0;
     for (int q = 0; q < 4; q++) ms[q] = 0.f;
-    if (p.members.empty()) return FMDG_OK;
-    for (Job *j : p.members)
-        if (j->left < 1) return fmdg_set_error("fmdg_srv_profile_pack: a job has no step left");
-    // wait for the pack's earlier chunks
-    FMDG_CK(cudaStreamSynchronize(p.stream));
-    cudaEvent_t ev[5];
-    for (int q = 0; q < 5; q++) ev[q] = get_event(S);
-    FMDG_CK(cudaEventRecord(ev[0], p.stream));
-    int n = fmdg_pack_launch_refresh(p.P);
-    if (n < 0) return -n;
-    S->kernels += n;
-    FMDG_CK(cudaEventRecord(ev[1], p.stream));
-    const int masks[3] = {1, 2, 4};
-    for (int q = 0; q < 3; q++)
+    for (Pack *pp : S->packs[cat][mixed])
     {
-        n = fmdg_pack_launch_forces(p.P, masks[q]);
+        Pack &p = *pp;
+        int rc;
+        if (p.exec && p.exec_fblk != want_fblk(S, p)) p.dirty = true;
+        if (p.dirty && (rc = rebuild(S, p))) return rc;
+        if (p.members.empty()) continue;
+        for (Job *j : p.members)
+            if (j->left < 1) return fmdg_set_error("fmdg_srv_profile_pack: a job has no step left");
+        // the pack's earlier chunks first
+        FMDG_CK(cudaStreamSynchronize(p.stream));
+        cudaEvent_t ev[5];
+        for (int q = 0; q < 5; q++) ev[q] = get_event(S);
+        FMDG_CK(cudaEventRecord(ev[0], p.stream));
+        int n = fmdg_pack_launch_refresh(p.P);
         if (n < 0) return -n;
         S->kernels += n;
-        FMDG_CK(cudaEventRecord(ev[q + 2], p.stream));
+        FMDG_CK(cudaEventRecord(ev[1], p.stream));
+        const int masks[3] = {1, 2, 4};
+        for (int q = 0; q < 3; q++)
+        {
+            n = fmdg_pack_launch_forces(p.P, masks[q]);
+            if (n < 0) return -n;
+            S->kernels += n;
+            FMDG_CK(cudaEventRecord(ev[q + 2], p.stream));
+        }
+        FMDG_CK(cudaEventSynchronize(ev[4]));
+        for (int q = 0; q < 4; q++)
+        {
+            float t = 0.f;
+            FMDG_CK(cudaEventElapsedTime(&t, ev[q], ev[q + 1]));
+            ms[q] += t;
+        }
+        for (int q = 0; q < 5; q++) put_event(S, ev[q]);
+        *members += (int)p.members.size();
+        double a = 0.0;
+        for (Job *j : p.members)
+        {
+            j->left -= 1;
+            a += j->n;
+            if (j->left == 0) p.dirty = true;
+        }
+        *atoms += a;
+        S->atom_steps_done += a;
     }
-    FMDG_CK(cudaEventSynchronize(ev[4]));
-    for (int q = 0; q < 4; q++) FMDG_CK(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
-    for (int q = 0; q < 5; q++) put_event(S, ev[q]);
-    for (Job *j : p.members)
-    {
-        j->left -= 1;
-        *atoms += j->n;
-        if (j->left == 0) p.dirty = true;
-    }
-    S->atom_steps_done += *atoms;
     return FMDG_OK;
 }

@@ -148,3 +148,25 @@ def test_mixed_force_error_bound(L, eam, pot):
     one.close()
     err = np.abs(F32 - F64).max() / np.abs(F64).max()
     assert err <= 1e-5, err
+
+
+def test_more_jobs_than_one_pack(L, eam):
+    """40 jobs of one category and precision need two packs (at most 32
+    systems travel in one launch); every job still equals its single-system
+    run bit for bit."""
+    jobs = [_job("lj", 5, 60.0 + 20.0 * k, 100 + k) for k in range(40)]
+    srv = serve.Server(L, chunk_steps=8, eam=eam)
+    ids = [srv.submit("lj", x, v, l, 21 + (k % 5), keep_state=True) for k, (x, v, l) in enumerate(jobs)]
+    srv.drain()
+    assert srv.stats().finished == 40
+    for k in (0, 17, 33, 39):
+        x, v, l = jobs[k]
+        one = serve.Single(L, "lj", x, v, l, precision=serve.PREC_MIXED, eam=eam)
+        one.steps(21 + (k % 5))
+        xs, vs, Fs, _ = one.state()
+        one.close()
+        xm, vm, Fm, _ = srv.state(ids[k], len(x))
+        np.testing.assert_array_equal(xs, xm)
+        np.testing.assert_array_equal(vs, vm)
+        np.testing.assert_array_equal(Fs, Fm)
+    srv.close()
