@@ -316,24 +316,37 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist(__grid_
         const int jy = nb_axis(g, 1, ci.y, off_y(code), &sdummy);
         const int jz = nb_axis(g, 2, ci.z, off_z(code), &sdummy);
         if (jx < 0 || jy < 0 || jz < 0) continue;
-        const int cx = off_x(code), cy = off_y(code), cz = off_z(code);
         const int c = jz + g.nc[2] * (jy + g.nc[1] * jx);
         const int jb = S.cell_start[c], je = S.cell_start[c + 1];
-        const float ox = (float)cx * g.cellh_f[0];
-        const float oy = (float)cy * g.cellh_f[1];
-        const float oz = (float)cz * g.cellh_f[2];
-        for (int j = jb; j < je; j++)
-        {
-            if (code == 13 && j == i) continue;
-            const float4 xj = g.xf4[j];
-            const float dx = xi.x - xj.x - ox, dy = xi.y - xj.y - oy, dz = xi.z - xj.z - oz;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 < rl2)
+        // i's position in the neighbour cell's frame
+        const float qx = xi.x - (float)off_x(code) * g.cellh_f[0];
+        const float qy = xi.y - (float)off_y(code) * g.cellh_f[1];
+        const float qz = xi.z - (float)off_z(code) * g.cellh_f[2];
+        const int tag = code << 26;
+        auto test = [&](int j, float4 xj) {
+            const float dx = qx - xj.x, dy = qy - xj.y, dz = qz - xj.z;
+            if (dx * dx + dy * dy + dz * dz < rl2)
             {
-                if (cnt < maxnb) g.nbr[(size_t)cnt * cap + i] = j | (code << 26);
+                if (cnt < maxnb) g.nbr[(size_t)cnt * cap + i] = j | tag;
                 cnt++;
             }
+        };
+        int j = jb;
+        if (code != 13)
+        {
+            // four candidates per round, their loads in flight together
+            for (; j + 4 <= je; j += 4)
+            {
+                const float4 a0 = __ldg(g.xf4 + j), a1 = __ldg(g.xf4 + j + 1);
+                const float4 a2 = __ldg(g.xf4 + j + 2), a3 = __ldg(g.xf4 + j + 3);
+                test(j, a0);
+                test(j + 1, a1);
+                test(j + 2, a2);
+                test(j + 3, a3);
+            }
         }
+        for (; j < je; j++)
+            if (j != i) test(j, __ldg(g.xf4 + j));
     }
     g.nbr_count[i] = cnt;
 }
