@@ -59,6 +59,12 @@ FLOP_FORCE = 68.0 * PAIRS_PER_ATOM
 # LJ 35.5 x 31 (src/lj.h:35-56), Morse 91 x 31 (src/morse.h:35-56),
 # EAM 29.5 x 68 (src/eam.h:186-226)
 SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0}
+# DRAM bytes (read + write) per atom of one pair-force launch, from ncu
+# captures of the same kernels (dram__bytes_read.sum + dram__bytes_write.sum
+# divided by the atoms of the launch): packed Morse on a 149616-atom pack,
+# single-system EAM on the 256000-atom system; the traffic grows with the
+# atoms (the neighbour list dominates it)
+FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 120.45e6 / 149616, "eam_single": 71.26e6 / 256000}
 
 
 def clocks_sampler(stop, out):
@@ -279,7 +285,8 @@ def run_ours(args):
                      "kernel": "k_force (EAM pair forces + finish step)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": "measured FMA-chain microkernel (no CUDA-core peak in MEASURED_PEAKS.json)",
-                     "traffic": None},
+                     "traffic": (FORCE_DRAM_BYTES_PER_ATOM["eam_single"] * natoms if args.precision == "mixed"
+                                 else None)},
         "clocks": clocks,
         "device_errors": errs.value,
         "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 2 * 3 * natoms * 8,
@@ -501,7 +508,10 @@ def run_served(args):
                      "achieved": achieved, "peak": peak32.value, "unit": "TFLOP/s",
                      "frac": achieved / peak32.value,
                      "peak_source": "measured FMA-chain microkernel (MEASURED_PEAKS.json has no CUDA-core peak)",
-                     "traffic": None},
+                     "traffic": (FORCE_DRAM_BYTES_PER_ATOM["morse_pack"] * phases[dom]["atoms"] if dom == "morse"
+                                 else None),
+                     "traffic_note": "DRAM bytes of the force phase of this category per step (all its packs), "
+                                     "scaled by atoms from an ncu capture of a 149616-atom Morse pack"},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "atom-steps/s",
                 "h2d_bytes_per_step": h2d / total_steps, "d2h_bytes_per_step": d2h / total_steps,
