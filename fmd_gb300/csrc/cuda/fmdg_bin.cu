@@ -138,6 +138,12 @@ __global__ void k_bin_classify(__grid_constant__ const L loc, int mode)
     if (deleted)
     {
         g.bdest[i] = -1;
+        if (g.skin_on)
+        {
+            // the slot is gone: its list entries must go too
+            g.pos[S.slot[i]] = -1;
+            dyn->rebuild = 1;
+        }
         return;
     }
     for (int d = 0; d < 3; d++) S.x[d * cap + i] = x[d];
@@ -341,6 +347,7 @@ __global__ void k_bin_scatter(__grid_constant__ const L loc)
     T.group[idx] = S.group[i];
     T.atomid[idx] = S.atomid[i];
     T.cell_of[idx] = D;
+    if (g.skin_on) T.slot[idx] = S.slot[i];
 }
 
 // swaps sides after a refresh that moved atoms; advances the device copy of

@@ -60,7 +60,7 @@ void free_atoms(fmdg_sys_t *s)
     {
         Side &S = g.side[k];
         dfree(s, S.x); dfree(s, S.v); dfree(s, S.kind); dfree(s, S.group); dfree(s, S.atomid);
-        dfree(s, S.cell_of); dfree(s, S.cell_start);
+        dfree(s, S.cell_of); dfree(s, S.cell_start); dfree(s, S.slot);
         memset(&S, 0, sizeof S);
     }
     dfree(s, g.F); dfree(s, g.vaream);
@@ -69,6 +69,10 @@ void free_atoms(fmdg_sys_t *s)
     dfree(s, g.bdest); dfree(s, g.bpath); dfree(s, g.bslot); dfree(s, g.brank); dfree(s, g.bnewidx);
     dfree(s, g.dep_count); dfree(s, g.arr_base); dfree(s, g.bucket); dfree(s, g.arr_slot);
     dfree(s, g.partials);
+    dfree(s, g.pos); dfree(s, g.cb); dfree(s, g.xl); dfree(s, g.xb); dfree(s, (void *)g.xd);
+    dfree(s, g.gslot); dfree(s, g.fpb); dfree(s, g.fpd);
+    g.pos = g.cb = nullptr; g.xl = g.xb = nullptr; g.xd = nullptr; g.gslot = nullptr;
+    g.fpb = nullptr; g.fpd = nullptr;
     g.F = g.vaream = nullptr;
     g.bdest = g.bpath = g.bslot = g.brank = g.bnewidx = nullptr;
     g.dep_count = g.arr_lower = g.arr_total = g.bucket_fill = g.arr_base = nullptr;
@@ -388,7 +392,7 @@ int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
         const double hmin = fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
         rc2max = hmin * hmin;
     }
-    const double rlist = sqrt(rc2max) + 1e-2;
+    const double rlist = sqrt(rc2max) + (s->g.skin > 0.0 ? s->g.skin : 1e-2);
     int maxcell = 0;
     for (int c = 0; c < ncell; c++) maxcell = cell_count[c] > maxcell ? cell_count[c] : maxcell;
     const double nmax = maxcell / (g.cellh[0] * g.cellh[1] * g.cellh[2]);
@@ -413,6 +417,16 @@ size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
 int fmdg_set_steps_left(fmdg_sys_t *s, int steps)
 {
     FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, steps_left), &steps, sizeof steps, cudaMemcpyHostToDevice));
+    return FMDG_OK;
+}
+
+// Verlet-skin list for packed stepping (before fmdg_upload): the list radius
+// is the largest cutoff + skin; every periodic box length must exceed twice
+// that radius so one image of a pair at most lies inside it.
+int fmdg_set_skin(fmdg_sys_t *s, double skin)
+{
+    if (!(skin >= 0.0)) return fmdg_set_error("fmdg_set_skin: negative skin");
+    s->g.skin = skin;
     return FMDG_OK;
 }
 
@@ -506,6 +520,29 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     // partials for the smallest block size the tuner may pick (64)
     const int nb = fmdg_grid(cap, 64);
     if ((rc = dalloc(s, &g.partials, (size_t)nb * 9 + 8))) return rc;
+    g.skin_on = g.skin > 0.0;
+    if (g.skin_on && cap >= (1 << 25)) return fmdg_set_error("fmdg_upload: skin lists hold at most 2^25 atoms");
+    if (g.skin_on)
+    {
+        for (int k = 0; k < 2; k++)
+            if ((rc = dalloc(s, &g.side[k].slot, cap))) return rc;
+        if ((rc = dalloc(s, &g.pos, cap)) || (rc = dalloc(s, &g.cb, cap)) || (rc = dalloc(s, &g.xl, cap)) ||
+            (rc = dalloc(s, &g.xb, cap)) || (rc = dalloc(s, (double4_32a **)&g.xd, cap)) ||
+            (rc = dalloc(s, &g.gslot, cap)) || (rc = dalloc(s, &g.fpb, cap)) || (rc = dalloc(s, &g.fpd, cap)))
+            return rc;
+        std::vector<int> iota(cap);
+        for (int k = 0; k < cap; k++) iota[k] = k;
+        FMDG_CK(cudaMemcpy(g.side[0].slot, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpy(g.pos, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice));
+        const double rsk = sqrt(rc2max) + g.skin;
+        g.rskin2 = (float)(rsk * rsk);
+        g.half_skin2 = (float)(0.25 * g.skin * g.skin);
+        g.srad = 1;
+        for (int d = 0; d < 3; d++)
+            if (rsk > g.cellh[d]) g.srad = 2;
+        if (rsk > 2.0 * fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2])))
+            return fmdg_set_error("fmdg_upload: skin list radius above two cells");
+    }
     // host SoA staging
     std::vector<double> hx(3 * (size_t)cap, 0.0), hv(3 * (size_t)cap, 0.0);
     for (int i = 0; i < n; i++)
@@ -534,6 +571,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     d.cur = 0;
     d.n = n;
     d.lambda = 1.0;
+    d.rebuild = 1;
     d.time = keep_time;
     d.dt = keep_dt;
     FMDG_CK(cudaMemcpy(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));

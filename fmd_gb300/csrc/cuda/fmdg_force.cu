@@ -31,79 +31,12 @@
 // FMDG_PREC_MIXED: pair geometry from the binary32 cell-local coordinates,
 // pair/spline/embedding arithmetic in binary32, forces and energies summed
 // in binary64 (binary32 partial sums of at most 8 pair terms are added to
-// binary64 accumulators).  Pairs within 1e-4 relative of a cutoff are
+// binary64 accumulators, every 8 list entries so a warp's lanes flush
+// together).  Pairs within 1e-4 relative of a cutoff are
 // re-tested in binary64 so both modes include exactly the same pairs.
-#include "fmdg_internal.cuh"
+#include "fmdg_pairs.cuh"
 
 namespace {
-
-enum { CAT_LJ = 1, CAT_EAM = 2, CAT_MORSE = 3, CAT_HYBRID = 4 };
-
-struct SmemPot
-{
-    fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
-    float pf[FMDG_MAXK * FMDG_MAXK][4];
-    double mass[FMDG_MAXK];
-    int elem[FMDG_MAXK];
-    float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
-};
-
-__device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
-{
-    const int nk2 = g.nkinds * g.nkinds;
-    for (int k = threadIdx.x; k < nk2; k += blockDim.x)
-    {
-        sp.pairs[k] = g.pairs[k];
-        for (int q = 0; q < 4; q++) sp.pf[k][q] = (float)g.pairs[k].p[q];
-    }
-    for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
-    {
-        sp.mass[k] = g.mass[k];
-        sp.elem[k] = g.eam_elem[k];
-    }
-    for (int c = threadIdx.x; c < 27; c += blockDim.x)
-        sp.off[c] = make_float4((float)(c / 9 - 1) * g.cellh_f[0], (float)((c / 3) % 3 - 1) * g.cellh_f[1],
-                                (float)(c % 3 - 1) * g.cellh_f[2], 0.f);
-    __syncthreads();
-}
-
-// stencil offset code: (ox+1)*9 + (oy+1)*3 + (oz+1); 13 is the cell itself
-__device__ __forceinline__ int off_x(int code) { return code / 9 - 1; }
-__device__ __forceinline__ int off_y(int code) { return (code / 3) % 3 - 1; }
-__device__ __forceinline__ int off_z(int code) { return code % 3 - 1; }
-
-struct CellXYZ { int x, y, z; };
-
-__device__ __forceinline__ CellXYZ cell_xyz(const Geo &g, int c)
-{
-    CellXYZ r;
-    r.x = c / (g.nc[1] * g.nc[2]);
-    r.y = (c / g.nc[2]) % g.nc[1];
-    r.z = c % g.nc[2];
-    return r;
-}
-
-// Neighbour cell index along one axis for home coordinate h and offset o;
-// -1 when the neighbour is outside an open face.  *shift is the image
-// translation of src/md-ghost.c:85-107 (ghost copy of the far layer).
-__device__ __forceinline__ int nb_axis(const Geo &g, int d, int h, int o, double *shift)
-{
-    int j = h + o;
-    *shift = 0.0;
-    if (j < 0)
-    {
-        if (!g.pbc[d]) return -1;
-        j += g.nc[d];
-        *shift = -g.l[d];
-    }
-    else if (j >= g.nc[d])
-    {
-        if (!g.pbc[d]) return -1;
-        j -= g.nc[d];
-        *shift = g.l[d];
-    }
-    return j;
-}
 
 // Every (j, stencil code) of the 27-cell stencil of cell c except i itself.
 template <typename F>
@@ -188,36 +121,6 @@ __device__ __forceinline__ float3 geom32(const SmemPot &sp, float4 xi, float4 xj
     return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
 }
 
-// interval index k = floor(q) (clamped to kmax) and fraction b = q - k of a
-// binary32 table coordinate 0 <= q < 2^23, without conversion instructions:
-// adding 2^23 rounding towards minus infinity leaves floor(q) in the
-// significand
-__device__ __forceinline__ int table_index(float q, float kmax, float &b)
-{
-    const float fl = fminf(__fadd_rd(q, 8388608.f) - 8388608.f, kmax);
-    b = q - fl;
-    return __float_as_int(fl + 8388608.f) - 0x4B000000;
-}
-
-// natural cubic spline on a uniform grid (src/cspline.h:26-27) as a cubic
-// in the fraction b of interval k: t = {k0, k1, k2, k3}
-__device__ __forceinline__ double spl_val(double4_32a t, double b)
-{
-    return ((t.w * b + t.z) * b + t.y) * b + t.x;
-}
-__device__ __forceinline__ double spl_der(double4_32a t, double b, double inv_h)
-{
-    return ((3.0 * t.w * b + 2.0 * t.z) * b + t.y) * inv_h;
-}
-__device__ __forceinline__ float spl_val(float4 t, float b)
-{
-    return ((t.w * b + t.z) * b + t.y) * b + t.x;
-}
-__device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
-{
-    return ((3.f * t.w * b + 2.f * t.z) * b + t.y) * inv_h;
-}
-
 // is r2 (binary32) within rc2?  Near the cutoff the decision is taken in
 // binary64 from the absolute positions, as the reference does.
 __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i, CellXYZ ci, int j, int code,
@@ -228,51 +131,6 @@ __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i,
     const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
     return geom64(g, S, xi, ci, j, code).r2 < rc2;
 }
-
-// Deterministic block reduction of NV doubles; thread 0 writes out[0..NV).
-template <int NV>
-__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
-{
-    __shared__ double red[32][NV];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k = 0; k < NV; k++)
-        for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
-    if (lane == 0)
-        for (int k = 0; k < NV; k++) red[w][k] = v[k];
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        const int nw = (blockDim.x + 31) >> 5;
-        for (int k = 0; k < NV; k++)
-        {
-            double t = 0.0;
-            for (int q = 0; q < nw; q++) t += red[q][k];
-            out[k] = t;
-        }
-    }
-}
-
-// binary32 partial sums flushed into binary64 every 8 terms
-template <int NV>
-struct Acc32
-{
-    float part[NV];
-    double sum[NV];
-    int n;
-    __device__ __forceinline__ Acc32() : n(0)
-    {
-        for (int k = 0; k < NV; k++) { part[k] = 0.f; sum[k] = 0.0; }
-    }
-    __device__ __forceinline__ void tick()
-    {
-        if (++n == 8) flush();
-    }
-    __device__ __forceinline__ void flush()
-    {
-        for (int k = 0; k < NV; k++) { sum[k] += (double)part[k]; part[k] = 0.f; }
-        n = 0;
-    }
-};
 
 // ---------------------------------------------------------------- kernels
 
@@ -415,8 +273,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                         float b;
                         const int ir2 = table_index(r2 * inv_h, kmax, b);
                         ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], b);
-                        ac.tick();
                     }
+                    ac.tick();
                 });
                 ac.flush();
                 rho = ac.sum[0];
@@ -454,46 +312,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
         }
     }
     block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
-}
-
-// Second level: sums the per-block partials in a fixed order, writes the
-// thermo record (src/integrators.c:78-92) and, when a Berendsen thermostat
-// is active, the velocity scale of the next start step
-// (src/integrators.c:44-50): lambda = sqrt(1 + dt/tau * (T0/T - 1)).
-// Run by one whole block of at most 256 threads.
-__device__ void final_reduce(const Geo &g, int nblocks, int keep_pe, int with_emb, int thermostat,
-                             double dt, double tau, double T0)
-{
-    __shared__ double red[8][7];
-    const int t = threadIdx.x;
-    double s[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int b = t; b < nblocks; b += blockDim.x)
-    {
-        for (int k = 0; k < 6; k++) s[k] += __ldcg(&g.partials[(size_t)k * nblocks + b]);
-        if (with_emb) s[6] += __ldcg(&g.partials[(size_t)nblocks * 8 + b]);
-    }
-    for (int k = 0; k < 7; k++)
-        for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], off);
-    if ((t & 31) == 0)
-        for (int k = 0; k < 7; k++) red[t >> 5][k] = s[k];
-    __syncthreads();
-    if (t == 0)
-    {
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
-            for (int k = 0; k < 7; k++) red[0][k] += red[w][k];
-        fmdg_thermo_t *th = g.thermo;
-        const double mv2 = red[0][1];
-        const double N = red[0][5];
-        th->kinetic = 0.5 * mv2;
-        th->temperature = mv2 / (3.0 * N * K_BOLTZMANN_D);
-        th->momentum[0] = red[0][2];
-        th->momentum[1] = red[0][3];
-        th->momentum[2] = red[0][4];
-        th->count = N;
-        if (!keep_pe) th->potential = red[0][0] + red[0][6];
-        if (thermostat)
-            g.dyn->lambda = sqrt(1 + dt / tau * (T0 / th->temperature - 1));
-    }
 }
 
 __global__ void k_reduce_final(Geo g, int nblocks, int keep_pe, int with_emb, int thermostat,
@@ -619,7 +437,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] += rv.y * factor;
                             ac.part[2] += rv.z * factor;
                             ac.part[3] += 0.5f * (eps4 * (inv_rs12 - inv_rs6));
-                            ac.tick();
                         }
                     }
                     else if (cat == FMDG_POT_MORSE)
@@ -636,7 +453,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] += factor * rv.y;
                             ac.part[2] += factor * rv.z;
                             ac.part[3] += 0.5f * (D0 * (e2 - 2.f * e1));
-                            ac.tick();
                         }
                     }
                     else if (cat == FMDG_POT_EAM)
@@ -656,9 +472,9 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] -= mag * rv.y;
                             ac.part[2] -= mag * rv.z;
                             ac.part[3] += 0.5f * spl_val(tph, b);
-                            ac.tick();
                         }
                     }
+                    ac.tick();
                 });
                 ac.flush();
                 for (int d = 0; d < 3; d++) f[d] = ac.sum[d];
@@ -845,35 +661,6 @@ int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int ther
 
 // Neighbour lists, EAM density and pair forces + finish step for every
 // system of a pack (one launch per kernel).
-// phases: bit 0 neighbour lists, bit 1 EAM density, bit 2 pair forces +
-// finish step (all three for a step).  Returns the kernels launched.
-int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
-{
-    cudaStream_t st = P.stream;
-    const int nab = P.la.bstart[P.nsys], nfb = P.lf.bstart[P.nsys];
-    int n = 0;
-    if (phases & 1)
-    {
-        k_prep_local<<<nab, 128, 0, st>>>(P.la);
-        k_nlist<<<nfb, P.fblk, 0, st>>>(P.lf);
-        n += 2;
-    }
-    const int cats = 1 << P.cat;
-    if ((phases & 2) && P.cat == FMDG_POT_EAM)
-    {
-        launch_density_t(P.lf, P.mixed != 0, false, nfb, P.fblk, st);
-        n++;
-    }
-    if (phases & 4)
-    {
-        if (P.mixed) launch_force_t<LocPack, true>(P.lf, cats, 1, nfb, P.fblk, st);
-        else launch_force_t<LocPack, false>(P.lf, cats, 1, nfb, P.fblk, st);
-        n++;
-    }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return -fmdg_fail("pack forces", e);
-    return n;
-}
 
 // thermo-only reduction (no force evaluation); keeps the potential energy
 int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0)

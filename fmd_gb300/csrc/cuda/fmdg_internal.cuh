@@ -32,6 +32,8 @@ struct Dyn
     unsigned err;       // sticky error bits (FMDG_ERRBIT_*)
     unsigned blocks_done;   // ticket of the force kernel's last-block reduction
     int steps_left;     // packed launches: steps this system still takes
+    int rebuild;        // skin list: rebuild before the next force pass
+    unsigned nl_done;   // ticket of the skin-list build's last block
     int pad;
     double lambda;      // Berendsen scale for the next start step
     double time;        // simulation time (advanced by every step)
@@ -46,6 +48,7 @@ struct Side
     unsigned *atomid;
     int *cell_of;
     int *cell_start;
+    int *slot;          // skin-list systems: stable slot number of the atom
 };
 
 // integrator arguments of the step in flight (set by the host before a
@@ -106,6 +109,27 @@ struct Geo   // passed by value to kernels
     double *partials;             // per block: 8 doubles
     fmdg_thermo_t *thermo;
     Dyn *dyn;
+    // Verlet-skin neighbour list of packed (served) systems, indexed by a
+    // stable slot number: the reference's binning renumbers atoms every step,
+    // the slots do not, so the list (radius largest cutoff + skin) is reused
+    // until an atom has moved more than skin/2 since its build.  List entries
+    // hold the neighbour's slot and the stencil offset between the two
+    // atoms' cells at the build; positions are kept relative to the cell an
+    // atom had at the build (unwrapped across periodic faces), so the offset
+    // stays valid for the list's lifetime.
+    int skin_on;
+    int *pos;              // pos[slot] = current index, -1 after deletion
+    int *cb;               // by slot: cell at the last build
+    float4 *xl;            // by slot: position relative to that cell, kind bits
+    float4 *xb;            // by slot: xl at the last build
+    double4_32a *xd;       // by slot: binary64 position, kind
+    int *gslot;            // by slot: group
+    float *fpb;            // by slot: F'(rho) binary32
+    double *fpd;           // by slot: F'(rho) binary64
+    int srad;              // stencil radius in cells of the list build
+    float rskin2;          // (largest cutoff + skin)^2
+    float half_skin2;      // (skin/2)^2: displacement that triggers a rebuild
+    double skin;
 };
 
 struct fmdg_sys
@@ -240,6 +264,7 @@ int fmdg_force_blocks(const fmdg_sys_t *s);
 int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell);
 size_t fmdg_bytes_estimate(int n, int ncell, int maxnb);
 int fmdg_set_steps_left(fmdg_sys_t *s, int steps);
+int fmdg_set_skin(fmdg_sys_t *s, double skin);
 
 // refresh modes
 #define FMDG_REFRESH_ONLY  0     // positions already updated

@@ -1,0 +1,236 @@
+// Device helpers shared by the pair kernels of the single-system path
+// (fmdg_force.cu) and of the packed skin-list path (fmdg_skin.cu): pair
+// table in shared memory, stencil codes, spline evaluation, deterministic
+// block reductions and the thermo record.
+#pragma once
+
+#include "fmdg_internal.cuh"
+
+namespace {
+
+enum { CAT_LJ = 1, CAT_EAM = 2, CAT_MORSE = 3, CAT_HYBRID = 4 };
+
+struct SmemPot
+{
+    fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
+    float pf[FMDG_MAXK * FMDG_MAXK][4];
+    double mass[FMDG_MAXK];
+    int elem[FMDG_MAXK];
+    float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
+};
+
+__device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
+{
+    const int nk2 = g.nkinds * g.nkinds;
+    for (int k = threadIdx.x; k < nk2; k += blockDim.x)
+    {
+        sp.pairs[k] = g.pairs[k];
+        for (int q = 0; q < 4; q++) sp.pf[k][q] = (float)g.pairs[k].p[q];
+    }
+    for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
+    {
+        sp.mass[k] = g.mass[k];
+        sp.elem[k] = g.eam_elem[k];
+    }
+    for (int c = threadIdx.x; c < 27; c += blockDim.x)
+        sp.off[c] = make_float4((float)(c / 9 - 1) * g.cellh_f[0], (float)((c / 3) % 3 - 1) * g.cellh_f[1],
+                                (float)(c % 3 - 1) * g.cellh_f[2], 0.f);
+    __syncthreads();
+}
+
+// stencil offset code: (ox+1)*9 + (oy+1)*3 + (oz+1); 13 is the cell itself
+__device__ __forceinline__ int off_x(int code) { return code / 9 - 1; }
+__device__ __forceinline__ int off_y(int code) { return (code / 3) % 3 - 1; }
+__device__ __forceinline__ int off_z(int code) { return code % 3 - 1; }
+
+struct CellXYZ { int x, y, z; };
+
+__device__ __forceinline__ CellXYZ cell_xyz(const Geo &g, int c)
+{
+    CellXYZ r;
+    r.x = c / (g.nc[1] * g.nc[2]);
+    r.y = (c / g.nc[2]) % g.nc[1];
+    r.z = c % g.nc[2];
+    return r;
+}
+
+// Neighbour cell index along one axis for home coordinate h and offset o;
+// -1 when the neighbour is outside an open face.  *shift is the image
+// translation of src/md-ghost.c:85-107 (ghost copy of the far layer).
+__device__ __forceinline__ int nb_axis(const Geo &g, int d, int h, int o, double *shift)
+{
+    int j = h + o;
+    *shift = 0.0;
+    if (j < 0)
+    {
+        if (!g.pbc[d]) return -1;
+        j += g.nc[d];
+        *shift = -g.l[d];
+    }
+    else if (j >= g.nc[d])
+    {
+        if (!g.pbc[d]) return -1;
+        j -= g.nc[d];
+        *shift = g.l[d];
+    }
+    return j;
+}
+
+// interval index k = floor(q) (clamped to kmax) and fraction b = q - k of a
+// binary32 table coordinate 0 <= q < 2^23, without conversion instructions:
+// adding 2^23 rounding towards minus infinity leaves floor(q) in the
+// significand
+__device__ __forceinline__ int table_index(float q, float kmax, float &b)
+{
+    const float fl = fminf(__fadd_rd(q, 8388608.f) - 8388608.f, kmax);
+    b = q - fl;
+    return __float_as_int(fl + 8388608.f) - 0x4B000000;
+}
+
+// natural cubic spline on a uniform grid (src/cspline.h:26-27) as a cubic
+// in the fraction b of interval k: t = {k0, k1, k2, k3}
+__device__ __forceinline__ double spl_val(double4_32a t, double b)
+{
+    return ((t.w * b + t.z) * b + t.y) * b + t.x;
+}
+__device__ __forceinline__ double spl_der(double4_32a t, double b, double inv_h)
+{
+    return ((3.0 * t.w * b + 2.0 * t.z) * b + t.y) * inv_h;
+}
+__device__ __forceinline__ float spl_val(float4 t, float b)
+{
+    return ((t.w * b + t.z) * b + t.y) * b + t.x;
+}
+__device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
+{
+    return ((3.f * t.w * b + 2.f * t.z) * b + t.y) * inv_h;
+}
+
+// Deterministic block reduction of NV doubles; thread 0 writes out[0..NV).
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
+{
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < NV; k++)
+        for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+    if (lane == 0)
+        for (int k = 0; k < NV; k++) red[w][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int k = 0; k < NV; k++)
+        {
+            double t = 0.0;
+            for (int q = 0; q < nw; q++) t += red[q][k];
+            out[k] = t;
+        }
+    }
+}
+
+// binary32 partial sums flushed into binary64 every 8 ticks (one tick per
+// list entry visited, so the lanes of a warp flush together)
+template <int NV>
+struct Acc32
+{
+    float part[NV];
+    double sum[NV];
+    int n;
+    __device__ __forceinline__ Acc32() : n(0)
+    {
+        for (int k = 0; k < NV; k++) { part[k] = 0.f; sum[k] = 0.0; }
+    }
+    __device__ __forceinline__ void tick()
+    {
+        if (++n == 8) flush();
+    }
+    __device__ __forceinline__ void flush()
+    {
+        for (int k = 0; k < NV; k++) { sum[k] += (double)part[k]; part[k] = 0.f; }
+        n = 0;
+    }
+};
+
+// Second level: sums the per-block partials in a fixed order, writes the
+// thermo record (src/integrators.c:78-92) and, when a Berendsen thermostat
+// is active, the velocity scale of the next start step
+// (src/integrators.c:44-50): lambda = sqrt(1 + dt/tau * (T0/T - 1)).
+// Run by one whole block of at most 256 threads.
+__device__ __forceinline__ void final_reduce(const Geo &g, int nblocks, int keep_pe, int with_emb, int thermostat,
+                             double dt, double tau, double T0)
+{
+    __shared__ double red[8][7];
+    const int t = threadIdx.x;
+    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int b = t; b < nblocks; b += blockDim.x)
+    {
+        for (int k = 0; k < 6; k++) s[k] += __ldcg(&g.partials[(size_t)k * nblocks + b]);
+        if (with_emb) s[6] += __ldcg(&g.partials[(size_t)nblocks * 8 + b]);
+    }
+    for (int k = 0; k < 7; k++)
+        for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], off);
+    if ((t & 31) == 0)
+        for (int k = 0; k < 7; k++) red[t >> 5][k] = s[k];
+    __syncthreads();
+    if (t == 0)
+    {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+            for (int k = 0; k < 7; k++) red[0][k] += red[w][k];
+        fmdg_thermo_t *th = g.thermo;
+        const double mv2 = red[0][1];
+        const double N = red[0][5];
+        th->kinetic = 0.5 * mv2;
+        th->temperature = mv2 / (3.0 * N * K_BOLTZMANN_D);
+        th->momentum[0] = red[0][2];
+        th->momentum[1] = red[0][3];
+        th->momentum[2] = red[0][4];
+        th->count = N;
+        if (!keep_pe) th->potential = red[0][0] + red[0][6];
+        if (thermostat)
+            g.dyn->lambda = sqrt(1 + dt / tau * (T0 / th->temperature - 1));
+    }
+}
+
+// ---- pair terms: force factor f (F_i += f * rv, rv = x_i - x_j) and half
+// the pair energy (each atom of the pair takes half)
+// LJ (src/lj.h:35-56): p = {4 eps, sigma^2, rc^2}
+__device__ __forceinline__ void lj_pair(double r2, const fmdg_pair_t &pp, double &f, double &e)
+{
+    const double inv_r2 = 1.0 / r2;
+    const double inv_rs2 = pp.p[1] * inv_r2;
+    const double inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
+    const double inv_rs12 = inv_rs6 * inv_rs6;
+    f = 12.0 * pp.p[0] * inv_r2 * (inv_rs12 - 0.5 * inv_rs6);
+    e = 0.5 * (pp.p[0] * (inv_rs12 - inv_rs6));
+}
+__device__ __forceinline__ void lj_pair(float r2, float eps4, float sig2, float &f, float &e)
+{
+    const float inv_r2 = __fdividef(1.f, r2);
+    const float inv_rs2 = sig2 * inv_r2;
+    const float inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
+    const float inv_rs12 = inv_rs6 * inv_rs6;
+    f = 12.f * eps4 * inv_r2 * (inv_rs12 - 0.5f * inv_rs6);
+    e = 0.5f * (eps4 * (inv_rs12 - inv_rs6));
+}
+// Morse (src/morse.h:35-56): p = {D0, alpha, r0, rc^2}
+__device__ __forceinline__ void morse_pair(double r2, const fmdg_pair_t &pp, double &f, double &e)
+{
+    const double r = sqrt(r2);
+    const double inv_r = 1.0 / r;
+    const double e1 = exp(-pp.p[1] * (r - pp.p[2]));
+    const double e2 = e1 * e1;
+    f = 2.0 * pp.p[1] * pp.p[0] * inv_r * (e2 - e1);
+    e = 0.5 * (pp.p[0] * (e2 - 2.0 * e1));
+}
+__device__ __forceinline__ void morse_pair(float r2, float D0, float al, float r0, float &f, float &e)
+{
+    const float inv_r = rsqrtf(r2);
+    const float r = r2 * inv_r;
+    const float e1 = expf(-al * (r - r0));
+    const float e2 = e1 * e1;
+    f = 2.f * al * D0 * inv_r * (e2 - e1);
+    e = 0.5f * (D0 * (e2 - 2.f * e1));
+}
+
+} // namespace

@@ -64,6 +64,7 @@ struct Job
     int cat;
     int nc[3];
     double cellh[3];
+    double rcmax;
     std::vector<int> order, cell_count;   // host binning (upload order)
     // runtime
     fmdg_sys_t *sys = nullptr;
@@ -141,6 +142,7 @@ struct fmdg_server
     size_t budget, used = 0, peak = 0;
     int max_jobs, chunk;
     int fixed_fblk = 0;               // 0: autotune
+    double skin = 0.5;                // Verlet skin of the packed neighbour lists (A)
     double t0;
     long long next_id = 1, seq = 0;
     std::deque<Job *> queue;
@@ -239,6 +241,11 @@ int setup_job(fmdg_server_t *S, Job *j)
     if (rc) return rc;
     fmdg_sys_t *s = j->sys;
     if ((rc = fmdg_set_box(s, j->l, j->pbc, j->nc, j->cellh))) return rc;
+    // list radius rc + skin below half of every periodic box length
+    double skin = S->skin;
+    for (int d = 0; d < 3; d++)
+        if (j->pbc[d]) skin = std::min(skin, 0.9 * (0.5 * j->l[d] - j->rcmax));
+    if ((rc = fmdg_set_skin(s, skin))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
     if (j->cat == FMDG_POT_EAM)
@@ -589,6 +596,13 @@ extern "C" int fmdg_srv_set_tuning(fmdg_server_t *S, int fblk)
     return FMDG_OK;
 }
 
+extern "C" int fmdg_srv_set_skin(fmdg_server_t *S, double skin)
+{
+    if (!(skin > 0.0 && skin < 5.0)) return fmdg_set_error("fmdg_srv_set_skin: skin in (0, 5) A");
+    S->skin = skin;
+    return FMDG_OK;
+}
+
 extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long long *id)
 {
     if (d->nkinds < 1 || d->nkinds > FMDG_MAXK) return fmdg_set_error("fmdg_srv_submit: 1..8 kinds");
@@ -623,8 +637,14 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
         return fmdg_set_error("fmdg_srv_submit: EAM job with an unknown table key");
     }
     const double rcmax = sqrt(rc2max);
+    j->rcmax = rcmax;
     for (int k = 0; k < 3; k++)
     {
+        if (d->pbc[k] && !(d->l[k] > 2.0 * rcmax))
+        {
+            delete j;
+            return fmdg_set_error("fmdg_srv_submit: a periodic box length is not above twice the cutoff");
+        }
         j->l[k] = d->l[k];
         j->pbc[k] = d->pbc[k];
         // src/misc.c:41-50: nc = (int)(l/rc_max), cellh = l/nc

@@ -1,0 +1,590 @@
+// Packed (served) systems: pair kernels over a Verlet-skin neighbour list.
+//
+// The single-system path rebuilds its list every step in the current
+// (reference cell) order.  Packed systems keep a list of radius
+// rc + skin, indexed by a stable slot number (the atom's position in the
+// upload order, carried through every re-binning), and rebuild it only
+// when an atom has moved more than skin/2 since the last build -- the
+// usual Verlet-list criterion, which keeps every pair that can come within
+// the cutoff in the list.  Pairs are still tested against the exact cutoff
+// at every evaluation, so the list only prunes.
+//
+// Per step (after the refresh, which is the reference's exact binning):
+//   k_prep_skin     slot tables: position (binary32 relative to the build
+//                   cell, binary64), kind, group, current index;
+//                   displacement test -> rebuild flag
+//   k_nlist_skin    (when flagged) stencil scan of the cells within the list
+//                   radius of the atom's current cell
+//   k_density_skin  EAM pass 1 + embedding, one thread per slot
+//   k_force_skin    pair forces + velocity-Verlet finish step + thermo
+//                   record, one thread per slot
+//
+// Geometry.  An atom's binary32 position is kept relative to the cell it
+// had at the last build (unwrapped across periodic faces: it moves less
+// than skin/2 before the next build), and a list entry holds the stencil
+// offset between the two build cells, so a pair is formed exactly as on the
+// single-system path: x_i - x_j - offset * cellh.  Binary64: the minimum
+// image as the reference's ghost copy forms it (x_j + shift, then x_i minus
+// that, src/md-ghost.c:85-107, src/forces.h:25-34); every periodic box
+// length exceeds twice the list radius, so one image at most lies inside
+// it.  Pair arithmetic, precision modes and the near-cutoff binary64
+// re-test are those of the single-system kernels (fmdg_force.cu).
+#include "fmdg_pairs.cuh"
+
+namespace {
+
+// list entry (read as unsigned): neighbour slot | stencil code << 25; code
+// < 125 over a stencil of radius R (width W = 2R + 1):
+// ((ox + R) W + (oy + R)) W + (oz + R)
+constexpr int SLOT_BITS = 25;
+constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
+
+struct SkinOff
+{
+    float4 off[125];    // image offset of each stencil code, binary32
+};
+
+__device__ __forceinline__ void load_offsets(const Geo &g, SkinOff &so)
+{
+    const int R = g.srad, W = 2 * R + 1;
+    for (int c = threadIdx.x; c < W * W * W; c += blockDim.x)
+        so.off[c] = make_float4((float)(c / (W * W) - R) * g.cellh_f[0], (float)((c / W) % W - R) * g.cellh_f[1],
+                                (float)(c % W - R) * g.cellh_f[2], 0.f);
+    __syncthreads();
+}
+
+__device__ __forceinline__ float3 rv_of(float4 xi, float4 xj, float4 o)
+{
+    return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
+}
+
+struct Geom64 { double rv[3]; double r2; };
+
+// binary64 minimum-image geometry rv = x_a - (x_b + shift)
+__device__ __forceinline__ Geom64 geom64_mi(const Geo &g, double4_32a a, double4_32a b)
+{
+    const double xa[3] = {a.x, a.y, a.z}, xb[3] = {b.x, b.y, b.z};
+    Geom64 p;
+    for (int d = 0; d < 3; d++)
+    {
+        double x2 = xb[d];
+        if (g.pbc[d])
+        {
+            const double dd = xa[d] - x2;
+            if (dd > 0.5 * g.l[d]) x2 = __dadd_rn(x2, g.l[d]);
+            else if (dd < -0.5 * g.l[d]) x2 = __dadd_rn(x2, -g.l[d]);
+        }
+        p.rv[d] = __dsub_rn(xa[d], x2);
+    }
+    p.r2 = __dadd_rn(__dadd_rn(__dmul_rn(p.rv[0], p.rv[0]), __dmul_rn(p.rv[1], p.rv[1])),
+                     __dmul_rn(p.rv[2], p.rv[2]));
+    return p;
+}
+
+// binary32 cutoff test; within 1e-4 relative of the cutoff the decision is
+// taken in binary64 from the binary64 positions
+__device__ __forceinline__ bool within_cut_skin(const Geo &g, int ta, int tb, float r2f, float rc2f, double rc2)
+{
+    if (fabsf(r2f - rc2f) > 1e-4f * rc2f) return r2f < rc2f;
+    return geom64_mi(g, g.xd[ta], g.xd[tb]).r2 < rc2;
+}
+
+// Every (j, code) of the stencil of radius R around i's current cell, j
+// the current index, in a fixed order; on a periodic axis shorter than the
+// stencil a cell recurs with another image (at most one image of a pair
+// lies within the list radius).
+template <typename F>
+__device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, int i, F &&f)
+{
+    const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
+    const int R = g.srad, W = 2 * R + 1;
+    for (int ox = -R; ox <= R; ox++)
+    {
+        int cx = ci.x + ox;
+        if (cx < 0 || cx >= g.nc[0])
+        {
+            if (!g.pbc[0]) continue;
+            cx = (cx + 2 * g.nc[0]) % g.nc[0];
+        }
+        for (int oy = -R; oy <= R; oy++)
+        {
+            int cy = ci.y + oy;
+            if (cy < 0 || cy >= g.nc[1])
+            {
+                if (!g.pbc[1]) continue;
+                cy = (cy + 2 * g.nc[1]) % g.nc[1];
+            }
+            for (int oz = -R; oz <= R; oz++)
+            {
+                int cz = ci.z + oz;
+                if (cz < 0 || cz >= g.nc[2])
+                {
+                    if (!g.pbc[2]) continue;
+                    cz = (cz + 2 * g.nc[2]) % g.nc[2];
+                }
+                const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
+                const bool home = (ox == 0 && oy == 0 && oz == 0);
+                const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
+                const int je = S.cell_start[c + 1];
+                for (int j = S.cell_start[c]; j < je; j++)
+                    if (!(home && j == i)) f(j, code);
+            }
+        }
+    }
+}
+
+// List walk of slot t (four entries per round): f(neighbour slot, its
+// binary32 position, image offset).  An atom whose list overflowed scans
+// its candidates directly, with positions relative to the current cells.
+template <typename F>
+__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
+                                                   float4 &xi, F &&f)
+{
+    const int cnt = g.nbr_count[t];
+    if (cnt <= g.maxnb)
+    {
+        const int cap = g.cap;
+        const int *col = g.nbr + t;
+        int k = 0;
+        for (; k + 4 <= cnt; k += 4)
+        {
+            const int e0 = __ldg(col + (size_t)k * cap), e1 = __ldg(col + (size_t)(k + 1) * cap);
+            const int e2 = __ldg(col + (size_t)(k + 2) * cap), e3 = __ldg(col + (size_t)(k + 3) * cap);
+            const float4 x0 = g.xl[e0 & SLOT_MASK], x1 = g.xl[e1 & SLOT_MASK];
+            const float4 x2 = g.xl[e2 & SLOT_MASK], x3 = g.xl[e3 & SLOT_MASK];
+            f(e0 & SLOT_MASK, x0, so.off[(unsigned)e0 >> SLOT_BITS]);
+            f(e1 & SLOT_MASK, x1, so.off[(unsigned)e1 >> SLOT_BITS]);
+            f(e2 & SLOT_MASK, x2, so.off[(unsigned)e2 >> SLOT_BITS]);
+            f(e3 & SLOT_MASK, x3, so.off[(unsigned)e3 >> SLOT_BITS]);
+        }
+        for (; k < cnt; k++)
+        {
+            const int e = __ldg(col + (size_t)k * cap);
+            f(e & SLOT_MASK, g.xl[e & SLOT_MASK], so.off[(unsigned)e >> SLOT_BITS]);
+        }
+    }
+    else
+    {
+        xi = g.xf4[i];
+        for_each_candidate(g, S, i, [&](int j, int code) { f(S.slot[j], g.xf4[j], so.off[code]); });
+    }
+}
+
+// ---------------------------------------------------------------- kernels
+
+// one thread per current atom index
+__global__ void k_prep_skin(__grid_constant__ const LocPack loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    Dyn *dyn = g.dyn;
+    const int i = bx * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    const int cap = g.cap;
+    const int t = S.slot[i];
+    const double x[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+    const int kind = (int)S.kind[i];
+    const float kb = __int_as_float(kind);
+    g.pos[t] = i;
+    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
+    g.gslot[t] = S.group[i];
+    // relative to the current cell (a rebuild starts from these)
+    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
+    g.xf4[i] = make_float4((float)(x[0] - c.x * g.cellh[0]), (float)(x[1] - c.y * g.cellh[1]),
+                           (float)(x[2] - c.z * g.cellh[2]), kb);
+    // relative to the cell of the last build, unwrapped
+    const CellXYZ b = cell_xyz(g, g.cb[t]);
+    const int b3[3] = {b.x, b.y, b.z};
+    float l3[3];
+    for (int d = 0; d < 3; d++)
+    {
+        double u = x[d] - b3[d] * g.cellh[d];
+        if (g.pbc[d])
+        {
+            if (u > 0.5 * g.l[d]) u -= g.l[d];
+            else if (u < -0.5 * g.l[d]) u += g.l[d];
+        }
+        l3[d] = (float)u;
+    }
+    g.xl[t] = make_float4(l3[0], l3[1], l3[2], kb);
+    const float4 o = g.xb[t];
+    const float dx = l3[0] - o.x, dy = l3[1] - o.y, dz = l3[2] - o.z;
+    if (!(dx * dx + dy * dy + dz * dz <= g.half_skin2)) dyn->rebuild = 1;
+}
+
+// one thread per slot; every block leaves at once when no rebuild is due
+__global__ void __launch_bounds__(256) k_nlist_skin(__grid_constant__ const LocPack loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    Dyn *dyn = g.dyn;
+    if (!dyn->rebuild) return;
+    __shared__ SkinOff so;
+    load_offsets(g, so);
+    const int cap = g.cap, maxnb = g.maxnb;
+    const int t = bx * blockDim.x + threadIdx.x;
+    if (t < cap)
+    {
+        int cnt = 0;
+        const int i = g.pos[t];
+        if (i >= 0)
+        {
+            const Side S = g.side[dyn->cur];
+            const float4 xi = g.xf4[i];
+            const float rl2 = g.rskin2;
+            for_each_candidate(g, S, i, [&](int j, int code) {
+                const float3 d = rv_of(xi, __ldg(g.xf4 + j), so.off[code]);
+                if (d.x * d.x + d.y * d.y + d.z * d.z < rl2)
+                {
+                    if (cnt < maxnb) g.nbr[(size_t)cnt * cap + t] = (int)((unsigned)S.slot[j] | ((unsigned)code << SLOT_BITS));
+                    cnt++;
+                }
+            });
+            g.cb[t] = S.cell_of[i];
+            g.xl[t] = xi;
+            g.xb[t] = xi;
+        }
+        g.nbr_count[t] = cnt;
+    }
+    // the last block to finish clears the flag
+    __shared__ unsigned ticket;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        __threadfence();
+        ticket = atomicAdd(&dyn->nl_done, 1u);
+    }
+    __syncthreads();
+    if (ticket == (unsigned)nb - 1 && threadIdx.x == 0)
+    {
+        dyn->nl_done = 0;
+        dyn->rebuild = 0;
+    }
+}
+
+// EAM pass 1 + embedding (src/eam.h:270-406, src/eam.c:160-179), one
+// thread per slot
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const LocPack loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const int group = g.st.group;
+    __shared__ SmemPot sp;
+    __shared__ SkinOff so;
+    load_pot(g, sp);
+    load_offsets(g, so);
+    Dyn *dyn = g.dyn;
+    const Side S = g.side[dyn->cur];
+    const int t = bx * blockDim.x + threadIdx.x;
+    double acc[1] = {0.0};
+    const int i = (t < g.cap) ? g.pos[t] : -1;
+    if (i >= 0)
+    {
+        float4 xi = g.xl[t];
+        const int ki = __float_as_int(xi.w);
+        const int ei = sp.elem[ki];
+        const bool active = (group < 0 || g.gslot[t] == group) && ei >= 0;
+        const int nk = g.nkinds, nint = g.Nr2 - 1;
+        double rho = 0.0;
+        if (active)
+        {
+            if (!MIXED)
+            {
+                const double4_32a xdi = g.xd[t];
+                const double inv_h = g.inv_dr2;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4, float4) {
+                    if (group >= 0 && g.gslot[js] != group) return;
+                    const double4_32a xj = g.xd[js];
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    const Geom64 p = geom64_mi(g, xdi, xj);
+                    if (p.r2 < pp.p[2])
+                    {
+                        const double q = p.r2 * inv_h;
+                        const int ir2 = min((int)q, nint - 1);
+                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], q - ir2);
+                    }
+                });
+            }
+            else
+            {
+                const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
+                Acc32<1> ac;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                    if (group >= 0 && g.gslot[js] != group) return;
+                    const int pidx = ki * nk + __float_as_int(xj.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const float3 rv = rv_of(xi, xj, o);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
+                    {
+                        float b;
+                        const int ir2 = table_index(r2 * inv_h, kmax, b);
+                        ac.part[0] += spl_val(g.pkf_rho[(size_t)pp.jloc * nint + ir2], b);
+                    }
+                    ac.tick();
+                });
+                ac.flush();
+                rho = ac.sum[0];
+            }
+            const double qr = rho * g.inv_drho;
+            int irho = (int)qr;
+            if (irho >= g.Nrho - 1 || irho < 0)
+            {
+                atomic_or_err(dyn, FMDG_ERRBIT_RHO_RANGE);
+                irho = irho < 0 ? 0 : g.Nrho - 2;
+            }
+            const int nrint = g.Nrho - 1;
+            double fp;
+            if (!MIXED)
+            {
+                const double b = qr - irho;
+                const double4_32a tf = g.pk_F[(size_t)ei * nrint + irho];
+                fp = spl_der(tf, b, g.inv_drho);
+                acc[0] = spl_val(tf, b);
+            }
+            else
+            {
+                const float b = (float)(qr - irho);
+                const float4 tf = g.pkf_F[(size_t)ei * nrint + irho];
+                const float f32 = spl_der(tf, b, (float)g.inv_drho);
+                g.fpb[t] = f32;
+                fp = (double)f32;
+                acc[0] = (double)spl_val(tf, b);
+            }
+            g.vaream[i] = fp;
+            g.fpd[t] = fp;
+        }
+        else
+        {
+            g.vaream[i] = 0.0;
+            g.fpd[t] = 0.0;
+            g.fpb[t] = 0.f;
+        }
+    }
+    block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
+}
+
+// Pair forces + velocity-Verlet finish step (src/integrators.c:94-126) and
+// the thermo record, one thread per slot; the forces are stored in the
+// current order for the next start step.
+template <int CAT, bool MIXED>
+__global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocPack loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const int group = g.st.group;
+    const double dt = g.st.dt;
+    __shared__ SmemPot sp;
+    __shared__ SkinOff so;
+    load_pot(g, sp);
+    load_offsets(g, so);
+    Dyn *dyn = g.dyn;
+    const Side S = g.side[dyn->cur];
+    const int cap = g.cap;
+    const int t = bx * blockDim.x + threadIdx.x;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const int i = (t < cap) ? g.pos[t] : -1;
+    if (i >= 0)
+    {
+        float4 xi = g.xl[t];
+        const int ki = __float_as_int(xi.w);
+        const bool active = (group < 0 || g.gslot[t] == group);
+        const int nk = g.nkinds;
+        double f[3] = {0.0, 0.0, 0.0};
+        double pe = 0.0;
+        if (active)
+        {
+            const int nint = g.Nr2 - 1;
+            const size_t ne = g.nelem;
+            if (!MIXED)
+            {
+                const double4_32a xdi = g.xd[t];
+                const double fpi = (CAT == CAT_EAM) ? g.fpd[t] : 0.0;
+                const double inv_h = g.inv_dr2;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4, float4) {
+                    if (group >= 0 && g.gslot[js] != group) return;
+                    const double4_32a xj = g.xd[js];
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    const Geom64 p = geom64_mi(g, xdi, xj);
+                    if (CAT == CAT_LJ && p.r2 < pp.p[2])
+                    {
+                        double fa, e;
+                        lj_pair(p.r2, pp, fa, e);
+                        for (int d = 0; d < 3; d++) f[d] += p.rv[d] * fa;
+                        pe += e;
+                    }
+                    else if (CAT == CAT_MORSE && p.r2 < pp.p[3])
+                    {
+                        double fa, e;
+                        morse_pair(p.r2, pp, fa, e);
+                        for (int d = 0; d < 3; d++) f[d] += fa * p.rv[d];
+                        pe += e;
+                    }
+                    else if (CAT == CAT_EAM && p.r2 < pp.p[2])
+                    {
+                        const double q = p.r2 * inv_h;
+                        const int ir2 = min((int)q, nint - 1);
+                        const double b = q - ir2;
+                        const int ei = pp.iloc, ej = pp.jloc;
+                        const double4_32a tph = g.pk_phi[((size_t)ei * ne + ej) * nint + ir2];
+                        const double phi_d = spl_der(tph, b, inv_h);
+                        const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], b, inv_h);
+                        const double rho_jp = (ei == ej) ? rho_ip
+                                            : spl_der(g.pk_rho[(size_t)ej * nint + ir2], b, inv_h);
+                        const double mag = 2 * (fpi * rho_jp + g.fpd[js] * rho_ip + phi_d);
+                        for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
+                        pe += 0.5 * spl_val(tph, b);
+                    }
+                });
+            }
+            else
+            {
+                const float fpi = (CAT == CAT_EAM) ? g.fpb[t] : 0.f;
+                const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
+                Acc32<4> ac;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                    if (group >= 0 && g.gslot[js] != group) return;
+                    const int pidx = ki * nk + __float_as_int(xj.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const float3 rv = rv_of(xi, xj, o);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    if (CAT == CAT_LJ)
+                    {
+                        if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
+                        {
+                            float fa, e;
+                            lj_pair(r2, sp.pf[pidx][0], sp.pf[pidx][1], fa, e);
+                            ac.part[0] += rv.x * fa;
+                            ac.part[1] += rv.y * fa;
+                            ac.part[2] += rv.z * fa;
+                            ac.part[3] += e;
+                        }
+                    }
+                    else if (CAT == CAT_MORSE)
+                    {
+                        if (within_cut_skin(g, t, js, r2, sp.pf[pidx][3], pp.p[3]))
+                        {
+                            float fa, e;
+                            morse_pair(r2, sp.pf[pidx][0], sp.pf[pidx][1], sp.pf[pidx][2], fa, e);
+                            ac.part[0] += fa * rv.x;
+                            ac.part[1] += fa * rv.y;
+                            ac.part[2] += fa * rv.z;
+                            ac.part[3] += e;
+                        }
+                    }
+                    else if (CAT == CAT_EAM)
+                    {
+                        if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
+                        {
+                            float b;
+                            const int ir2 = table_index(r2 * inv_h, kmax, b);
+                            const int ei = pp.iloc, ej = pp.jloc;
+                            const float4 tph = g.pkf_phi[((size_t)ei * ne + ej) * nint + ir2];
+                            const float phi_d = spl_der(tph, b, inv_h);
+                            const float rho_ip = spl_der(g.pkf_rho[(size_t)ei * nint + ir2], b, inv_h);
+                            const float rho_jp = (ei == ej) ? rho_ip
+                                               : spl_der(g.pkf_rho[(size_t)ej * nint + ir2], b, inv_h);
+                            const float mag = 2.f * (fpi * rho_jp + g.fpb[js] * rho_ip + phi_d);
+                            ac.part[0] -= mag * rv.x;
+                            ac.part[1] -= mag * rv.y;
+                            ac.part[2] -= mag * rv.z;
+                            ac.part[3] += 0.5f * spl_val(tph, b);
+                        }
+                    }
+                    ac.tick();
+                });
+                ac.flush();
+                for (int d = 0; d < 3; d++) f[d] = ac.sum[d];
+                pe = ac.sum[3];
+            }
+        }
+        for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
+        acc[0] = pe;
+        if (active)
+        {
+            const double m = sp.mass[ki];
+            double v[3] = {S.v[i], S.v[cap + i], S.v[2 * (size_t)cap + i]};
+            const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
+            for (int d = 0; d < 3; d++)
+            {
+                v[d] = __dadd_rn(v[d], __dmul_rn(coef, f[d]));
+                S.v[(size_t)d * cap + i] = v[d];
+            }
+            acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            acc[2] = m * v[0];
+            acc[3] = m * v[1];
+            acc[4] = m * v[2];
+            acc[5] = 1.0;
+        }
+    }
+    __shared__ double blk[6];
+    __shared__ unsigned ticket;
+    block_reduce_store<6>(acc, blk);
+    if (threadIdx.x == 0)
+    {
+        for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
+        __threadfence();
+        ticket = atomicAdd(&dyn->blocks_done, 1u);
+    }
+    __syncthreads();
+    if (ticket == (unsigned)nb - 1)
+    {
+        __threadfence();
+        final_reduce(g, nb, 0, g.has_eam, g.st.thermostat, dt, g.st.tau, g.st.T0);
+        if (threadIdx.x == 0)
+        {
+            dyn->blocks_done = 0;
+            if (dyn->steps_left > 0) dyn->steps_left--;
+        }
+    }
+}
+
+template <bool MIXED>
+void launch_force_skin(const fmdg_pack_launch &P, int nfb)
+{
+    const LocPack &L = P.lf;
+    if (P.cat == FMDG_POT_LJ) k_force_skin<CAT_LJ, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
+    else if (P.cat == FMDG_POT_MORSE) k_force_skin<CAT_MORSE, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
+    else k_force_skin<CAT_EAM, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
+}
+
+} // namespace
+
+// phases: bit 0 slot tables + list (re)build, bit 1 EAM density, bit 2
+// pair forces + finish step (all three for a step).  Returns the kernels
+// launched, or minus a status.
+int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
+{
+    cudaStream_t st = P.stream;
+    const int nab = P.la.bstart[P.nsys], nfb = P.lf.bstart[P.nsys];
+    int n = 0;
+    if (phases & 1)
+    {
+        k_prep_skin<<<nab, 128, 0, st>>>(P.la);
+        k_nlist_skin<<<nfb, P.fblk, 0, st>>>(P.lf);
+        n += 2;
+    }
+    if ((phases & 2) && P.cat == FMDG_POT_EAM)
+    {
+        if (P.mixed) k_density_skin<true><<<nfb, P.fblk, 0, st>>>(P.lf);
+        else k_density_skin<false><<<nfb, P.fblk, 0, st>>>(P.lf);
+        n++;
+    }
+    if (phases & 4)
+    {
+        if (P.mixed) launch_force_skin<true>(P, nfb);
+        else launch_force_skin<false>(P, nfb);
+        n++;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -fmdg_fail("pack forces", e);
+    return n;
+}

@@ -85,7 +85,7 @@ def bind(L):
         "fmdg_last_error": ([], C.c_char_p),
         "fmdg_srv_create": ([P(vp), i, sz, i, i], i), "fmdg_srv_destroy": ([vp], None),
         "fmdg_srv_set_eam": ([vp, i, i, i, d, i, d] + [P(d)] * 6, i),
-        "fmdg_srv_set_tuning": ([vp, i], i), "fmdg_srv_submit": ([vp, P(JobDesc), P(C.c_longlong)], i),
+        "fmdg_srv_set_tuning": ([vp, i], i), "fmdg_srv_set_skin": ([vp, d], i), "fmdg_srv_submit": ([vp, P(JobDesc), P(C.c_longlong)], i),
         "fmdg_srv_progress": ([vp, i, P(i)], i), "fmdg_srv_result": ([vp, C.c_longlong, P(JobResult)], i),
         "fmdg_srv_state": ([vp, C.c_longlong, P(d), P(d), P(d), P(C.c_uint)], i),
         "fmdg_srv_release": ([vp, C.c_longlong], i), "fmdg_srv_now": ([vp, P(d)], i),
@@ -219,6 +219,9 @@ class Server:
 
     def set_tuning(self, fblk):
         check(self.L, self.L.fmdg_srv_set_tuning(self.h, fblk), "fmdg_srv_set_tuning")
+
+    def set_skin(self, skin):
+        check(self.L, self.L.fmdg_srv_set_skin(self.h, skin), "fmdg_srv_set_skin")
 
     def submit(self, pot, x, v, l, steps, precision=PREC_MIXED, keep_state=False, dt=None):
         P = POTENTIALS[pot]

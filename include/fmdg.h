@@ -242,8 +242,9 @@ int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner);
    category and precision are stepped together by one launch per kernel
    (velocity Verlet, NVE), chunk_steps steps per captured CUDA graph; the
    threads per block of the list/density/force kernels are autotuned per
-   pack unless fixed with fmdg_srv_set_tuning.  A job's per-atom arithmetic
-   is the single-system arithmetic, independent of the other jobs. */
+   pack unless fixed with fmdg_srv_set_tuning.  A job's arithmetic does not
+   depend on the other jobs: alone or in any mix its trajectory is the same
+   bit for bit. */
 typedef struct fmdg_server fmdg_server_t;
 
 typedef struct
@@ -295,6 +296,12 @@ int  fmdg_srv_set_eam(fmdg_server_t *srv, int key, int nelem, int Nrho, double d
                       const double *phi, const double *phiDD);
 /* 0: autotune (default); 64, 128 or 256: fixed threads per block */
 int  fmdg_srv_set_tuning(fmdg_server_t *srv, int fblk);
+/* Verlet skin of the packed neighbour lists (default 0.5 A): a job's list
+   holds the pairs within its largest cutoff + skin and is rebuilt once an
+   atom has moved more than skin/2 since the last build; the skin is capped
+   below half of every periodic box length minus the cutoff.  Jobs need
+   periodic box lengths above twice the cutoff. */
+int  fmdg_srv_set_skin(fmdg_server_t *srv, double skin);
 /* queue a job (the description is copied) */
 int  fmdg_srv_submit(fmdg_server_t *srv, const fmdg_job_desc_t *job, long long *id);
 /* one turn of the serving loop (reap finished chunks, admit, launch);
