@@ -56,32 +56,36 @@ void dfree(fmdg_sys_t *s, void *p) { if (p) cudaFreeAsync(p, s->stream); }
 void free_atoms(fmdg_sys_t *s)
 {
     Geo &g = s->g;
-    for (int k = 0; k < 2; k++)
-    {
-        Side &S = g.side[k];
-        dfree(s, S.x); dfree(s, S.v); dfree(s, S.kind); dfree(s, S.group); dfree(s, S.atomid);
-        dfree(s, S.cell_of); dfree(s, S.cell_start); dfree(s, S.slot);
-        memset(&S, 0, sizeof S);
-    }
-    dfree(s, g.F); dfree(s, g.vaream);
-    dfree(s, g.xf4); dfree(s, g.nbr); dfree(s, g.nbr_count); dfree(s, g.fpf);
-    g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr; g.fpf = nullptr;
-    dfree(s, g.bdest); dfree(s, g.bpath); dfree(s, g.bslot); dfree(s, g.brank); dfree(s, g.bnewidx);
-    dfree(s, g.dep_count); dfree(s, g.arr_base); dfree(s, g.bucket); dfree(s, g.arr_slot);
-    dfree(s, g.partials);
-    dfree(s, g.pos); dfree(s, g.cb); dfree(s, g.xl); dfree(s, g.xb); dfree(s, (void *)g.xd);
-    dfree(s, g.gslot); dfree(s, g.fpb); dfree(s, g.fpd);
-    g.pos = g.cb = nullptr; g.xl = g.xb = nullptr; g.xd = nullptr; g.gslot = nullptr;
-    g.fpb = nullptr; g.fpd = nullptr;
+    dfree(s, s->arena);
+    s->arena = nullptr;
+    for (int k = 0; k < 2; k++) memset(&g.side[k], 0, sizeof(Side));
     g.F = g.vaream = nullptr;
+    g.xf4 = nullptr; g.nbr = nullptr; g.nbr_count = nullptr; g.fpf = nullptr;
     g.bdest = g.bpath = g.bslot = g.brank = g.bnewidx = nullptr;
     g.dep_count = g.arr_lower = g.arr_total = g.bucket_fill = g.arr_base = nullptr;
     g.bucket = g.arr_slot = nullptr;
     g.partials = nullptr;
+    g.pos = g.cb = nullptr; g.xl = g.xb = nullptr; g.xd = nullptr; g.gslot = nullptr;
+    g.fpb = nullptr; g.fpd = nullptr;
     g.cap = 0;
     s->atoms = false;
     if (s->graph_key_valid) { cudaGraphExecDestroy(s->graph); s->graph_key_valid = 0; }
 }
+
+// Lays the per-atom and per-cell buffers of a system out in one device
+// allocation (256-byte aligned); a pass without a base measures it.
+struct Carver
+{
+    char *base;
+    size_t off;
+    template <typename T>
+    void take(T *&p, size_t n)
+    {
+        off = (off + 255) & ~(size_t)255;
+        p = base ? (T *)(base + off) : nullptr;
+        off += (n ? n : 1) * sizeof(T);
+    }
+};
 
 // forget EAM tables that belong to another system
 void drop_eam(fmdg_sys_t *s)
@@ -475,24 +479,12 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     for (int i = 0; i < n; i++)
         if (kind[i] >= (unsigned)(s->nkinds > 0 ? s->nkinds : FMDG_MAXK))
             return fmdg_set_error("fmdg_upload: atom kind out of range");
+    Dyn d;
+    FMDG_CK(cudaMemcpy(&d, g.dyn, sizeof d, cudaMemcpyDeviceToHost));
     free_atoms(s);
     const int cap = n > 0 ? n : 1;
     g.cap = cap;
     int rc;
-    for (int k = 0; k < 2; k++)
-    {
-        Side &S = g.side[k];
-        if ((rc = dalloc(s, &S.x, 3 * (size_t)cap)) || (rc = dalloc(s, &S.v, 3 * (size_t)cap)) ||
-            (rc = dalloc(s, &S.kind, cap)) || (rc = dalloc(s, &S.group, cap)) || (rc = dalloc(s, &S.atomid, cap)) ||
-            (rc = dalloc(s, &S.cell_of, cap)) || (rc = dalloc(s, &S.cell_start, (size_t)ncell + 1)))
-            return rc;
-    }
-    if ((rc = dalloc(s, &g.F, 3 * (size_t)cap)) || (rc = dalloc(s, &g.vaream, cap)) ||
-        (rc = dalloc(s, &g.bdest, cap)) || (rc = dalloc(s, &g.bpath, cap)) || (rc = dalloc(s, &g.bslot, cap)) ||
-        (rc = dalloc(s, &g.brank, cap)) || (rc = dalloc(s, &g.bnewidx, cap)) ||
-        (rc = dalloc(s, &g.dep_count, 4 * (size_t)ncell)) || (rc = dalloc(s, &g.arr_base, (size_t)ncell + 1)) ||
-        (rc = dalloc(s, &g.bucket, cap)) || (rc = dalloc(s, &g.arr_slot, cap)))
-        return rc;
     // neighbour list: size from the densest cell (an atom with more
     // candidates falls back to a direct stencil scan)
     double rc2max = 0.0;
@@ -511,35 +503,54 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     g.rlist2 = (float)(rlist * rlist);
     const int maxnb = fmdg_list_capacity(s, cell_count, ncell);
     g.maxnb = maxnb;
-    for (int d = 0; d < 3; d++) g.cellh_f[d] = (float)g.cellh[d];
-    if ((rc = dalloc(s, &g.fpf, cap)) || (rc = dalloc(s, &g.xf4, cap)) || (rc = dalloc(s, &g.nbr, (size_t)cap * maxnb)) || (rc = dalloc(s, &g.nbr_count, cap)))
-        return rc;
+    for (int d3 = 0; d3 < 3; d3++) g.cellh_f[d3] = (float)g.cellh[d3];
+    g.skin_on = g.skin > 0.0;
+    if (g.skin_on && cap >= (1 << 25)) return fmdg_set_error("fmdg_upload: skin lists hold at most 2^25 atoms");
+    // partials for the smallest block size the tuner may pick (64)
+    const int nb = fmdg_grid(cap, 64);
+    auto layout = [&](Carver &c) {
+        for (int k = 0; k < 2; k++)
+        {
+            Side &S = g.side[k];
+            c.take(S.x, 3 * (size_t)cap); c.take(S.v, 3 * (size_t)cap);
+            c.take(S.kind, cap); c.take(S.group, cap); c.take(S.atomid, cap);
+            c.take(S.cell_of, cap); c.take(S.cell_start, (size_t)ncell + 1);
+            if (g.skin_on) c.take(S.slot, cap);
+        }
+        c.take(g.F, 3 * (size_t)cap); c.take(g.vaream, cap);
+        c.take(g.bdest, cap); c.take(g.bpath, cap); c.take(g.bslot, cap); c.take(g.brank, cap);
+        c.take(g.bnewidx, cap); c.take(g.dep_count, 4 * (size_t)ncell); c.take(g.arr_base, (size_t)ncell + 1);
+        c.take(g.bucket, cap); c.take(g.arr_slot, cap);
+        c.take(g.fpf, cap); c.take(g.xf4, cap); c.take(g.nbr, (size_t)cap * maxnb); c.take(g.nbr_count, cap);
+        c.take(g.partials, (size_t)nb * 9 + 8);
+        if (g.skin_on)
+        {
+            c.take(g.pos, cap); c.take(g.cb, cap); c.take(g.xl, cap); c.take(g.xb, cap);
+            c.take(g.xd, cap); c.take(g.gslot, cap); c.take(g.fpb, cap); c.take(g.fpd, cap);
+        }
+    };
+    Carver measure{nullptr, 0};
+    layout(measure);
+    if ((rc = dalloc(s, &s->arena, measure.off))) return rc;
+    Carver carve{s->arena, 0};
+    layout(carve);
     g.arr_lower = g.dep_count + ncell;
     g.arr_total = g.dep_count + 2 * ncell;
     g.bucket_fill = g.dep_count + 3 * ncell;
-    // partials for the smallest block size the tuner may pick (64)
-    const int nb = fmdg_grid(cap, 64);
-    if ((rc = dalloc(s, &g.partials, (size_t)nb * 9 + 8))) return rc;
-    g.skin_on = g.skin > 0.0;
-    if (g.skin_on && cap >= (1 << 25)) return fmdg_set_error("fmdg_upload: skin lists hold at most 2^25 atoms");
+    cudaStream_t st = s->stream;
+    std::vector<int> iota;
     if (g.skin_on)
     {
-        for (int k = 0; k < 2; k++)
-            if ((rc = dalloc(s, &g.side[k].slot, cap))) return rc;
-        if ((rc = dalloc(s, &g.pos, cap)) || (rc = dalloc(s, &g.cb, cap)) || (rc = dalloc(s, &g.xl, cap)) ||
-            (rc = dalloc(s, &g.xb, cap)) || (rc = dalloc(s, (double4_32a **)&g.xd, cap)) ||
-            (rc = dalloc(s, &g.gslot, cap)) || (rc = dalloc(s, &g.fpb, cap)) || (rc = dalloc(s, &g.fpd, cap)))
-            return rc;
-        std::vector<int> iota(cap);
+        iota.resize(cap);
         for (int k = 0; k < cap; k++) iota[k] = k;
-        FMDG_CK(cudaMemcpy(g.side[0].slot, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(g.pos, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync(g.side[0].slot, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice, st));
+        FMDG_CK(cudaMemcpyAsync(g.pos, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice, st));
         const double rsk = sqrt(rc2max) + g.skin;
         g.rskin2 = (float)(rsk * rsk);
         g.half_skin2 = (float)(0.25 * g.skin * g.skin);
         g.srad = 1;
-        for (int d = 0; d < 3; d++)
-            if (rsk > g.cellh[d]) g.srad = 2;
+        for (int d3 = 0; d3 < 3; d3++)
+            if (rsk > g.cellh[d3]) g.srad = 2;
         if (rsk > 2.0 * fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2])))
             return fmdg_set_error("fmdg_upload: skin list radius above two cells");
     }
@@ -552,20 +563,18 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
             hv[(size_t)d * cap + i] = v[3 * (size_t)i + d];
         }
     Side &S = g.side[0];
-    FMDG_CK(cudaMemcpy(S.x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy(S.v, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync(S.x, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, st));
+    FMDG_CK(cudaMemcpyAsync(S.v, hv.data(), hv.size() * 8, cudaMemcpyHostToDevice, st));
     if (n > 0)
     {
-        FMDG_CK(cudaMemcpy(S.kind, kind, (size_t)n * 4, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(S.group, group, (size_t)n * 4, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(S.atomid, atomid, (size_t)n * 4, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(S.cell_of, cell_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync(S.kind, kind, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+        FMDG_CK(cudaMemcpyAsync(S.group, group, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+        FMDG_CK(cudaMemcpyAsync(S.atomid, atomid, (size_t)n * 4, cudaMemcpyHostToDevice, st));
+        FMDG_CK(cudaMemcpyAsync(S.cell_of, cell_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
     }
-    FMDG_CK(cudaMemcpy(S.cell_start, start.data(), ((size_t)ncell + 1) * 4, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemset(g.F, 0, 3 * (size_t)cap * 8));
-    FMDG_CK(cudaMemset(g.vaream, 0, (size_t)cap * 8));
-    Dyn d;
-    FMDG_CK(cudaMemcpy(&d, g.dyn, sizeof d, cudaMemcpyDeviceToHost));
+    FMDG_CK(cudaMemcpyAsync(S.cell_start, start.data(), ((size_t)ncell + 1) * 4, cudaMemcpyHostToDevice, st));
+    FMDG_CK(cudaMemsetAsync(g.F, 0, 3 * (size_t)cap * 8, st));
+    FMDG_CK(cudaMemsetAsync(g.vaream, 0, (size_t)cap * 8, st));
     const double keep_time = d.time, keep_dt = d.dt;
     memset(&d, 0, sizeof d);
     d.cur = 0;
@@ -574,7 +583,9 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     d.rebuild = 1;
     d.time = keep_time;
     d.dt = keep_dt;
-    FMDG_CK(cudaMemcpy(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice, st));
+    // the host staging buffers are released on return
+    FMDG_CK(cudaStreamSynchronize(st));
     s->atoms = true;
     return FMDG_OK;
 }

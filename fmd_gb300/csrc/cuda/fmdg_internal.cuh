@@ -164,6 +164,7 @@ struct fmdg_sys
     int graph_mode;               // 0 velocity Verlet, 1 symplectic Euler
     int fblk;                     // threads per block of the list/density/force kernels
     bool eam_borrowed;            // EAM tables belong to another system
+    char *arena;                  // one device allocation holding the per-atom and per-cell buffers
 };
 
 // ---- which system a thread block works on ------------------------------------

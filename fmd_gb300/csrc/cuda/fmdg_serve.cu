@@ -12,9 +12,9 @@
 //    thermo record are computed on that stream;
 //  * admitted systems of one pair category and precision form a pack; one
 //    launch per kernel advances every member by one velocity-Verlet step
-//    (LocPack: a block->system table), and a chunk of `chunk_steps` steps
-//    is captured once as a CUDA graph and replayed until the membership
-//    changes;
+//    (LocPack: the systems' geometry in kernel parameters), one step is
+//    captured once as a CUDA graph, a chunk replays it `chunk_steps` times,
+//    until the membership changes;
 //  * every member carries its own step budget on the device (steps_left):
 //    a member that has finished is skipped by every kernel, so a chunk
 //    needs no host decision in the middle;
@@ -286,9 +286,13 @@ int setup_job(fmdg_server_t *S, Job *j)
 
 int retire(fmdg_server_t *S, Job *j);
 
-int admit(fmdg_server_t *S)
+// Admits queued jobs in FIFO order while they fit; at most `budget_s` of
+// host time per call (0: no limit), so a serving loop keeps launching
+// chunks between admissions.
+int admit(fmdg_server_t *S, double budget_s)
 {
-    while (!S->queue.empty())
+    const double t_end = wall_s() + budget_s;
+    while (!S->queue.empty() && (budget_s <= 0.0 || wall_s() < t_end))
     {
         Job *j = S->queue.front();
         if (j->bytes > S->budget)
@@ -371,13 +375,14 @@ int rebuild(fmdg_server_t *S, Pack &p)
         if (j->ready) FMDG_CK(cudaStreamWaitEvent(p.stream, j->ready, 0));
     cudaGraph_t graph;
     FMDG_CK(cudaStreamBeginCapture(p.stream, cudaStreamCaptureModeThreadLocal));
+    // one step per graph, replayed chunk_steps times: a membership change
+    // re-captures 10-11 kernels, not chunk_steps times as many
     int rc = FMDG_OK, nk = 0;
-    for (int k = 0; k < S->chunk && !rc; k++)
     {
         int a = fmdg_pack_launch_refresh(P);
         int b = a < 0 ? a : fmdg_pack_launch_forces(P, 7);
         if (a < 0 || b < 0) rc = -(a < 0 ? a : b);
-        else nk += a + b;
+        else nk = a + b;
     }
     cudaError_t e = cudaStreamEndCapture(p.stream, &graph);
     if (rc) return rc;
@@ -408,9 +413,9 @@ int launch_chunk(fmdg_server_t *S, Pack &p)
     c.atom_steps = 0.0;
     c.members = p.members;
     FMDG_CK(cudaEventRecord(c.ev0, p.stream));
-    FMDG_CK(cudaGraphLaunch(p.exec, p.stream));
+    for (int k = 0; k < S->chunk; k++) FMDG_CK(cudaGraphLaunch(p.exec, p.stream));
     FMDG_CK(cudaEventRecord(c.ev1, p.stream));
-    S->kernels += p.exec_kernels;
+    S->kernels += (long long)p.exec_kernels * S->chunk;
     bool full = true;
     for (Job *j : c.members)
     {
@@ -727,7 +732,9 @@ extern "C" int fmdg_srv_progress(fmdg_server_t *S, int wait, int *active)
     int rc = FMDG_OK;
     each_pack(S, [&](Pack &p) { if (!rc) rc = reap(S, p, false); });
     if (rc) return rc;
-    if ((rc = admit(S))) return rc;
+    const size_t queued = S->queue.size();
+    if ((rc = admit(S, 0.002))) return rc;
+    const bool admitted = S->queue.size() != queued;
     bool launched = false;
     each_pack(S, [&](Pack &p) {
         if (rc || p.inflight.size() >= 2 || p.active() == 0) return;
@@ -735,7 +742,7 @@ extern "C" int fmdg_srv_progress(fmdg_server_t *S, int wait, int *active)
         launched = true;
     });
     if (rc) return rc;
-    if (wait && !launched)
+    if (wait && !launched && !admitted)
     {
         // the pack whose oldest chunk was launched first
         Pack *oldest = nullptr;
@@ -830,7 +837,7 @@ extern "C" int fmdg_srv_stats(fmdg_server_t *S, fmdg_srv_stats_t *out)
 extern "C" int fmdg_srv_admit(fmdg_server_t *S)
 {
     FMDG_CK(cudaSetDevice(S->device));
-    return admit(S);
+    return admit(S, 0.0);
 }
 
 // Advance every admitted job by k chunks: the packs' chunk graphs are
