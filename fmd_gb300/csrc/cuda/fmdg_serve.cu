@@ -241,10 +241,14 @@ int setup_job(fmdg_server_t *S, Job *j)
     if (rc) return rc;
     fmdg_sys_t *s = j->sys;
     if ((rc = fmdg_set_box(s, j->l, j->pbc, j->nc, j->cellh))) return rc;
-    // list radius rc + skin below half of every periodic box length
+    // list radius rc + skin below half of every periodic box length; when
+    // the cells leave room for a skin of 0.25 A or more, the skin stays
+    // inside one cell so a rebuild scans 27 cells, not 125
     double skin = S->skin;
     for (int d = 0; d < 3; d++)
         if (j->pbc[d]) skin = std::min(skin, 0.9 * (0.5 * j->l[d] - j->rcmax));
+    const double room = std::min(j->cellh[0], std::min(j->cellh[1], j->cellh[2])) - j->rcmax;
+    if (room >= 0.25 && room < skin) skin = 0.999 * room;
     if ((rc = fmdg_set_skin(s, skin))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
