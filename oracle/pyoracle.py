@@ -60,6 +60,9 @@ class Oracle:
         self.o = C.c_void_p(self.L.oracle_create())
         self.L.oracle_set_threads(self.o, threads)
 
+    def set_threads(self, threads: int):
+        self.L.oracle_set_threads(self.o, threads)
+
     def close(self):
         if self.o:
             self.L.oracle_destroy(self.o)

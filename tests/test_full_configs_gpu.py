@@ -1,0 +1,173 @@
+"""Full-size runs of the reference-path configurations through the fmd.h
+API on the GPU.
+
+* argon LJ, 4000 atoms: 2 ps Berendsen equilibration (tau 0.1 ps, 100 K)
+  then 10 000 NVE steps at 2 fs; trajectories diverge chaotically, so the
+  NVE energy drift (max |E(t) - E(0)| / |E(0)| over 20 samples) is compared:
+  binary64 and mixed precision within 2x the oracle's drift (+1e-7).
+* Morse collision, 512 000-atom slab + a 20 A projectile sphere at 2 km/s,
+  periodic x, y, 100 A vacuum in z: step-0 forces against the oracle
+  (binary64 1e-10, mixed 1e-5 of max |F|), then 200 steps: no atom lost
+  before the impact, transverse momentum conserved (binary64: to 1e-9 of
+  sum |m v|; mixed: centre-of-mass velocity change below 1e-4 A/ps).
+* laser-heated EAM slab with a 1-D TTM grid (20 x 20 x 100 FCC cells =
+  160 000 atoms, vacuum above and below, 50 TTM cells along z): 120 steps
+  around the pulse: no error, every active cell's electron temperature
+  finite and above the initial 300 K where the pulse arrives.
+"""
+import ctypes as C
+import os
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+import cases
+from test_parity_oracle_gpu import build_both
+
+from fmd_gb300 import api, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _energy(lib, md):
+    return lib.fmd_matt_getTotalEnergy(md)
+
+
+def _lj4000():
+    x, v = workloads.fcc_state(10, 10, 10, 5.26, 100.0, 39.948, seed=1)
+    return dict(box=(52.6,) * 3, pbc=(1, 1, 1), kinds=[("Ar", 39.948)],
+                pots=[("lj", 0, 0, 3.405, 0.0104, 8.5125)], x=x, v=v, kind=np.zeros(len(x), np.uint32),
+                group=np.zeros(len(x), np.int32), dt=0.002)
+
+
+def _drift(series):
+    e = np.asarray(series)
+    assert np.all(np.isfinite(e))
+    return float(np.abs(e - e[0]).max() / abs(e[0]))
+
+
+def test_lj_argon_nve_drift(gpu_lib):
+    lib = gpu_lib
+    spec = _lj4000()
+    drifts = {}
+    with tempfile.TemporaryDirectory() as work:
+        for prec in (0, 1):
+            md, o = build_both(lib, spec, work, precision=prec)
+            lib.fmd_dync_equilibrate(md, -1, 2.0, 0.002, 0.1, 100.0)
+            es = [_energy(lib, md)]
+            for _ in range(20):
+                lib.fmd_dync_integrate(md, -1, 1.0, 0.002)
+                es.append(_energy(lib, md))
+            drifts[prec] = _drift(es)
+            lib.fmd_free(md)
+            if prec == 1:
+                # the oracle: the same protocol in binary64 on the host
+                o.set_threads(os.cpu_count() or 1)
+                o.forces(-1)
+                o.thermo(-1)          # the first Berendsen scale needs T
+                o.vv(1000, 0.002, -1, 1, 0.1, 100.0)
+                th = o.get_thermo()
+                eo = [th.kinetic + th.potential]
+                for _ in range(20):
+                    o.vv(500, 0.002)
+                    th = o.get_thermo()
+                    eo.append(th.kinetic + th.potential)
+                drifts["oracle"] = _drift(eo)
+            o.close()
+    bound = 2.0 * drifts["oracle"] + 1e-7
+    assert drifts[0] <= bound, drifts
+    assert drifts[1] <= bound, drifts
+
+
+def _collision(seed=3):
+    a = 3.615
+    lx = 80 * a
+    x, v = workloads.fcc_state(80, 80, 20, a, 300.0, 63.546, seed=seed, origin=(0.0, 0.0, 2.0))
+    top = 2.0 + 20 * a
+    lz = 20 * a + 100.0
+    # projectile: FCC sites within 20 A of a centre 25 A above the slab
+    c = np.array([lx / 2, lx / 2, top + 25.0])
+    n = 13
+    sph = workloads.fcc_sites(n, n, n, a, origin=tuple(c - n * a / 2))
+    sph = sph[np.linalg.norm(sph - c, axis=1) <= 20.0]
+    rng = np.random.default_rng(seed + 1)
+    vs = workloads.maxwell_velocities(len(sph), 63.546, 300.0, rng)
+    vs[:, 2] -= 20.0                      # -2 km/s (src/general.h:40: 1e-2 A/ps per m/s)
+    x = np.concatenate([x, sph])
+    v = np.concatenate([v, vs])
+    return dict(box=(lx, lx, lz), pbc=(1, 1, 0), kinds=[("Cu", 63.546)],
+                pots=[("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)], x=x, v=v,
+                kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), dt=0.001)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_morse_collision_full_size(gpu_lib, precision):
+    lib = gpu_lib
+    spec = _collision()
+    n0 = len(spec["x"])
+    assert n0 > 512000
+    with tempfile.TemporaryDirectory() as work:
+        md, o = build_both(lib, spec, work, precision=precision)
+        lib.fmd_dync_integrate(md, -1, 0.0, 0.001)
+        g0 = lib.dump(md)
+        o.set_threads(os.cpu_count() or 1)
+        o.forces(-1)
+        r0 = o.dump()
+        o.close()
+        np.testing.assert_array_equal(g0["id"], r0["id"])
+        tol = 1e-10 if precision == 0 else 1e-5
+        err = np.abs(g0["F"] - r0["F"]).max() / np.abs(r0["F"]).max()
+        assert err <= tol, err
+        p0 = (C.c_double * 3)()
+        lib.fmd_matt_getMomentum(md, p0)
+        lib.fmd_dync_integrate(md, -1, 0.1995, 0.001)
+        p1 = (C.c_double * 3)()
+        lib.fmd_matt_getMomentum(md, p1)
+        d = lib.dump(md)
+        assert len(d["id"]) == n0
+        m = 63.546 / workloads.MD_MASS_UNIT
+        if precision == 0:
+            scale = np.abs(d["v"]).sum() * m
+            assert abs(p1[0] - p0[0]) <= 1e-9 * scale and abs(p1[1] - p0[1]) <= 1e-9 * scale
+        else:
+            # pair forces are exactly antisymmetric, but in a crystal every
+            # atom's binary32 partial sums round alike, so the net force is
+            # N times one rounding error, not sqrt(N) times: bound the
+            # centre-of-mass velocity it leaves (A/ps)
+            dv = np.hypot(p1[0] - p0[0], p1[1] - p0[1]) / (n0 * m)
+            assert dv <= 1e-4, dv
+        lib.fmd_free(md)
+
+
+def test_ttm_slab_full_size(gpu_lib):
+    lib = gpu_lib
+    a = 3.615
+    nx, nz = 20, 100
+    lx, lz = nx * a, nz * a + 40.0
+    x, v = workloads.fcc_state(nx, nx, nz, a, 300.0, 63.546, seed=4, origin=(0.0, 0.0, 20.0))
+    n = len(x)
+    assert n == 160000
+    state = dict(names=["Cu"], kind=np.zeros(n, np.uint32), group=np.zeros(n, np.int32), x=x, v=v)
+    case = dict(box=(lx, lx, lz), pbc=(1, 1, 0), names=["Cu"], pots=[("eam_analytic", 0, 0)],
+                turi=dict(cat=1, dims=(1, 1, 50), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100, frac=0.1,
+                          laser=(500.0, 0.0, 0.06e-12, 100e-15, 15e-9)))
+    cases.CASES["ttm_slab_full"] = dict(case, state=lambda: state, run=("integrate", -1, 0.001), steps=120, every=40)
+    try:
+        with tempfile.TemporaryDirectory() as work:
+            md, _ = cases.setup(lib, "ttm_slab_full", work, state)
+            rec = cases.Recorder(lib)
+            lib.fmd_setEventHandler(md, None, rec.cb)
+            lib.fmd_dync_integrate(md, -1, 0.1195, 0.001)
+            assert rec.errors == [], rec.errors
+            ttm = lib.ttm_1d(md)
+            te = np.asarray(ttm["Te"])
+            active = te >= 0.0
+            assert active.sum() > 10
+            assert np.all(np.isfinite(te[active]))
+            assert te[active].max() > 300.5
+            assert len(lib.dump(md)["id"]) == n
+            lib.fmd_free(md)
+    finally:
+        del cases.CASES["ttm_slab_full"]
