@@ -211,6 +211,10 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     FMDG_CK(cudaMemset(s->g.thermo, 0, sizeof(fmdg_thermo_t)));
     s->ttm_turi = -1;
     s->fblk = 128;
+    // Verlet skin of the neighbour list (A) of mixed-precision systems;
+    // FMD_SKIN=0 keeps the exact per-step stencil list
+    s->g.skin = 0.5;
+    if (const char *e = getenv("FMD_SKIN")) s->g.skin = atof(e);
     *out = s;
     return FMDG_OK;
 }
@@ -424,13 +428,12 @@ int fmdg_set_steps_left(fmdg_sys_t *s, int steps)
     return FMDG_OK;
 }
 
-// Verlet-skin list for packed stepping (before fmdg_upload): the list radius
-// is the largest cutoff + skin; every periodic box length must exceed twice
-// that radius so one image of a pair at most lies inside it.
-int fmdg_set_skin(fmdg_sys_t *s, double skin)
+// Verlet skin of the neighbour list (before fmdg_upload), any precision.
+extern "C" int fmdg_set_skin(fmdg_sys_t *s, double skin)
 {
     if (!(skin >= 0.0)) return fmdg_set_error("fmdg_set_skin: negative skin");
     s->g.skin = skin;
+    s->skin_set = true;
     return FMDG_OK;
 }
 
@@ -504,8 +507,20 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     const int maxnb = fmdg_list_capacity(s, cell_count, ncell);
     g.maxnb = maxnb;
     for (int d3 = 0; d3 < 3; d3++) g.cellh_f[d3] = (float)g.cellh[d3];
-    g.skin_on = g.skin > 0.0;
-    if (g.skin_on && cap >= (1 << 25)) return fmdg_set_error("fmdg_upload: skin lists hold at most 2^25 atoms");
+    // a skin list needs the list radius below half of every periodic box
+    // length (one image inside it) and within two cells; otherwise the
+    // exact stencil list is rebuilt every step
+    // (default: mixed precision only -- binary64 kernels are bound by the
+    // binary64 pipe and lose more on the longer list than the rebuilds cost)
+    g.skin_on = 0;
+    if (g.skin > 0.0 && cap < (1 << 25) && (s->skin_set || g.prec == FMDG_PREC_MIXED))
+    {
+        const double rsk = sqrt(rc2max) + g.skin;
+        bool ok = rsk <= 2.0 * fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
+        for (int d3 = 0; d3 < 3; d3++)
+            if (g.pbc[d3] && !(g.l[d3] > 2.0 * rsk)) ok = false;
+        g.skin_on = ok;
+    }
     // partials for the smallest block size the tuner may pick (64)
     const int nb = fmdg_grid(cap, 64);
     auto layout = [&](Carver &c) {
@@ -551,8 +566,6 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         g.srad = 1;
         for (int d3 = 0; d3 < 3; d3++)
             if (rsk > g.cellh[d3]) g.srad = 2;
-        if (rsk > 2.0 * fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2])))
-            return fmdg_set_error("fmdg_upload: skin list radius above two cells");
     }
     // host SoA staging
     std::vector<double> hx(3 * (size_t)cap, 0.0), hv(3 * (size_t)cap, 0.0);
@@ -649,6 +662,12 @@ extern "C" int fmdg_set_state(fmdg_sys_t *s, const double *x, const double *v)
     };
     if (x && (rc = put3(x, S.x))) return rc;
     if (v && (rc = put3(v, S.v))) return rc;
+    if (x)
+    {
+        // positions set from outside: the skin list is rebuilt first
+        const int one = 1;
+        FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, rebuild), &one, sizeof one, cudaMemcpyHostToDevice));
+    }
     return FMDG_OK;
 }
 

@@ -614,6 +614,7 @@ void launch_force_t(const L &loc, int cats, int finish, int nb, int blk, cudaStr
 
 int fmdg_launch_nlist(fmdg_sys_t *s)
 {
+    if (s->g.skin_on) return fmdg_skin_launch_nlist(s);
     launch_nlist_t(LocOne{s->g}, fmdg_grid(s->g.cap, 256), 256, fmdg_force_blocks(s), s->fblk, s->stream);
     s->launches += 2;
     FMDG_CK(cudaGetLastError());
@@ -625,6 +626,7 @@ int fmdg_launch_density(fmdg_sys_t *s, int group)
     const bool eam = (s->cats & (1 << FMDG_POT_EAM)) != 0;
     if (!eam) return FMDG_OK;
     s->g.st.group = group;
+    if (s->g.skin_on) return fmdg_skin_launch_density(s);
     launch_density_t(LocOne{s->g}, s->g.prec == FMDG_PREC_MIXED, __builtin_popcount(s->cats) > 1,
                      fmdg_force_blocks(s), s->fblk, s->stream);
     s->launches++;
@@ -642,6 +644,7 @@ int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int
     a.thermostat = thermostat;
     a.tau = tau;
     a.T0 = T0;
+    if (s->g.skin_on) return fmdg_skin_launch_pair_forces(s, finish);
     const LocOne L{s->g};
     const int nb = fmdg_force_blocks(s);
     if (s->g.prec == FMDG_PREC_MIXED) launch_force_t<LocOne, true>(L, s->cats, finish, nb, s->fblk, s->stream);

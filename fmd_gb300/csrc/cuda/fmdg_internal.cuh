@@ -165,6 +165,7 @@ struct fmdg_sys
     int fblk;                     // threads per block of the list/density/force kernels
     bool eam_borrowed;            // EAM tables belong to another system
     char *arena;                  // one device allocation holding the per-atom and per-cell buffers
+    bool skin_set;                // skin chosen by the caller (any precision)
 };
 
 // ---- which system a thread block works on ------------------------------------
@@ -265,7 +266,10 @@ int fmdg_force_blocks(const fmdg_sys_t *s);
 int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell);
 size_t fmdg_bytes_estimate(int n, int ncell, int maxnb);
 int fmdg_set_steps_left(fmdg_sys_t *s, int steps);
-int fmdg_set_skin(fmdg_sys_t *s, double skin);
+// single-system path on a skin list (fmdg_skin.cu)
+int fmdg_skin_launch_nlist(fmdg_sys_t *s);
+int fmdg_skin_launch_density(fmdg_sys_t *s);
+int fmdg_skin_launch_pair_forces(fmdg_sys_t *s, int finish);
 
 // refresh modes
 #define FMDG_REFRESH_ONLY  0     // positions already updated

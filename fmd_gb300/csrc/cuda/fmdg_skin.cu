@@ -173,7 +173,8 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
 // ---------------------------------------------------------------- kernels
 
 // one thread per current atom index
-__global__ void k_prep_skin(__grid_constant__ const LocPack loc)
+template <class L>
+__global__ void k_prep_skin(__grid_constant__ const L loc)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
@@ -215,7 +216,8 @@ __global__ void k_prep_skin(__grid_constant__ const LocPack loc)
 }
 
 // one thread per slot; every block leaves at once when no rebuild is due
-__global__ void __launch_bounds__(256) k_nlist_skin(__grid_constant__ const LocPack loc)
+template <class L>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__grid_constant__ const L loc)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
@@ -267,8 +269,8 @@ __global__ void __launch_bounds__(256) k_nlist_skin(__grid_constant__ const LocP
 
 // EAM pass 1 + embedding (src/eam.h:270-406, src/eam.c:160-179), one
 // thread per slot
-template <bool MIXED>
-__global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const LocPack loc)
+template <class L, bool MIXED, bool HYBRID>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(__grid_constant__ const L loc)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
@@ -288,7 +290,7 @@ __global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const Lo
         float4 xi = g.xl[t];
         const int ki = __float_as_int(xi.w);
         const int ei = sp.elem[ki];
-        const bool active = (group < 0 || g.gslot[t] == group) && ei >= 0;
+        const bool active = (group < 0 || g.gslot[t] == group) && ei >= 0;   // hybrid: EAM kinds only
         const int nk = g.nkinds, nint = g.Nr2 - 1;
         double rho = 0.0;
         if (active)
@@ -301,6 +303,7 @@ __global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const Lo
                     if (group >= 0 && g.gslot[js] != group) return;
                     const double4_32a xj = g.xd[js];
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    if (HYBRID && pp.cat != FMDG_POT_EAM) return;
                     const Geom64 p = geom64_mi(g, xdi, xj);
                     if (p.r2 < pp.p[2])
                     {
@@ -321,7 +324,8 @@ __global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const Lo
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                    if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
+                    if ((!HYBRID || pp.cat == FMDG_POT_EAM) &&
+                        within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
                     {
                         float b;
                         const int ir2 = table_index(r2 * inv_h, kmax, b);
@@ -373,8 +377,8 @@ __global__ void __launch_bounds__(256) k_density_skin(__grid_constant__ const Lo
 // Pair forces + velocity-Verlet finish step (src/integrators.c:94-126) and
 // the thermo record, one thread per slot; the forces are stored in the
 // current order for the next start step.
-template <int CAT, bool MIXED>
-__global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocPack loc)
+template <class L, int CAT, bool MIXED>
+__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__grid_constant__ const L loc, int finish)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
@@ -406,28 +410,29 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
             if (!MIXED)
             {
                 const double4_32a xdi = g.xd[t];
-                const double fpi = (CAT == CAT_EAM) ? g.fpd[t] : 0.0;
+                const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpd[t] : 0.0;
                 const double inv_h = g.inv_dr2;
                 for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4, float4) {
                     if (group >= 0 && g.gslot[js] != group) return;
                     const double4_32a xj = g.xd[js];
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
                     const Geom64 p = geom64_mi(g, xdi, xj);
-                    if (CAT == CAT_LJ && p.r2 < pp.p[2])
+                    if (cat == FMDG_POT_LJ && p.r2 < pp.p[2])
                     {
                         double fa, e;
                         lj_pair(p.r2, pp, fa, e);
                         for (int d = 0; d < 3; d++) f[d] += p.rv[d] * fa;
                         pe += e;
                     }
-                    else if (CAT == CAT_MORSE && p.r2 < pp.p[3])
+                    else if (cat == FMDG_POT_MORSE && p.r2 < pp.p[3])
                     {
                         double fa, e;
                         morse_pair(p.r2, pp, fa, e);
                         for (int d = 0; d < 3; d++) f[d] += fa * p.rv[d];
                         pe += e;
                     }
-                    else if (CAT == CAT_EAM && p.r2 < pp.p[2])
+                    else if (cat == FMDG_POT_EAM && p.r2 < pp.p[2])
                     {
                         const double q = p.r2 * inv_h;
                         const int ir2 = min((int)q, nint - 1);
@@ -446,7 +451,7 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
             }
             else
             {
-                const float fpi = (CAT == CAT_EAM) ? g.fpb[t] : 0.f;
+                const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpb[t] : 0.f;
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
                 Acc32<4> ac;
@@ -454,9 +459,10 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
                     if (group >= 0 && g.gslot[js] != group) return;
                     const int pidx = ki * nk + __float_as_int(xj.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
                     const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                    if (CAT == CAT_LJ)
+                    if (cat == FMDG_POT_LJ)
                     {
                         if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
                         {
@@ -468,7 +474,7 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
                             ac.part[3] += e;
                         }
                     }
-                    else if (CAT == CAT_MORSE)
+                    else if (cat == FMDG_POT_MORSE)
                     {
                         if (within_cut_skin(g, t, js, r2, sp.pf[pidx][3], pp.p[3]))
                         {
@@ -480,7 +486,7 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
                             ac.part[3] += e;
                         }
                     }
-                    else if (CAT == CAT_EAM)
+                    else if (cat == FMDG_POT_EAM)
                     {
                         if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
                         {
@@ -506,17 +512,37 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
                 pe = ac.sum[3];
             }
         }
+        if (active && g.ttm_on)
+        {
+            // TTM friction (src/forces.c:292-330, 1-D): F_z += xi m (v_z - vcm_z)
+            const double time = dyn->time, hdt = dyn->dt / 2.0;
+            if ((time >= g.ttm_start - hdt) && ((time < g.ttm_stop + hdt) || g.ttm_stop < g.ttm_start))
+            {
+                const double z = S.x[2 * (size_t)cap + i];
+                const double q = z * g.ttm_inv_tcellh_z;
+                const double r = rint(q);
+                int it = (fabs(q - r) <= 1e-9 * fmax(1.0, fabs(q))) ? (int)__ddiv_rn(z, g.ttm_tcellh_z) : (int)q;
+                it += g.ttm_g2l_z;
+                if (it >= 0 && it < g.ttm_nz)
+                    f[2] += g.ttm_xi[it] * sp.mass[ki] * (S.v[2 * (size_t)cap + i] - g.ttm_vcm[3 * it + 2]);
+                else
+                    atomic_or_err(dyn, FMDG_ERRBIT_TTM);
+            }
+        }
         for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
         acc[0] = pe;
         if (active)
         {
             const double m = sp.mass[ki];
             double v[3] = {S.v[i], S.v[cap + i], S.v[2 * (size_t)cap + i]};
-            const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
-            for (int d = 0; d < 3; d++)
+            if (finish)
             {
-                v[d] = __dadd_rn(v[d], __dmul_rn(coef, f[d]));
-                S.v[(size_t)d * cap + i] = v[d];
+                const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
+                for (int d = 0; d < 3; d++)
+                {
+                    v[d] = __dadd_rn(v[d], __dmul_rn(coef, f[d]));
+                    S.v[(size_t)d * cap + i] = v[d];
+                }
             }
             acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
             acc[2] = m * v[0];
@@ -542,18 +568,34 @@ __global__ void __launch_bounds__(256) k_force_skin(__grid_constant__ const LocP
         if (threadIdx.x == 0)
         {
             dyn->blocks_done = 0;
-            if (dyn->steps_left > 0) dyn->steps_left--;
+            if (finish && dyn->steps_left > 0) dyn->steps_left--;
         }
     }
 }
 
-template <bool MIXED>
-void launch_force_skin(const fmdg_pack_launch &P, int nfb)
+template <class L, bool MIXED>
+void launch_force_skin(const L &loc, int cats, int finish, int nb, int blk, cudaStream_t st)
 {
-    const LocPack &L = P.lf;
-    if (P.cat == FMDG_POT_LJ) k_force_skin<CAT_LJ, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
-    else if (P.cat == FMDG_POT_MORSE) k_force_skin<CAT_MORSE, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
-    else k_force_skin<CAT_EAM, MIXED><<<nfb, P.fblk, 0, P.stream>>>(L);
+    const int ncat = __builtin_popcount(cats);
+    if (ncat > 1) k_force_skin<L, CAT_HYBRID, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else if (cats == (1 << FMDG_POT_LJ)) k_force_skin<L, CAT_LJ, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else if (cats == (1 << FMDG_POT_MORSE)) k_force_skin<L, CAT_MORSE, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    else k_force_skin<L, CAT_EAM, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+}
+
+template <class L>
+void launch_density_skin(const L &loc, bool mixed, bool hyb, int nb, int blk, cudaStream_t st)
+{
+    if (mixed)
+    {
+        if (hyb) k_density_skin<L, true, true><<<nb, blk, 0, st>>>(loc);
+        else k_density_skin<L, true, false><<<nb, blk, 0, st>>>(loc);
+    }
+    else
+    {
+        if (hyb) k_density_skin<L, false, true><<<nb, blk, 0, st>>>(loc);
+        else k_density_skin<L, false, false><<<nb, blk, 0, st>>>(loc);
+    }
 }
 
 } // namespace
@@ -574,17 +616,49 @@ int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
     }
     if ((phases & 2) && P.cat == FMDG_POT_EAM)
     {
-        if (P.mixed) k_density_skin<true><<<nfb, P.fblk, 0, st>>>(P.lf);
-        else k_density_skin<false><<<nfb, P.fblk, 0, st>>>(P.lf);
+        launch_density_skin(P.lf, P.mixed != 0, false, nfb, P.fblk, st);
         n++;
     }
     if (phases & 4)
     {
-        if (P.mixed) launch_force_skin<true>(P, nfb);
-        else launch_force_skin<false>(P, nfb);
+        if (P.mixed) launch_force_skin<LocPack, true>(P.lf, 1 << P.cat, 1, nfb, P.fblk, st);
+        else launch_force_skin<LocPack, false>(P.lf, 1 << P.cat, 1, nfb, P.fblk, st);
         n++;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return -fmdg_fail("pack forces", e);
     return n;
+}
+
+// The single-system path on a skin list (fmdg_launch_nlist/density/
+// pair_forces dispatch here when the system has one): slot tables + list
+// (re)build; EAM density; pair forces (+ finish step).
+int fmdg_skin_launch_nlist(fmdg_sys_t *s)
+{
+    const LocOne L{s->g};
+    k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L);
+    k_nlist_skin<<<fmdg_force_blocks(s), s->fblk, 0, s->stream>>>(L);
+    s->launches += 2;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
+int fmdg_skin_launch_density(fmdg_sys_t *s)
+{
+    launch_density_skin(LocOne{s->g}, s->g.prec == FMDG_PREC_MIXED, __builtin_popcount(s->cats) > 1,
+                        fmdg_force_blocks(s), s->fblk, s->stream);
+    s->launches++;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
+int fmdg_skin_launch_pair_forces(fmdg_sys_t *s, int finish)
+{
+    const LocOne L{s->g};
+    const int nb = fmdg_force_blocks(s);
+    if (s->g.prec == FMDG_PREC_MIXED) launch_force_skin<LocOne, true>(L, s->cats, finish, nb, s->fblk, s->stream);
+    else launch_force_skin<LocOne, false>(L, s->cats, finish, nb, s->fblk, s->stream);
+    s->launches++;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
 }

@@ -97,6 +97,15 @@ int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int Nr2, doubl
                  const double *F, const double *F_DD, const double *rho, const double *rhoDD,
                  const double *phi, const double *phiDD);
 int fmdg_set_precision(fmdg_sys_t *s, int mode);
+/* Verlet skin (A) of the neighbour list, before fmdg_upload: the list holds
+   the pairs within the largest cutoff + skin, indexed by stable atom slots,
+   and is rebuilt on the device once an atom has moved more than skin/2.
+   Used when every periodic box length exceeds twice the list radius and
+   the radius spans at most two cells; otherwise (and with skin 0) the
+   exact stencil list is rebuilt every step.  Default: 0.5 A for systems in
+   mixed precision at upload (environment FMD_SKIN overrides), none in
+   binary64 unless set here. */
+int fmdg_set_skin(fmdg_sys_t *s, double skin);
 
 /* --- atoms (replaces the distribution of the global grid to the local grid,
        src/matter.c:329-447, and the state gathers of src/misc.c:310-422) -- */
