@@ -223,11 +223,12 @@ __device__ __forceinline__ void morse_pair(double r2, const fmdg_pair_t &pp, dou
     f = 2.0 * pp.p[1] * pp.p[0] * inv_r * (e2 - e1);
     e = 0.5 * (pp.p[0] * (e2 - 2.0 * e1));
 }
+// (binary32: exp(-alpha (r - r0)) as 2^((r0 - r) alpha log2(e)))
 __device__ __forceinline__ void morse_pair(float r2, float D0, float al, float r0, float &f, float &e)
 {
     const float inv_r = rsqrtf(r2);
     const float r = r2 * inv_r;
-    const float e1 = expf(-al * (r - r0));
+    const float e1 = exp2f((r0 - r) * (al * 1.44269504f));
     const float e2 = e1 * e1;
     f = 2.f * al * D0 * inv_r * (e2 - e1);
     e = 0.5f * (D0 * (e2 - 2.f * e1));
