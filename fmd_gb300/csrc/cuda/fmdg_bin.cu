@@ -52,6 +52,11 @@ __global__ void k_bin_classify(__grid_constant__ const L loc, int mode)
     if (loc_idle(loc, g)) return;
     const double dt = g.st.dt;
     const int group = g.st.group, thermostat = g.st.thermostat;
+    // half kick dt * 0.5 / m per kind: one binary64 division per kind, not
+    // per atom (the same operations, so the same bits)
+    __shared__ double hk[FMDG_MAXK];
+    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = __ddiv_rn(__dmul_rn(dt, 0.5), g.mass[threadIdx.x]);
+    __syncthreads();
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const int i = bx * blockDim.x + threadIdx.x;
@@ -64,11 +69,12 @@ __global__ void k_bin_classify(__grid_constant__ const L loc, int mode)
 
     if (mode != FMDG_REFRESH_ONLY && (group < 0 || S.group[i] == group))
     {
-        const double m = g.mass[S.kind[i]];
+        const int k = S.kind[i];
+        const double m = g.mass[k];
         if (mode == FMDG_REFRESH_VV)
         {
             const double lam = dyn->lambda;
-            const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
+            const double coef = hk[k];
             for (int d = 0; d < 3; d++)
             {
                 double vv = v[d];

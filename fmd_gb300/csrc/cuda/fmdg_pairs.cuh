@@ -15,6 +15,7 @@ struct SmemPot
     fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
     float pf[FMDG_MAXK * FMDG_MAXK][4];
     double mass[FMDG_MAXK];
+    double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
     float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
 };
@@ -30,6 +31,7 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
     for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
     {
         sp.mass[k] = g.mass[k];
+        sp.hk[k] = __ddiv_rn(__dmul_rn(g.st.dt, 0.5), g.mass[k]);
         sp.elem[k] = g.eam_elem[k];
     }
     for (int c = threadIdx.x; c < 27; c += blockDim.x)

@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
             double v[3] = {S.v[i], S.v[cap + i], S.v[2 * (size_t)cap + i]};
             if (finish)
             {
-                const double coef = __ddiv_rn(__dmul_rn(dt, 0.5), m);
+                const double coef = sp.hk[ki];   // dt * 0.5 / m, as the reference forms it
                 for (int d = 0; d < 3; d++)
                 {
                     v[d] = __dadd_rn(v[d], __dmul_rn(coef, f[d]));
