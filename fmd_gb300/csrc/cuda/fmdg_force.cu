@@ -25,6 +25,9 @@
 //   k_force       pair forces over the list + velocity-Verlet finish step
 // An atom with more candidates than the list holds falls back to scanning
 // the stencil directly, so the list size is a performance knob only.
+// These kernels serve single systems on the exact per-step list (binary64
+// by default, and boxes too small for a skin list); packed systems and
+// mixed-precision single systems use the skin-list kernels (fmdg_skin.cu).
 //
 // Precision modes.  FMDG_PREC_FP64: every pair quantity in binary64, the
 // binary32 list only prunes (its margin keeps every pair within the cutoff).
@@ -59,10 +62,8 @@ __device__ __forceinline__ void scan_stencil(const Geo &g, const Side &S, int i,
     }
 }
 
-// list walk with stencil fallback; UNROLL: four entries per round, their
-// index and coordinate loads independent and in flight together (the walk
-// is latency bound; pays where registers do not limit occupancy further)
-template <bool UNROLL, typename F>
+// list walk with stencil fallback
+template <typename F>
 __device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i, CellXYZ ci, F &&f)
 {
     const int cnt = g.nbr_count[i];
@@ -70,18 +71,7 @@ __device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i
     {
         const int cap = g.cap;
         const int *col = g.nbr + i;
-        int k = 0;
-        if (UNROLL)
-            for (; k + 4 <= cnt; k += 4)
-            {
-                const int e0 = __ldg(col + (size_t)k * cap), e1 = __ldg(col + (size_t)(k + 1) * cap);
-                const int e2 = __ldg(col + (size_t)(k + 2) * cap), e3 = __ldg(col + (size_t)(k + 3) * cap);
-                f(e0 & 0x3ffffff, e0 >> 26);
-                f(e1 & 0x3ffffff, e1 >> 26);
-                f(e2 & 0x3ffffff, e2 >> 26);
-                f(e3 & 0x3ffffff, e3 >> 26);
-            }
-        for (; k < cnt; k++)
+        for (int k = 0; k < cnt; k++)
         {
             const int e = __ldg(col + (size_t)k * cap);
             f(e & 0x3ffffff, e >> 26);
@@ -241,7 +231,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double inv_h = g.inv_dr2;
-                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
@@ -260,7 +250,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
                 Acc32<1> ac;
-                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const float4 xj = g.xf4[j];
                     const int kj = __float_as_int(xj.w);
@@ -356,7 +346,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
                 const double inv_h = g.inv_dr2;
-                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
@@ -414,7 +404,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
                 Acc32<4> ac;
-                for_each_pair<L::unroll>(g, S, i, ci, [&](int j, int code) {
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const float4 xj = g.xf4[j];
                     const int kj = __float_as_int(xj.w);

@@ -185,7 +185,6 @@ struct LocOne
 {
     static constexpr int max_threads = 128;
     static constexpr int min_blocks = 0;      // 0: register count left to the compiler
-    static constexpr bool unroll = false;
     Geo g;
 };
 
@@ -193,7 +192,6 @@ struct LocPack
 {
     static constexpr int max_threads = 256;
     static constexpr int min_blocks = 0;
-    static constexpr bool unroll = true;      // list walk four entries per round
     int nsys;
     int bstart[FMDG_PACK_MAX + 1];
     Geo geos[FMDG_PACK_MAX];
