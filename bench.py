@@ -61,10 +61,10 @@ FLOP_FORCE = 68.0 * PAIRS_PER_ATOM
 SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0}
 # DRAM bytes (read + write) per atom of one pair-force launch, from ncu
 # captures of the same kernels (dram__bytes_read.sum + dram__bytes_write.sum
-# divided by the atoms of the launch): packed Morse (skin list) on a
-# 149616-atom pack, single-system EAM on the 256000-atom system; the traffic
+# divided by the atoms of the launch): packed Morse on a 149616-atom pack,
+# single-system mixed EAM on the 256000-atom system (both skin lists); the traffic
 # grows with the atoms (the neighbour list dominates it)
-FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 147.06e6 / 149616, "eam_single": 71.63e6 / 256000}
+FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 147.45e6 / 149616, "eam_single": 97.40e6 / 256000}
 
 
 def clocks_sampler(stop, out):
