@@ -1,7 +1,8 @@
 /*
  * CPU restatement of FMD 0.4.0's per-timestep hot path -- TEST
- * INFRASTRUCTURE ONLY.  Used by tests/ as the checker for the GPU engine,
- * by __graft_entry__.smoke(), and by bench.py as the timed CPU baseline.
+ * INFRASTRUCTURE ONLY.  Used by tests/ as the restatement the GPU engine is
+ * compared with, by __graft_entry__.smoke(), and by bench.py as the timed
+ * CPU baseline.
  * Nothing in the product (libfmd.so) links or calls it.
  *
  * It follows the reference's algorithms (file:line in fmd_oracle.c) with the
