@@ -97,13 +97,50 @@ def golden_binning(lib, name, work, rounds=4, seed=99):
     np.savez_compressed(os.path.join(HERE, "bin_" + name + ".npz"), nc=nc, cellh=cellh, rounds=rounds, **recs)
 
 
+IO_MODES = [("xyz", 1), ("csv", 2), ("vtf", 3)]
+
+
+def io_files(lib, md, work, tag):
+    """Files the reference writes for the current state: fmd_io_saveState
+    (src/misc.c:310-422) and fmd_matt_saveConfiguration in every mode
+    (src/matter.c:650-829), read back as bytes."""
+    out = {}
+    lib.fmd_io_setSaveDirectory(md, (work + "/").encode())
+    lib.fmd_io_saveState(md, (tag + ".stt").encode())
+    out[tag + "_state"] = open(os.path.join(work, tag + ".stt"), "rb").read()
+    for name, mode in IO_MODES:
+        before = set(os.listdir(work))
+        lib.fmd_io_setSaveConfigMode(md, mode)
+        lib.fmd_matt_saveConfiguration(md)
+        new = sorted(set(os.listdir(work)) - before)
+        assert len(new) == 1, (name, new)
+        out[tag + "_" + name] = open(os.path.join(work, new[0]), "rb").read()
+        os.remove(os.path.join(work, new[0]))
+    return out
+
+
+def golden_io(lib, name, work):
+    """State and configuration files of case `name` right after distribution
+    and after the case's run."""
+    case = cases.CASES[name]
+    md, st = cases.setup(lib, name, work)
+    lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+    files = io_files(lib, md, work, "s0")
+    cases.run(lib, name, md, None)
+    files.update(io_files(lib, md, work, "s1"))
+    lib.fmd_free(md)
+    np.savez_compressed(os.path.join(HERE, "io_" + name + ".npz"),
+                        **{k: np.frombuffer(v, dtype=np.uint8) for k, v in files.items()})
+    print("io", name, {k: len(v) for k, v in files.items()})
+
+
 def main():
     names = sys.argv[1:] or list(cases.CASES)
     if len(names) > 1 or not sys.argv[1:]:
         # one process per case: the reference's fmd_free reads the instance
         # after freeing it (src/misc.c:650-660), so instances are not reused
         import subprocess
-        for name in names + ([] if sys.argv[1:] else ["bin_lj", "bin_morse_open"]):
+        for name in names + ([] if sys.argv[1:] else ["bin_lj", "bin_morse_open", "io_lj_small", "io_hybrid"]):
             subprocess.run([sys.executable, os.path.abspath(__file__), name], check=True)
         return
     lib = api.Lib(REF_LIB, prefix="oref_")
@@ -111,6 +148,8 @@ def main():
         for name in names:
             if name.startswith("bin_"):
                 golden_binning(lib, name[4:], work)
+            elif name.startswith("io_"):
+                golden_io(lib, name[3:], work)
             else:
                 golden_case(lib, name, work)
 
