@@ -223,13 +223,13 @@ __device__ __forceinline__ const Geo &loc_geo(const LocPack &L, int &bx, int &nb
 __device__ __forceinline__ bool loc_idle(const LocOne &, const Geo &) { return false; }
 __device__ __forceinline__ bool loc_idle(const LocPack &, const Geo &g) { return g.dyn->steps_left <= 0; }
 
-// A pack: systems of one pair category and precision stepped together; one
-// locator per block shape (its grid is bstart[nsys]).
+// A pack: systems of one pair-category class and precision stepped
+// together; one locator per block shape (its grid is bstart[nsys]).
 struct fmdg_pack_launch
 {
     cudaStream_t stream;
     int nsys;
-    int cat;                    // FMDG_POT_* (single category)
+    int cats;                   // bit mask (1 << FMDG_POT_*) of the members' pair categories
     int mixed;
     int fblk;                   // threads per block of the list/density/force kernels
     LocPack la;                 // 128-thread atom blocks

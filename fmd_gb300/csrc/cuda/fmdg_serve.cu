@@ -61,7 +61,7 @@ struct Job
     double dt;
     int prec;
     int keep_state;
-    int cat;
+    int cats;           // bit mask (1 << FMDG_POT_*) of the pair categories
     int nc[3];
     double cellh[3];
     double rcmax;
@@ -92,11 +92,12 @@ struct Chunk
 };
 
 // At most FMDG_PACK_MAX systems (their Geo travel as kernel parameters);
-// more systems of one category and precision form further packs, each on
-// its own stream.
+// more systems of one class and precision form further packs, each on its
+// own stream.  Class: the pair category of single-category jobs
+// (FMDG_POT_LJ, _EAM, _MORSE), 0 for jobs that mix categories (hybrid).
 struct Pack
 {
-    int cat = 0, mixed = 0;
+    int cls = 0, mixed = 0;
     cudaStream_t stream = nullptr;
     std::vector<Job *> members;
     bool dirty = true;
@@ -116,7 +117,7 @@ struct Pack
     }
 };
 
-// block-size autotuner of one category and precision (shared by its packs)
+// block-size autotuner of one class and precision (shared by its packs)
 struct Tuner
 {
     int fblk = 128;
@@ -148,7 +149,7 @@ struct fmdg_server
     std::deque<Job *> queue;
     std::map<long long, Job *> jobs;
     int running = 0;
-    std::vector<Pack *> packs[4][2];  // [category][mixed]
+    std::vector<Pack *> packs[4][2];  // [class][mixed]
     Tuner tuners[4][2];
     std::map<int, fmdg_sys_t *> eam_owner;   // shared EAM tables by key
     std::vector<cudaEvent_t> free_events;
@@ -187,24 +188,26 @@ void each_pack(fmdg_server_t *S, F f)
 int want_fblk(const fmdg_server_t *S, const Pack &p)
 {
     if (S->fixed_fblk) return S->fixed_fblk;
-    const Tuner &t = S->tuners[p.cat][p.mixed];
+    const Tuner &t = S->tuners[p.cls][p.mixed];
     return t.tuned ? t.fblk : TUNE_BLK[t.step % 3];
 }
 
-// a pack of (cat, mixed) with room for one more system
-Pack *pack_for(fmdg_server_t *S, int cat, int mixed)
+int pack_class(int cats) { return __builtin_popcount(cats) > 1 ? 0 : __builtin_ctz(cats); }
+
+// a pack of (class, mixed) with room for one more system
+Pack *pack_for(fmdg_server_t *S, int cls, int mixed)
 {
-    for (Pack *p : S->packs[cat][mixed])
+    for (Pack *p : S->packs[cls][mixed])
         if (p->active() < FMDG_PACK_MAX) return p;
     Pack *p = new Pack();
-    p->cat = cat;
+    p->cls = cls;
     p->mixed = mixed;
     if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
     {
         delete p;
         return nullptr;
     }
-    S->packs[cat][mixed].push_back(p);
+    S->packs[cls][mixed].push_back(p);
     return p;
 }
 
@@ -252,7 +255,7 @@ int setup_job(fmdg_server_t *S, Job *j)
     if ((rc = fmdg_set_skin(s, skin))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
-    if (j->cat == FMDG_POT_EAM)
+    if (j->cats & (1 << FMDG_POT_EAM))
     {
         auto it = S->eam_owner.find(j->eam_key);
         if (it == S->eam_owner.end()) return fmdg_set_error("fmdg_srv: unknown EAM table key");
@@ -325,7 +328,7 @@ int admit(fmdg_server_t *S, double budget_s)
             retire(S, j);
             continue;
         }
-        Pack *p = pack_for(S, j->cat, j->prec == FMDG_PREC_MIXED);
+        Pack *p = pack_for(S, pack_class(j->cats), j->prec == FMDG_PREC_MIXED);
         if (!p)
         {
             fail_job(S, j, fmdg_set_error("fmdg_srv: cannot create a pack stream"), true);
@@ -355,7 +358,8 @@ int rebuild(fmdg_server_t *S, Pack &p)
     fmdg_pack_launch &P = p.P;
     P.stream = p.stream;
     P.nsys = (int)p.members.size();
-    P.cat = p.cat;
+    P.cats = 0;
+    for (const Job *j : p.members) P.cats |= j->cats;
     P.mixed = p.mixed;
     P.fblk = fblk;
     LocPack *locs[4] = {&P.la, &P.lc, &P.lf, &P.ls};
@@ -430,7 +434,7 @@ int launch_chunk(fmdg_server_t *S, Pack &p)
         c.atom_steps += (double)j->n * k;
         if (j->left == 0) p.dirty = true;
     }
-    c.timed = full && !S->tuners[p.cat][p.mixed].tuned && !S->fixed_fblk;
+    c.timed = full && !S->tuners[p.cls][p.mixed].tuned && !S->fixed_fblk;
     p.inflight.push_back(c);
     p.chunks++;
     return FMDG_OK;
@@ -485,7 +489,7 @@ int reap(fmdg_server_t *S, Pack &p, bool block)
         const cudaError_t q = cudaEventQuery(c.ev1);
         if (q == cudaErrorNotReady) break;
         if (q != cudaSuccess) return fmdg_fail("chunk", q);
-        Tuner &t = S->tuners[p.cat][p.mixed];
+        Tuner &t = S->tuners[p.cls][p.mixed];
         if (c.timed && !t.tuned && c.atom_steps > 0)
         {
             // device time per atom-step of this block size; the next chunks
@@ -634,16 +638,31 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
         rc2max = std::max(rc2max, pp.cat == FMDG_POT_MORSE ? pp.p[3] : pp.p[2]);
         j->pairs[k] = pp;
     }
-    if (__builtin_popcount(cats) != 1)
+    j->cats = cats;
+    if (cats & (1 << FMDG_POT_EAM))
     {
-        delete j;
-        return fmdg_set_error("fmdg_srv_submit: packed jobs use one pair category");
-    }
-    j->cat = __builtin_ctz(cats);
-    if (j->cat == FMDG_POT_EAM && !S->eam_owner.count(d->eam_key))
-    {
-        delete j;
-        return fmdg_set_error("fmdg_srv_submit: EAM job with an unknown table key");
+        // EAM pairs read the shared tables of eam_key: both kinds need an
+        // element of those tables, and so do the pair's table indices
+        auto it = S->eam_owner.find(d->eam_key);
+        if (it == S->eam_owner.end())
+        {
+            delete j;
+            return fmdg_set_error("fmdg_srv_submit: EAM job with an unknown table key");
+        }
+        const int ne = it->second->g.nelem;
+        for (int a = 0; a < d->nkinds; a++)
+            for (int b = 0; b < d->nkinds; b++)
+            {
+                const fmdg_pair_t &pp = d->pairs[a * d->nkinds + b];
+                if (pp.cat != FMDG_POT_EAM) continue;
+                const int ea = d->eam_elem ? d->eam_elem[a] : -1, eb = d->eam_elem ? d->eam_elem[b] : -1;
+                if (ea < 0 || ea >= ne || eb < 0 || eb >= ne || pp.iloc < 0 || pp.iloc >= ne || pp.jloc < 0 ||
+                    pp.jloc >= ne)
+                {
+                    delete j;
+                    return fmdg_set_error("fmdg_srv_submit: an EAM pair without elements of the tables");
+                }
+            }
     }
     const double rcmax = sqrt(rc2max);
     j->rcmax = rcmax;
@@ -887,15 +906,15 @@ extern "C" int fmdg_srv_run_resident(fmdg_server_t *S, int k, float *ms)
 // between events on its stream (no graph): ms[0] refresh, ms[1] neighbour
 // lists, ms[2] EAM density, ms[3] pair forces + finish step; *atoms = the
 // pack's atoms, *members = its jobs.
-extern "C" int fmdg_srv_profile_pack(fmdg_server_t *S, int cat, int mixed, float ms[4], double *atoms,
+extern "C" int fmdg_srv_profile_pack(fmdg_server_t *S, int cls, int mixed, float ms[4], double *atoms,
                                      int *members)
 {
     FMDG_CK(cudaSetDevice(S->device));
-    if (cat < 0 || cat > 3 || mixed < 0 || mixed > 1) return fmdg_set_error("fmdg_srv_profile_pack: bad pack");
+    if (cls < 0 || cls > 3 || mixed < 0 || mixed > 1) return fmdg_set_error("fmdg_srv_profile_pack: bad pack");
     *atoms = 0.0;
     *members = 0;
     for (int q = 0; q < 4; q++) ms[q] = 0.f;
-    for (Pack *pp : S->packs[cat][mixed])
+    for (Pack *pp : S->packs[cls][mixed])
     {
         Pack &p = *pp;
         int rc;

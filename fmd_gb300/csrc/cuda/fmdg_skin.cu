@@ -614,15 +614,15 @@ int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
         k_nlist_skin<<<nfb, P.fblk, 0, st>>>(P.lf);
         n += 2;
     }
-    if ((phases & 2) && P.cat == FMDG_POT_EAM)
+    if ((phases & 2) && (P.cats & (1 << FMDG_POT_EAM)))
     {
-        launch_density_skin(P.lf, P.mixed != 0, false, nfb, P.fblk, st);
+        launch_density_skin(P.lf, P.mixed != 0, __builtin_popcount(P.cats) > 1, nfb, P.fblk, st);
         n++;
     }
     if (phases & 4)
     {
-        if (P.mixed) launch_force_skin<LocPack, true>(P.lf, 1 << P.cat, 1, nfb, P.fblk, st);
-        else launch_force_skin<LocPack, false>(P.lf, 1 << P.cat, 1, nfb, P.fblk, st);
+        if (P.mixed) launch_force_skin<LocPack, true>(P.lf, P.cats, 1, nfb, P.fblk, st);
+        else launch_force_skin<LocPack, false>(P.lf, P.cats, 1, nfb, P.fblk, st);
         n++;
     }
     cudaError_t e = cudaGetLastError();

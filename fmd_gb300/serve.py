@@ -127,6 +127,69 @@ POTENTIALS = {
 }
 POT_NAMES = ["lj", "morse", "eam"]
 
+# Jobs that mix pair categories (the reference's hybrid tables,
+# src/potential.h:26-32): a copper block on the analytic EAM beside an argon
+# block on Lennard-Jones, copper-argon pairs Lennard-Jones (the parameters of
+# the hybrid test case).  They form packs of their own (class 0).
+HYBRID = {
+    "cuar": dict(kinds=[("Cu", 63.546, 0), ("Ar", 39.948, -1)], dt=0.001, rc=8.5,
+                 pairs={(0, 0): (FMDG_POT_EAM, (0.0, 0.0, workloads.EAM_RC ** 2, 0.0)),
+                        (1, 1): (FMDG_POT_LJ, (4 * 0.0104, 3.4 ** 2, 8.5 ** 2, 0.0)),
+                        (0, 1): (FMDG_POT_LJ, (4 * 0.0652, 2.87 ** 2, 7.175 ** 2, 0.0))}),
+}
+
+
+def job_table(pot):
+    """Masses (internal units), EAM elements and the kind-pair table of a
+    job type: one kind for the single-potential types, several for HYBRID."""
+    if pot in HYBRID:
+        H = HYBRID[pot]
+        nk = len(H["kinds"])
+        mass = np.array([m / MD_MASS_UNIT for _, m, _ in H["kinds"]])
+        elem = np.array([e for _, _, e in H["kinds"]], np.int32)
+        table = (Pair * (nk * nk))()
+        for (a, b), (cat, p) in H["pairs"].items():
+            for i, j in ((a, b), (b, a)):
+                t = table[i * nk + j]
+                t.cat = cat
+                t.iloc, t.jloc = (int(elem[i]), int(elem[j])) if cat == FMDG_POT_EAM else (0, 0)
+                for q in range(4):
+                    t.p[q] = p[q]
+        return mass, elem, table
+    P = POTENTIALS[pot]
+    mass = np.array([P["mass"] / MD_MASS_UNIT])
+    elem = np.array([0 if P["cat"] == FMDG_POT_EAM else -1], np.int32)
+    table = (Pair * 1)()
+    table[0].cat = P["cat"]
+    for q in range(4):
+        table[0].p[q] = P["p"][q]
+    return mass, elem, table
+
+
+def job_rc(pot):
+    return HYBRID[pot]["rc"] if pot in HYBRID else POTENTIALS[pot]["rc"]
+
+
+def job_dt(pot):
+    return HYBRID[pot]["dt"] if pot in HYBRID else POTENTIALS[pot]["dt"]
+
+
+def hybrid_atoms(job):
+    """A "cuar" job: an n^3-cell copper FCC block (a = 3.615 A) at the
+    origin and an argon FCC block of m^3 cells (m = round(n a / 5.26), its
+    lattice stretched to the copper block's width) 2 A beyond it along x;
+    periodic box (2 n a + 4, n a, n a).  Returns x, v, kind, l[3]."""
+    n = job["ncell"]
+    lc = n * 3.615
+    m = max(1, int(round(lc / 5.26)))
+    aa = lc / m
+    xc, vc = workloads.fcc_state(n, n, n, 3.615, job["T"], 63.546, seed=job["seed"])
+    xa, va = workloads.fcc_state(m, m, m, aa, job["T"], 39.948, seed=job["seed"] + 1, origin=(lc + 2.0, 0.0, 0.0))
+    x = np.concatenate([xc, xa])
+    v = np.concatenate([vc, va])
+    kind = np.concatenate([np.zeros(len(xc), np.uint32), np.ones(len(xa), np.uint32)])
+    return x, v, kind, np.array([2.0 * lc + 4.0, lc, lc])
+
 
 def eam_tables(L):
     """Tables of the analytic EAM as the setfl loader of libfmd builds them
@@ -223,24 +286,20 @@ class Server:
     def set_skin(self, skin):
         check(self.L, self.L.fmdg_srv_set_skin(self.h, skin), "fmdg_srv_set_skin")
 
-    def submit(self, pot, x, v, l, steps, precision=PREC_MIXED, keep_state=False, dt=None):
-        P = POTENTIALS[pot]
+    def submit(self, pot, x, v, l, steps, precision=PREC_MIXED, keep_state=False, dt=None, kind=None):
+        """Queue a job of type `pot` (POTENTIALS or HYBRID); `l` a cube edge
+        or three box lengths; `kind` per atom (default all 0)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)
         n = len(x)
-        kind = np.zeros(n, np.uint32)
-        mass = np.array([P["mass"] / MD_MASS_UNIT])
-        elem = np.array([0 if P["cat"] == FMDG_POT_EAM else -1], np.int32)
-        pair = (Pair * 1)()
-        pair[0].cat = P["cat"]
-        pair[0].iloc = pair[0].jloc = 0
-        for q in range(4):
-            pair[0].p[q] = P["p"][q]
+        kind = np.zeros(n, np.uint32) if kind is None else np.ascontiguousarray(kind, np.uint32)
+        mass, elem, pair = job_table(pot)
+        l3 = np.broadcast_to(np.asarray(l, np.float64), (3,))
         d = JobDesc()
         for q in range(3):
-            d.l[q] = l
+            d.l[q] = l3[q]
             d.pbc[q] = 1
-        d.nkinds = 1
+        d.nkinds = len(mass)
         d.mass = _dp(mass)
         d.eam_elem = elem.ctypes.data_as(C.POINTER(C.c_int))
         d.pairs = pair
@@ -250,7 +309,7 @@ class Server:
         d.v = _dp(v)
         d.kind = kind.ctypes.data_as(C.POINTER(C.c_uint))
         d.steps = int(steps)
-        d.dt = P["dt"] if dt is None else dt
+        d.dt = job_dt(pot) if dt is None else dt
         d.precision = precision
         d.keep_state = 1 if keep_state else 0
         jid = C.c_longlong()
@@ -298,7 +357,8 @@ class Server:
     def profile_pack(self, pot, precision=PREC_MIXED):
         ms = (C.c_float * 4)()
         atoms, members = C.c_double(), C.c_int()
-        check(self.L, self.L.fmdg_srv_profile_pack(self.h, POTENTIALS[pot]["cat"], precision, ms, C.byref(atoms),
+        cls = 0 if pot in HYBRID else POTENTIALS[pot]["cat"]
+        check(self.L, self.L.fmdg_srv_profile_pack(self.h, cls, precision, ms, C.byref(atoms),
                                                    C.byref(members)), "fmdg_srv_profile_pack")
         return list(ms), atoms.value, members.value
 
@@ -307,16 +367,24 @@ class Server:
             pass
 
 
-def host_binning(x, l, rc):
-    """Cell grid and upload order the served mode uses: nc = (int)(l/rc),
-    cellh = l/nc (src/misc.c:41-50), atoms in input order inside a cell."""
-    nc = max(1, int(l / rc))
+def host_binning3(x, l, rc):
+    """Cell grid and upload order the served mode uses, per axis:
+    nc = (int)(l/rc), cellh = l/nc (src/misc.c:41-50), atoms in input order
+    inside a cell.  Returns nc[3], cellh[3], order, counts."""
+    l = np.broadcast_to(np.asarray(l, np.float64), (3,))
+    nc = np.maximum(1, (l / rc).astype(np.int64))
     cellh = l / nc
     ic = np.floor(x / cellh).astype(np.int64)
-    flat = ic[:, 2] + nc * (ic[:, 1] + nc * ic[:, 0])
+    flat = ic[:, 2] + nc[2] * (ic[:, 1] + nc[1] * ic[:, 0])
     order = np.argsort(flat, kind="stable")
-    counts = np.bincount(flat, minlength=nc ** 3).astype(np.int32)
+    counts = np.bincount(flat, minlength=int(nc.prod())).astype(np.int32)
     return nc, cellh, order, counts
+
+
+def host_binning(x, l, rc):
+    """host_binning3 of a cube of edge l: (nc, cellh) as scalars."""
+    nc, cellh, order, counts = host_binning3(x, l, rc)
+    return int(nc[0]), float(cellh[0]), order, counts
 
 
 class Single:
@@ -324,27 +392,22 @@ class Single:
     path libfmd.so's fmd_dync_integrate drives): its own system, steps
     replayed from one captured graph, no packing."""
 
-    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0):
-        P = POTENTIALS[pot]
+    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0, kind=None):
         self.L = L
         h = C.c_void_p()
         check(L, L.fmdg_create(C.byref(h), device), "fmdg_create")
         self.h = h
-        nc, cellh, order, counts = host_binning(x, l, P["rc"])
-        lv = (C.c_double * 3)(l, l, l)
+        nc, cellh, order, counts = host_binning3(x, l, job_rc(pot))
+        l3 = np.broadcast_to(np.asarray(l, np.float64), (3,))
+        lv = (C.c_double * 3)(*l3)
         pbc = (C.c_int * 3)(1, 1, 1)
-        ncv = (C.c_int * 3)(nc, nc, nc)
-        ch = (C.c_double * 3)(cellh, cellh, cellh)
+        ncv = (C.c_int * 3)(*[int(c) for c in nc])
+        ch = (C.c_double * 3)(*cellh)
         check(L, L.fmdg_set_box(h, lv, pbc, ncv, ch), "set_box")
-        mass = (C.c_double * 1)(P["mass"] / MD_MASS_UNIT)
-        elem = (C.c_int * 1)(0 if P["cat"] == FMDG_POT_EAM else -1)
-        check(L, L.fmdg_set_kinds(h, 1, mass, elem), "set_kinds")
-        pair = (Pair * 1)()
-        pair[0].cat = P["cat"]
-        for q in range(4):
-            pair[0].p[q] = P["p"][q]
+        mass, elem, pair = job_table(pot)
+        check(L, L.fmdg_set_kinds(h, len(mass), _dp(mass), elem.ctypes.data_as(C.POINTER(C.c_int))), "set_kinds")
         check(L, L.fmdg_set_pairs(h, pair), "set_pairs")
-        if P["cat"] == FMDG_POT_EAM:
+        if (elem >= 0).any():
             t = eam
             check(L, L.fmdg_set_eam(h, t["nelem"], t["Nrho"], t["drho"], t["Nr2"], t["dr2"], _dp(t["F"]),
                                     _dp(t["F_DD"]), _dp(t["rho"]), _dp(t["rhoDD"]), _dp(t["phi"]),
@@ -353,7 +416,8 @@ class Single:
         n = len(x)
         xs = np.ascontiguousarray(x[order])
         vs = np.ascontiguousarray(v[order])
-        kind = np.zeros(n, np.uint32)
+        kind = (np.zeros(n, np.uint32) if kind is None else np.asarray(kind, np.uint32))[order]
+        kind = np.ascontiguousarray(kind)
         group = np.zeros(n, np.int32)
         ids = order.astype(np.uint32)
         check(L, L.fmdg_upload(h, n, counts.ctypes.data_as(C.POINTER(C.c_int)), _dp(xs), _dp(vs),
@@ -363,7 +427,7 @@ class Single:
         self.th0 = Thermo()
         check(L, L.fmdg_thermo(h, -1, C.byref(self.th0)), "thermo")
         self.n = n
-        self.dt = P["dt"]
+        self.dt = job_dt(pot)
 
     def steps(self, k, dt=None):
         check(self.L, self.L.fmdg_vv_steps(self.h, k, self.dt if dt is None else dt, -1, 0, 1.0, 0.0), "vv_steps")

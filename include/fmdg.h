@@ -247,13 +247,15 @@ int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner);
 /* --- served mode: continuous batching of independent jobs --------------
    No counterpart in the reference, which runs one simulation per process
    (one fmd_t, src/integrators.c:227-264).  Jobs wait in a FIFO queue until
-   the device bytes they need fit the HBM budget; admitted jobs of one pair
-   category and precision are stepped together by one launch per kernel
+   the device bytes they need fit the HBM budget; admitted jobs of one pack
+   class and precision are stepped together by one launch per kernel
    (velocity Verlet, NVE), chunk_steps steps per captured CUDA graph; the
    threads per block of the list/density/force kernels are autotuned per
    pack unless fixed with fmdg_srv_set_tuning.  A job's arithmetic does not
    depend on the other jobs: alone or in any mix its trajectory is the same
-   bit for bit. */
+   bit for bit.  Pack class: the pair category (FMDG_POT_LJ, _EAM, _MORSE)
+   of a job whose kind pairs all use one, 0 for a job that mixes categories
+   (src/potential.h:26-32 hybrid tables, e.g. EAM metal + LJ gas). */
 typedef struct fmdg_server fmdg_server_t;
 
 typedef struct
@@ -263,8 +265,8 @@ typedef struct
     int nkinds;               /* 1..8 */
     const double *mass;       /* [nkinds], internal units (src/potential.c:47) */
     const int *eam_elem;      /* [nkinds] element in the EAM tables, or NULL */
-    const fmdg_pair_t *pairs; /* [nkinds*nkinds], one category for all pairs */
-    int eam_key;              /* EAM jobs: tables registered with fmdg_srv_set_eam */
+    const fmdg_pair_t *pairs; /* [nkinds*nkinds] */
+    int eam_key;              /* jobs with EAM pairs: tables registered with fmdg_srv_set_eam */
     int n;                    /* atoms */
     const double *x, *v;      /* n*3 interleaved, positions inside [0, l) */
     const unsigned *kind;     /* [n] */
@@ -293,7 +295,7 @@ typedef struct
     double atom_steps;                  /* completed atom-steps */
     long long kernels;                  /* kernels launched (graph replays included) */
     double bytes_in_use, bytes_peak;    /* admission accounting */
-    int pack_fblk[4][2];                /* tuned threads per block [category][mixed], 0 = not yet */
+    int pack_fblk[4][2];                /* tuned threads per block [class][mixed], 0 = not yet */
     long long pack_chunks[4][2], pack_rebuilds[4][2];
 } fmdg_srv_stats_t;
 
@@ -330,7 +332,7 @@ int  fmdg_srv_stats(fmdg_server_t *srv, fmdg_srv_stats_t *out);
    ms[1] neighbour lists, ms[2] EAM density, ms[3] forces + finish step) */
 int  fmdg_srv_admit(fmdg_server_t *srv);
 int  fmdg_srv_run_resident(fmdg_server_t *srv, int k, float *ms);
-int  fmdg_srv_profile_pack(fmdg_server_t *srv, int category, int mixed, float ms[4], double *atoms,
+int  fmdg_srv_profile_pack(fmdg_server_t *srv, int pack_class, int mixed, float ms[4], double *atoms,
                            int *members);
 
 #ifdef __cplusplus

@@ -46,6 +46,28 @@ def test_job_atoms_inside_box():
         assert np.abs((v * m).sum(axis=0)).max() < 1e-9 * np.abs(v * m).sum()
 
 
+def test_hybrid_job_geometry_and_table():
+    """A "cuar" job: both blocks inside the periodic box, no two atoms
+    closer than 3.5 A across the interfaces or the periodic faces, every
+    periodic length above twice the largest cutoff, and a symmetric
+    two-kind pair table with EAM only between copper atoms."""
+    for n in (5, 6, 9):
+        x, v, kind, l = serve.hybrid_atoms(dict(ncell=n, T=300.0, seed=3))
+        assert x.min() >= 0.0 and np.all(x.max(axis=0) < l)
+        assert np.all(l > 2 * serve.job_rc("cuar"))
+        assert (kind == 0).sum() == 4 * n ** 3
+        cu, ar = x[kind == 0], x[kind == 1]
+        d = cu[:, None, :] - ar[None, :, :]
+        d -= l * np.round(d / l)
+        assert np.sqrt((d * d).sum(-1)).min() > 3.5
+    mass, elem, table = serve.job_table("cuar")
+    assert list(elem) == [0, -1]
+    cats = [[table[a * 2 + b].cat for b in range(2)] for a in range(2)]
+    assert cats == [[serve.FMDG_POT_EAM, serve.FMDG_POT_LJ], [serve.FMDG_POT_LJ, serve.FMDG_POT_LJ]]
+    assert list(table[1].p) == list(table[2].p)
+    assert abs(table[0].p[2] - workloads.EAM_RC ** 2) < 1e-12
+
+
 def test_host_binning_order():
     j = dict(pot="morse", ncell=5, T=300.0, seed=3)
     x, v, l = serve.job_atoms(j)

@@ -9,6 +9,9 @@
   after 25 steps; mixed within 1e-6 A and 5e-5;
 * pack vs the binary64 oracle at the pack's own final positions: forces
   within 1e-10 (binary64) and 1e-5 (mixed) of max |F|.
+
+Hybrid jobs ("cuar": EAM copper beside Lennard-Jones argon, copper-argon
+pairs Lennard-Jones) go through the same checks in packs of their own.
 """
 import os
 import sys
@@ -41,6 +44,23 @@ def _job(pot, n, T, seed):
     return x, v, l
 
 
+def _sys(pot, n, T, seed):
+    """x, v, l (edge or three lengths), kind (None: all 0)"""
+    j = dict(pot=pot, ncell=n, T=T, seed=seed)
+    if pot in serve.HYBRID:
+        x, v, kind, l = serve.hybrid_atoms(j)
+        return x, v, l, kind
+    x, v, l = serve.job_atoms(j)
+    return x, v, l, None
+
+
+ORACLE_POTS = {"lj": ([("Ar", 39.948)], [("lj", 0, 0, 3.405, 0.0104, 8.5125)]),
+               "morse": ([("Cu", 63.546)], [("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)]),
+               "eam": ([("Cu", 63.546)], [("eam", 0, 0)]),
+               "cuar": ([("Cu", 63.546), ("Ar", 39.948)],
+                        [("eam", 0, 0), ("lj", 1, 1, 3.4, 0.0104, 8.5), ("lj", 0, 1, 2.87, 0.0652, 7.175)])}
+
+
 def _thermo_close(a, b):
     for f in ("kinetic", "potential"):
         x, y = getattr(a, f), getattr(b, f)
@@ -53,19 +73,19 @@ def _by_id(state):
     return x[o], v[o], F[o]
 
 
-@pytest.mark.parametrize("pot", ["lj", "morse", "eam"])
+@pytest.mark.parametrize("pot", ["lj", "morse", "eam", "cuar"])
 @pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
 def test_pack_matches_single(L, eam, pot, precision):
-    x, v, l = _job(pot, 6, 700.0, 11)
+    x, v, l, kind = _sys(pot, 6, 700.0, 11)
     steps = 25
-    one = serve.Single(L, pot, x, v, l, precision=precision, eam=eam)
+    one = serve.Single(L, pot, x, v, l, precision=precision, eam=eam, kind=kind)
     one.steps(steps)
     xs, vs, Fs = _by_id(one.state())
     ts = one.thermo()
     one.close()
     srv = serve.Server(L, chunk_steps=8, eam=eam)
     srv.set_tuning(128)
-    jid = srv.submit(pot, x, v, l, steps, precision=precision, keep_state=True)
+    jid = srv.submit(pot, x, v, l, steps, precision=precision, keep_state=True, kind=kind)
     srv.drain()
     r = srv.result(jid)
     assert r.state == 2 and r.errbits == 0
@@ -78,7 +98,7 @@ def test_pack_matches_single(L, eam, pot, precision):
     assert abs(e_s - e_p) <= (1e-10 if precision == serve.PREC_FP64 else 1e-6) * abs(e_s)
 
 
-@pytest.mark.parametrize("pot,ncell", [("lj", 6), ("lj", 5), ("morse", 6), ("morse", 5), ("eam", 6)])
+@pytest.mark.parametrize("pot,ncell", [("lj", 6), ("lj", 5), ("morse", 6), ("morse", 5), ("eam", 6), ("cuar", 6)])
 @pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
 def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
     """Forces of the packed skin-list kernels after 40 steps of a 1200 K
@@ -87,25 +107,25 @@ def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
     two-cell stencil over three cells per axis); Morse 5^3: two cells per
     axis (a cell is its own upper and lower neighbour)."""
     import pyoracle
-    x, v, l = _job(pot, ncell, 1200.0, 71)
+    x, v, l, kind = _sys(pot, ncell, 1200.0, 71)
     srv = serve.Server(L, chunk_steps=8, eam=eam)
     srv.set_skin(0.3)
-    jid = srv.submit(pot, x, v, l, 40, precision=precision, keep_state=True)
+    jid = srv.submit(pot, x, v, l, 40, precision=precision, keep_state=True, kind=kind)
     srv.drain()
     assert srv.result(jid).state == 2
     xp, vp, Fp, ids = srv.state(jid, len(x))
     srv.close()
-    P = serve.POTENTIALS[pot]
-    nc, cellh, order, counts = serve.host_binning(xp, l, P["rc"])
-    pots = {"lj": [("lj", 0, 0, 3.405, 0.0104, 8.5125)], "morse": [("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)],
-            "eam": [("eam", 0, 0)]}[pot]
+    nc, cellh, order, counts = serve.host_binning3(xp, l, serve.job_rc(pot))
+    kinds, pots = ORACLE_POTS[pot]
     with tempfile.TemporaryDirectory() as work:
         setfl = workloads.write_analytic_eam(os.path.join(work, "a.eam.alloy"))
         o = pyoracle.Oracle()
-        o.setup([l] * 3, [1, 1, 1], [nc] * 3, [cellh] * 3, [("Cu", P["mass"])], pots, setfl)
+        o.setup(np.broadcast_to(l, (3,)), [1, 1, 1], nc, cellh, kinds, pots, setfl)
     n = len(xp)
-    o.upload(np.repeat(np.arange(nc ** 3, dtype=np.int32), counts), xp[order], vp[order], np.zeros(n, np.uint32),
-             np.zeros(n, np.int32), ids[order], nc ** 3)
+    kp = np.zeros(n, np.uint32) if kind is None else kind[ids]
+    ncell_all = int(np.prod(nc))
+    o.upload(np.repeat(np.arange(ncell_all, dtype=np.int32), counts), xp[order], vp[order], kp[order],
+             np.zeros(n, np.int32), ids[order], ncell_all)
     o.forces(-1)
     d = o.dump()
     o.close()
@@ -119,22 +139,24 @@ def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
 
 
 def test_alone_vs_mix(L, eam):
-    """Each job alone and in a mix of 9 jobs of three potentials and both
-    precisions, uneven sizes and step counts, chunk boundaries falling
+    """Each job alone and in a mix of 12 jobs of three potentials, hybrid
+    jobs and both precisions, uneven sizes and step counts, chunk boundaries falling
     inside jobs, the autotuner switching block sizes between chunks."""
     specs = [("eam", 6, 900.0, 21, 37, 1), ("lj", 5, 80.0, 22, 50, 1), ("morse", 5, 500.0, 23, 19, 1),
              ("eam", 9, 300.0, 24, 44, 1), ("lj", 7, 120.0, 25, 9, 0), ("morse", 7, 1100.0, 26, 31, 0),
-             ("eam", 5, 1200.0, 27, 23, 0), ("lj", 6, 60.0, 28, 40, 1), ("morse", 6, 250.0, 29, 28, 1)]
-    jobs = [(_job(p, n, T, s), st, pr, p) for (p, n, T, s, st, pr) in specs]
+             ("eam", 5, 1200.0, 27, 23, 0), ("lj", 6, 60.0, 28, 40, 1), ("morse", 6, 250.0, 29, 28, 1),
+             ("cuar", 6, 400.0, 30, 26, 1), ("cuar", 5, 800.0, 31, 33, 0), ("cuar", 7, 200.0, 32, 17, 1)]
+    jobs = [(_sys(p, n, T, s), st, pr, p) for (p, n, T, s, st, pr) in specs]
     alone = []
-    for (x, v, l), st, pr, p in jobs:
+    for (x, v, l, kind), st, pr, p in jobs:
         srv = serve.Server(L, chunk_steps=8, eam=eam)
-        jid = srv.submit(p, x, v, l, st, precision=pr, keep_state=True)
+        jid = srv.submit(p, x, v, l, st, precision=pr, keep_state=True, kind=kind)
         srv.drain()
         alone.append((srv.result(jid), srv.state(jid, len(x))))
         srv.close()
     srv = serve.Server(L, chunk_steps=8, eam=eam)
-    ids = [srv.submit(p, x, v, l, st, precision=pr, keep_state=True) for (x, v, l), st, pr, p in jobs]
+    ids = [srv.submit(p, x, v, l, st, precision=pr, keep_state=True, kind=kind)
+           for (x, v, l, kind), st, pr, p in jobs]
     srv.drain()
     st = srv.stats()
     assert st.finished == len(jobs) and st.failed == 0
@@ -189,13 +211,13 @@ def test_oversize_job_fails_cleanly(L, eam):
     srv.close()
 
 
-@pytest.mark.parametrize("pot", ["lj", "morse", "eam"])
+@pytest.mark.parametrize("pot", ["lj", "morse", "eam", "cuar"])
 def test_mixed_force_error_bound(L, eam, pot):
     """Mixed precision against binary64 at identical positions of a
     thermalised cube (1200 K, 20 binary64 steps): max |F32 - F64| <= 1e-5
     max |F64|."""
-    x, v, l = _job(pot, 7, 1200.0, 61)
-    one = serve.Single(L, pot, x, v, l, precision=serve.PREC_FP64, eam=eam)
+    x, v, l, kind = _sys(pot, 7, 1200.0, 61)
+    one = serve.Single(L, pot, x, v, l, precision=serve.PREC_FP64, eam=eam, kind=kind)
     one.steps(20)
     serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
     F64 = one.state()[2]
