@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     ac.tick();
                 });
                 ac.flush();
-                rho = ac.sum[0];
+                rho = ac.total(0);
             }
             // embedding (src/eam.c:160-179)
             const double qr = rho * g.inv_drho;
@@ -467,8 +467,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     ac.tick();
                 });
                 ac.flush();
-                for (int d = 0; d < 3; d++) f[d] = ac.sum[d];
-                pe = ac.sum[3];
+                for (int d = 0; d < 3; d++) f[d] = ac.total(d);
+                pe = ac.total(3);
             }
         }
         if (active && g.ttm_on)

@@ -108,16 +108,58 @@ __device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
     return ((3.f * t.w * b + 2.f * t.z) * b + t.y) * inv_h;
 }
 
+// Sum over the 32 lanes of a warp of v[0..NV), NV <= 8, by a transposing
+// butterfly: each exchange halves the values a lane carries (v padded to 8),
+// 4 + 2 + 1 + 1 + 1 additions per lane instead of 5 NV.  Value k ends in
+// every lane whose bits 4, 3, 2 spell k (bit 4 the most significant);
+// returns the value of this lane's index.  Fixed order: deterministic.
+template <int NV>
+__device__ __forceinline__ double warp_sum_transposed(const double (&v)[NV], int lane)
+{
+    static_assert(NV >= 1 && NV <= 8, "at most 8 values");
+    double a[8];
+    for (int k = 0; k < 8; k++) a[k] = (k < NV) ? v[k] : 0.0;
+    const bool up4 = (lane & 16) != 0;
+    double b[4];
+    for (int q = 0; q < 4; q++)
+    {
+        const double keep = up4 ? a[q + 4] : a[q], give = up4 ? a[q] : a[q + 4];
+        b[q] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+    }
+    const bool up3 = (lane & 8) != 0;
+    double c[2];
+    for (int q = 0; q < 2; q++)
+    {
+        const double keep = up3 ? b[q + 2] : b[q], give = up3 ? b[q] : b[q + 2];
+        c[q] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+    }
+    const bool up2 = (lane & 4) != 0;
+    const double keep = up2 ? c[1] : c[0], give = up2 ? c[0] : c[1];
+    double d = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+    d += __shfl_xor_sync(0xffffffffu, d, 2);
+    d += __shfl_xor_sync(0xffffffffu, d, 1);
+    return d;
+}
+
 // Deterministic block reduction of NV doubles; thread 0 writes out[0..NV).
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
 {
     __shared__ double red[32][NV];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k = 0; k < NV; k++)
-        for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
-    if (lane == 0)
-        for (int k = 0; k < NV; k++) red[w][k] = v[k];
+    if (NV >= 3)
+    {
+        const double s = warp_sum_transposed<NV>(v, lane);
+        const int k = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+        if ((lane & 3) == 0 && k < NV) red[w][k] = s;
+    }
+    else
+    {
+        for (int k = 0; k < NV; k++)
+            for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+        if (lane == 0)
+            for (int k = 0; k < NV; k++) red[w][k] = v[k];
+    }
     __syncthreads();
     if (threadIdx.x == 0)
     {
@@ -131,17 +173,22 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
     }
 }
 
-// binary32 partial sums flushed into binary64 every 8 ticks (one tick per
-// list entry visited, so the lanes of a warp flush together)
+// binary32 partial sums of at most 8 terms (one tick per list entry
+// visited, so the lanes of a warp flush together), accumulated into the
+// unevaluated sum hi + lo of two binary32 numbers by Knuth's TwoSum: the
+// running sum carries about 48 significant bits, as good as a binary64
+// accumulation of the same partials for these sums, with no binary64
+// instruction in the pair loop (binary64 issues at 1/64 of the binary32
+// rate on GB300).  total() = hi + lo in binary64.
 template <int NV>
 struct Acc32
 {
     float part[NV];
-    double sum[NV];
+    float hi[NV], lo[NV];
     int n;
     __device__ __forceinline__ Acc32() : n(0)
     {
-        for (int k = 0; k < NV; k++) { part[k] = 0.f; sum[k] = 0.0; }
+        for (int k = 0; k < NV; k++) { part[k] = 0.f; hi[k] = 0.f; lo[k] = 0.f; }
     }
     __device__ __forceinline__ void tick()
     {
@@ -149,9 +196,18 @@ struct Acc32
     }
     __device__ __forceinline__ void flush()
     {
-        for (int k = 0; k < NV; k++) { sum[k] += (double)part[k]; part[k] = 0.f; }
+        for (int k = 0; k < NV; k++)
+        {
+            const float s = __fadd_rn(hi[k], part[k]);
+            const float bp = __fsub_rn(s, hi[k]);
+            const float err = __fadd_rn(__fsub_rn(hi[k], __fsub_rn(s, bp)), __fsub_rn(part[k], bp));
+            lo[k] = __fadd_rn(lo[k], err);
+            hi[k] = s;
+            part[k] = 0.f;
+        }
         n = 0;
     }
+    __device__ __forceinline__ double total(int k) const { return (double)hi[k] + (double)lo[k]; }
 };
 
 // Second level: sums the per-block partials in a fixed order, writes the

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                     ac.tick();
                 });
                 ac.flush();
-                rho = ac.sum[0];
+                rho = ac.total(0);
             }
             const double qr = rho * g.inv_drho;
             int irho = (int)qr;
@@ -508,8 +508,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                     ac.tick();
                 });
                 ac.flush();
-                for (int d = 0; d < 3; d++) f[d] = ac.sum[d];
-                pe = ac.sum[3];
+                for (int d = 0; d < 3; d++) f[d] = ac.total(d);
+                pe = ac.total(3);
             }
         }
         if (active && g.ttm_on)
