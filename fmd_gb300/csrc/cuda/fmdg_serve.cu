@@ -143,7 +143,7 @@ struct fmdg_server
     size_t budget, used = 0, peak = 0;
     int max_jobs, chunk;
     int fixed_fblk = 0;               // 0: autotune
-    double skin = 0.5;                // Verlet skin of the packed neighbour lists (A)
+    double skin = 0.8;                // Verlet skin of the packed neighbour lists (A)
     double t0;
     long long next_id = 1, seq = 0;
     std::deque<Job *> queue;
@@ -244,14 +244,13 @@ int setup_job(fmdg_server_t *S, Job *j)
     if (rc) return rc;
     fmdg_sys_t *s = j->sys;
     if ((rc = fmdg_set_box(s, j->l, j->pbc, j->nc, j->cellh))) return rc;
-    // list radius rc + skin below half of every periodic box length; when
-    // the cells leave room for a skin of 0.25 A or more, the skin stays
-    // inside one cell so a rebuild scans 27 cells, not 125
-    double skin = S->skin;
+    // list radius rc + skin below half of every periodic box length and
+    // within two cells (skin <= rc: every cell is at least rc wide); a
+    // radius above the cell width scans the 125-cell stencil, pruned to the
+    // cells within the radius
+    double skin = std::min(S->skin, 0.99 * j->rcmax);
     for (int d = 0; d < 3; d++)
         if (j->pbc[d]) skin = std::min(skin, 0.9 * (0.5 * j->l[d] - j->rcmax));
-    const double room = std::min(j->cellh[0], std::min(j->cellh[1], j->cellh[2])) - j->rcmax;
-    if (room >= 0.25 && room < skin) skin = 0.999 * room;
     if ((rc = fmdg_set_skin(s, skin))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
@@ -278,6 +277,8 @@ int setup_job(fmdg_server_t *S, Job *j)
     }
     if ((rc = fmdg_upload(s, j->n, j->cell_count.data(), hx.data(), hv.data(), hk.data(), hg.data(), hid.data())))
         return rc;
+    // the packed kernels walk skin lists only
+    if (!s->g.skin_on) return fmdg_set_error("fmdg_srv: the job's box admits no skin list");
     if ((rc = fmdg_compute_forces(s, -1))) return rc;
     if ((rc = fmdg_thermo(s, -1, &j->th0))) return rc;
     if ((rc = fmdg_set_steps_left(s, j->steps))) return rc;

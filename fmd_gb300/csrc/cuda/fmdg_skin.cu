@@ -89,17 +89,29 @@ __device__ __forceinline__ bool within_cut_skin(const Geo &g, int ta, int tb, fl
     return geom64_mi(g, g.xd[ta], g.xd[tb]).r2 < rc2;
 }
 
+// Gap along one axis between a point at u inside its cell [0, h) and the
+// cell at offset o (0 for the cell itself).
+__device__ __forceinline__ float axis_gap(int o, float u, float h)
+{
+    return o > 0 ? fmaxf(0.f, (float)o * h - u) : (o < 0 ? fmaxf(0.f, u + (float)(-o - 1) * h) : 0.f);
+}
+
 // Every (j, code) of the stencil of radius R around i's current cell, j
 // the current index, in a fixed order; on a periodic axis shorter than the
 // stencil a cell recurs with another image (at most one image of a pair
-// lies within the list radius).
+// lies within the list radius).  xi: i's binary32 position relative to its
+// current cell; a cell whose box lies farther than the list radius from xi
+// (plus 1e-4 relative) holds no candidate and is skipped.
 template <typename F>
-__device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, int i, F &&f)
+__device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, int i, float4 xi, F &&f)
 {
     const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
     const int R = g.srad, W = 2 * R + 1;
+    const float lim2 = g.rskin2 * 1.0001f;
     for (int ox = -R; ox <= R; ox++)
     {
+        const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
+        if (gx * gx > lim2) continue;
         int cx = ci.x + ox;
         if (cx < 0 || cx >= g.nc[0])
         {
@@ -108,6 +120,8 @@ __device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, 
         }
         for (int oy = -R; oy <= R; oy++)
         {
+            const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
+            if (gx * gx + gy * gy > lim2) continue;
             int cy = ci.y + oy;
             if (cy < 0 || cy >= g.nc[1])
             {
@@ -116,6 +130,8 @@ __device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, 
             }
             for (int oz = -R; oz <= R; oz++)
             {
+                const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
+                if (gx * gx + gy * gy + gz * gz > lim2) continue;
                 int cz = ci.z + oz;
                 if (cz < 0 || cz >= g.nc[2])
                 {
@@ -166,7 +182,7 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
     else
     {
         xi = g.xf4[i];
-        for_each_candidate(g, S, i, [&](int j, int code) { f(S.slot[j], g.xf4[j], so.off[code]); });
+        for_each_candidate(g, S, i, xi, [&](int j, int code) { f(S.slot[j], g.xf4[j], so.off[code]); });
     }
 }
 
@@ -237,7 +253,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
             const Side S = g.side[dyn->cur];
             const float4 xi = g.xf4[i];
             const float rl2 = g.rskin2;
-            for_each_candidate(g, S, i, [&](int j, int code) {
+            for_each_candidate(g, S, i, xi, [&](int j, int code) {
                 const float3 d = rv_of(xi, __ldg(g.xf4 + j), so.off[code]);
                 if (d.x * d.x + d.y * d.y + d.z * d.z < rl2)
                 {

@@ -307,11 +307,11 @@ int  fmdg_srv_set_eam(fmdg_server_t *srv, int key, int nelem, int Nrho, double d
                       const double *phi, const double *phiDD);
 /* 0: autotune (default); 64, 128 or 256: fixed threads per block */
 int  fmdg_srv_set_tuning(fmdg_server_t *srv, int fblk);
-/* Verlet skin of the packed neighbour lists (default 0.5 A): a job's list
+/* Verlet skin of the packed neighbour lists (default 0.8 A): a job's list
    holds the pairs within its largest cutoff + skin and is rebuilt once an
    atom has moved more than skin/2 since the last build; the skin is capped
-   below half of every periodic box length minus the cutoff.  Jobs need
-   periodic box lengths above twice the cutoff. */
+   at 0.99 of the cutoff and below half of every periodic box length minus
+   the cutoff.  Jobs need periodic box lengths above twice the cutoff. */
 int  fmdg_srv_set_skin(fmdg_server_t *srv, double skin);
 /* queue a job (the description is copied) */
 int  fmdg_srv_submit(fmdg_server_t *srv, const fmdg_job_desc_t *job, long long *id);
