@@ -231,6 +231,7 @@ struct fmdg_pack_launch
     int nsys;
     int cats;                   // bit mask (1 << FMDG_POT_*) of the members' pair categories
     int mixed;
+    int lean;                   // every member has one kind (lean binary32 kernels)
     int fblk;                   // threads per block of the list/density/force kernels
     LocPack la;                 // 128-thread atom blocks
     LocPack lc;                 // 128-thread cell blocks

@@ -194,6 +194,13 @@ struct Acc32
     {
         if (++n == 8) flush();
     }
+    // k entries visited at once (rounds of four: the same flush points as
+    // k single ticks)
+    __device__ __forceinline__ void entries(int k)
+    {
+        n += k;
+        if (n >= 8) flush();
+    }
     __device__ __forceinline__ void flush()
     {
         for (int k = 0; k < NV; k++)
@@ -271,6 +278,29 @@ __device__ __forceinline__ void lj_pair(float r2, float eps4, float sig2, float 
     f = 12.f * eps4 * inv_r2 * (inv_rs12 - 0.5f * inv_rs6);
     e = 0.5f * (eps4 * (inv_rs12 - inv_rs6));
 }
+// Hardware approximations (PTX ex2.approx / rsqrt.approx / rcp.approx,
+// flush-to-zero; relative error about 2^-22) for the binary32 pair
+// arithmetic of the lean kernels; a mixed-precision pair never produces a
+// subnormal argument or result in them.
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Morse (src/morse.h:35-56): p = {D0, alpha, r0, rc^2}
 __device__ __forceinline__ void morse_pair(double r2, const fmdg_pair_t &pp, double &f, double &e)
 {

@@ -98,6 +98,7 @@ struct Chunk
 struct Pack
 {
     int cls = 0, mixed = 0;
+    int lean = 0;       // one-kind jobs (lean binary32 kernels); a job's variant never depends on the mix
     cudaStream_t stream = nullptr;
     std::vector<Job *> members;
     bool dirty = true;
@@ -194,14 +195,15 @@ int want_fblk(const fmdg_server_t *S, const Pack &p)
 
 int pack_class(int cats) { return __builtin_popcount(cats) > 1 ? 0 : __builtin_ctz(cats); }
 
-// a pack of (class, mixed) with room for one more system
-Pack *pack_for(fmdg_server_t *S, int cls, int mixed)
+// a pack of (class, mixed, lean) with room for one more system
+Pack *pack_for(fmdg_server_t *S, int cls, int mixed, int lean)
 {
     for (Pack *p : S->packs[cls][mixed])
-        if (p->active() < FMDG_PACK_MAX) return p;
+        if (p->lean == lean && p->active() < FMDG_PACK_MAX) return p;
     Pack *p = new Pack();
     p->cls = cls;
     p->mixed = mixed;
+    p->lean = lean;
     if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
     {
         delete p;
@@ -329,7 +331,7 @@ int admit(fmdg_server_t *S, double budget_s)
             retire(S, j);
             continue;
         }
-        Pack *p = pack_for(S, pack_class(j->cats), j->prec == FMDG_PREC_MIXED);
+        Pack *p = pack_for(S, pack_class(j->cats), j->prec == FMDG_PREC_MIXED, j->nkinds == 1);
         if (!p)
         {
             fail_job(S, j, fmdg_set_error("fmdg_srv: cannot create a pack stream"), true);
@@ -361,6 +363,7 @@ int rebuild(fmdg_server_t *S, Pack &p)
     P.nsys = (int)p.members.size();
     P.cats = 0;
     for (const Job *j : p.members) P.cats |= j->cats;
+    P.lean = p.lean;
     P.mixed = p.mixed;
     P.fblk = fblk;
     LocPack *locs[4] = {&P.la, &P.lc, &P.lf, &P.ls};

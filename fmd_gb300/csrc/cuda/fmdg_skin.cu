@@ -149,12 +149,18 @@ __device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, 
     }
 }
 
+struct NoRound
+{
+    __device__ __forceinline__ void operator()(int) const {}
+};
+
 // List walk of slot t (four entries per round): f(neighbour slot, its
-// binary32 position, image offset).  An atom whose list overflowed scans
-// its candidates directly, with positions relative to the current cells.
-template <typename F>
+// binary32 position, image offset); r(k) after every k entries visited (a
+// round of four, or one).  An atom whose list overflowed scans its
+// candidates directly, with positions relative to the current cells.
+template <typename F, typename R>
 __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
-                                                   float4 &xi, F &&f)
+                                                   float4 &xi, F &&f, R &&r)
 {
     const int cnt = g.nbr_count[t];
     if (cnt <= g.maxnb)
@@ -172,18 +178,30 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
             f(e1 & SLOT_MASK, x1, so.off[(unsigned)e1 >> SLOT_BITS]);
             f(e2 & SLOT_MASK, x2, so.off[(unsigned)e2 >> SLOT_BITS]);
             f(e3 & SLOT_MASK, x3, so.off[(unsigned)e3 >> SLOT_BITS]);
+            r(4);
         }
         for (; k < cnt; k++)
         {
             const int e = __ldg(col + (size_t)k * cap);
             f(e & SLOT_MASK, g.xl[e & SLOT_MASK], so.off[(unsigned)e >> SLOT_BITS]);
+            r(1);
         }
     }
     else
     {
         xi = g.xf4[i];
-        for_each_candidate(g, S, i, xi, [&](int j, int code) { f(S.slot[j], g.xf4[j], so.off[code]); });
+        for_each_candidate(g, S, i, xi, [&](int j, int code) {
+            f(S.slot[j], g.xf4[j], so.off[code]);
+            r(1);
+        });
     }
+}
+
+template <typename F>
+__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
+                                                   float4 &xi, F &&f)
+{
+    for_each_slot_pair(g, S, so, t, i, xi, f, NoRound{});
 }
 
 // ---------------------------------------------------------------- kernels
@@ -284,8 +302,9 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
 }
 
 // EAM pass 1 + embedding (src/eam.h:270-406, src/eam.c:160-179), one
-// thread per slot
-template <class L, bool MIXED, bool HYBRID>
+// thread per slot.  LEAN (binary32, one kind, no group): the pair's table
+// row and cutoff in registers, no per-entry kind or group lookups.
+template <class L, bool MIXED, bool HYBRID, bool LEAN>
 __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(__grid_constant__ const L loc)
 {
     int bx, nb;
@@ -328,6 +347,29 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                         rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], q - ir2);
                     }
                 });
+            }
+            else if constexpr (LEAN)
+            {
+                const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
+                const float4 *trho = g.pkf_rho + (size_t)sp.pairs[0].jloc * nint;
+                const float rc2f = sp.pf[0][2], band = 1e-4f * rc2f;
+                const double rc2 = sp.pairs[0].p[2];
+                Acc32<1> ac;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                    const float3 rv = rv_of(xi, xj, o);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    bool in = r2 < rc2f;
+                    if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
+                    if (in)
+                    {
+                        float b;
+                        const int ir2 = table_index(r2 * inv_h, kmax, b);
+                        ac.part[0] += spl_val(trho[ir2], b);
+                    }
+                }, [&](int k) { ac.entries(k); });
+                ac.flush();
+                rho = ac.total(0);
             }
             else
             {
@@ -392,8 +434,10 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
 
 // Pair forces + velocity-Verlet finish step (src/integrators.c:94-126) and
 // the thermo record, one thread per slot; the forces are stored in the
-// current order for the next start step.
-template <class L, int CAT, bool MIXED>
+// current order for the next start step.  LEAN (binary32, one kind, no
+// group): pair parameters in registers, no per-entry kind or group
+// lookups, hardware exp2 / rsqrt / rcp approximations.
+template <class L, int CAT, bool MIXED, bool LEAN>
 __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__grid_constant__ const L loc, int finish)
 {
     int bx, nb;
@@ -464,6 +508,66 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                         pe += 0.5 * spl_val(tph, b);
                     }
                 });
+            }
+            else if constexpr (LEAN)
+            {
+                const float4 pq = make_float4(sp.pf[0][0], sp.pf[0][1], sp.pf[0][2], sp.pf[0][3]);
+                const float rc2f = (CAT == CAT_MORSE) ? pq.w : pq.z, band = 1e-4f * rc2f;
+                const double rc2 = (CAT == CAT_MORSE) ? sp.pairs[0].p[3] : sp.pairs[0].p[2];
+                // Morse: 2^((r0 - r) alpha log2 e), force factor 2 alpha D0
+                const float m_c1 = pq.y * 1.44269504f, m_c2 = 2.f * pq.y * pq.x;
+                // LJ: 12 eps4
+                const float lj_c = 12.f * pq.x;
+                const float fpi = (CAT == CAT_EAM) ? g.fpb[t] : 0.f;
+                const float inv_h = (float)g.inv_dr2;
+                const float kmax = (float)(nint - 1);
+                const int ee = sp.pairs[0].iloc;
+                const float4 *tphi = g.pkf_phi + ((size_t)ee * ne + ee) * nint;
+                const float4 *trho = g.pkf_rho + (size_t)ee * nint;
+                Acc32<4> ac;
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                    const float3 rv = rv_of(xi, xj, o);
+                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                    bool in = r2 < rc2f;
+                    if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
+                    if (!in) return;
+                    float fa, e;
+                    if (CAT == CAT_LJ)
+                    {
+                        const float inv_r2 = rcp_approx(r2);
+                        const float s2 = pq.y * inv_r2;
+                        const float s6 = s2 * s2 * s2;
+                        const float s12 = s6 * s6;
+                        fa = lj_c * inv_r2 * (s12 - 0.5f * s6);
+                        e = 0.5f * (pq.x * (s12 - s6));
+                    }
+                    else if (CAT == CAT_MORSE)
+                    {
+                        const float inv_r = rsqrt_approx(r2);
+                        const float r = r2 * inv_r;
+                        const float e1 = ex2_approx((pq.z - r) * m_c1);
+                        const float e2 = e1 * e1;
+                        fa = m_c2 * inv_r * (e2 - e1);
+                        e = 0.5f * (pq.x * (e2 - 2.f * e1));
+                    }
+                    else
+                    {
+                        float b;
+                        const int ir2 = table_index(r2 * inv_h, kmax, b);
+                        const float4 tph = tphi[ir2];
+                        const float phi_d = spl_der(tph, b, inv_h);
+                        const float rho_d = spl_der(trho[ir2], b, inv_h);
+                        fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
+                        e = 0.5f * spl_val(tph, b);
+                    }
+                    ac.part[0] += fa * rv.x;
+                    ac.part[1] += fa * rv.y;
+                    ac.part[2] += fa * rv.z;
+                    ac.part[3] += e;
+                }, [&](int k) { ac.entries(k); });
+                ac.flush();
+                for (int d = 0; d < 3; d++) f[d] = ac.total(d);
+                pe = ac.total(3);
             }
             else
             {
@@ -589,28 +693,36 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
     }
 }
 
+// lean: one kind and no group (used in binary32 only)
 template <class L, bool MIXED>
-void launch_force_skin(const L &loc, int cats, int finish, int nb, int blk, cudaStream_t st)
+void launch_force_skin(const L &loc, int cats, int finish, int nb, int blk, cudaStream_t st, bool lean)
 {
     const int ncat = __builtin_popcount(cats);
-    if (ncat > 1) k_force_skin<L, CAT_HYBRID, MIXED><<<nb, blk, 0, st>>>(loc, finish);
-    else if (cats == (1 << FMDG_POT_LJ)) k_force_skin<L, CAT_LJ, MIXED><<<nb, blk, 0, st>>>(loc, finish);
-    else if (cats == (1 << FMDG_POT_MORSE)) k_force_skin<L, CAT_MORSE, MIXED><<<nb, blk, 0, st>>>(loc, finish);
-    else k_force_skin<L, CAT_EAM, MIXED><<<nb, blk, 0, st>>>(loc, finish);
+    if (ncat > 1) k_force_skin<L, CAT_HYBRID, MIXED, false><<<nb, blk, 0, st>>>(loc, finish);
+    else if (MIXED && lean)
+    {
+        if (cats == (1 << FMDG_POT_LJ)) k_force_skin<L, CAT_LJ, true, true><<<nb, blk, 0, st>>>(loc, finish);
+        else if (cats == (1 << FMDG_POT_MORSE)) k_force_skin<L, CAT_MORSE, true, true><<<nb, blk, 0, st>>>(loc, finish);
+        else k_force_skin<L, CAT_EAM, true, true><<<nb, blk, 0, st>>>(loc, finish);
+    }
+    else if (cats == (1 << FMDG_POT_LJ)) k_force_skin<L, CAT_LJ, MIXED, false><<<nb, blk, 0, st>>>(loc, finish);
+    else if (cats == (1 << FMDG_POT_MORSE)) k_force_skin<L, CAT_MORSE, MIXED, false><<<nb, blk, 0, st>>>(loc, finish);
+    else k_force_skin<L, CAT_EAM, MIXED, false><<<nb, blk, 0, st>>>(loc, finish);
 }
 
 template <class L>
-void launch_density_skin(const L &loc, bool mixed, bool hyb, int nb, int blk, cudaStream_t st)
+void launch_density_skin(const L &loc, bool mixed, bool hyb, int nb, int blk, cudaStream_t st, bool lean)
 {
     if (mixed)
     {
-        if (hyb) k_density_skin<L, true, true><<<nb, blk, 0, st>>>(loc);
-        else k_density_skin<L, true, false><<<nb, blk, 0, st>>>(loc);
+        if (hyb) k_density_skin<L, true, true, false><<<nb, blk, 0, st>>>(loc);
+        else if (lean) k_density_skin<L, true, false, true><<<nb, blk, 0, st>>>(loc);
+        else k_density_skin<L, true, false, false><<<nb, blk, 0, st>>>(loc);
     }
     else
     {
-        if (hyb) k_density_skin<L, false, true><<<nb, blk, 0, st>>>(loc);
-        else k_density_skin<L, false, false><<<nb, blk, 0, st>>>(loc);
+        if (hyb) k_density_skin<L, false, true, false><<<nb, blk, 0, st>>>(loc);
+        else k_density_skin<L, false, false, false><<<nb, blk, 0, st>>>(loc);
     }
 }
 
@@ -632,13 +744,13 @@ int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
     }
     if ((phases & 2) && (P.cats & (1 << FMDG_POT_EAM)))
     {
-        launch_density_skin(P.lf, P.mixed != 0, __builtin_popcount(P.cats) > 1, nfb, P.fblk, st);
+        launch_density_skin(P.lf, P.mixed != 0, __builtin_popcount(P.cats) > 1, nfb, P.fblk, st, P.lean != 0);
         n++;
     }
     if (phases & 4)
     {
-        if (P.mixed) launch_force_skin<LocPack, true>(P.lf, P.cats, 1, nfb, P.fblk, st);
-        else launch_force_skin<LocPack, false>(P.lf, P.cats, 1, nfb, P.fblk, st);
+        if (P.mixed) launch_force_skin<LocPack, true>(P.lf, P.cats, 1, nfb, P.fblk, st, P.lean != 0);
+        else launch_force_skin<LocPack, false>(P.lf, P.cats, 1, nfb, P.fblk, st, false);
         n++;
     }
     cudaError_t e = cudaGetLastError();
@@ -659,10 +771,13 @@ int fmdg_skin_launch_nlist(fmdg_sys_t *s)
     return FMDG_OK;
 }
 
+// one kind and every atom in the step's group: the lean kernels
+static bool lean_system(const fmdg_sys_t *s) { return s->nkinds == 1 && s->g.st.group < 0; }
+
 int fmdg_skin_launch_density(fmdg_sys_t *s)
 {
     launch_density_skin(LocOne{s->g}, s->g.prec == FMDG_PREC_MIXED, __builtin_popcount(s->cats) > 1,
-                        fmdg_force_blocks(s), s->fblk, s->stream);
+                        fmdg_force_blocks(s), s->fblk, s->stream, lean_system(s));
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
@@ -672,8 +787,9 @@ int fmdg_skin_launch_pair_forces(fmdg_sys_t *s, int finish)
 {
     const LocOne L{s->g};
     const int nb = fmdg_force_blocks(s);
-    if (s->g.prec == FMDG_PREC_MIXED) launch_force_skin<LocOne, true>(L, s->cats, finish, nb, s->fblk, s->stream);
-    else launch_force_skin<LocOne, false>(L, s->cats, finish, nb, s->fblk, s->stream);
+    if (s->g.prec == FMDG_PREC_MIXED)
+        launch_force_skin<LocOne, true>(L, s->cats, finish, nb, s->fblk, s->stream, lean_system(s));
+    else launch_force_skin<LocOne, false>(L, s->cats, finish, nb, s->fblk, s->stream, false);
     s->launches++;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
