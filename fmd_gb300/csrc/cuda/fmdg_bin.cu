@@ -43,13 +43,15 @@ __device__ __forceinline__ int cell_flat(const Geo &g, int x, int y, int z)
 //  mode SE: src/integrators.c:129-152 (v += dt*F/m; x += dt*v)
 // Explicit _rn intrinsics keep the reference's operation order with no
 // fused multiply-add, so positions and velocities match bit for bit given
-// the same forces.
+// the same forces.  lazy (packed systems, mode REFRESH_ONLY): the cells are
+// refreshed only on a step that rebuilds the skin list.
 template <class L>
-__global__ void k_bin_classify(__grid_constant__ const L loc, int mode)
+__global__ void k_bin_classify(__grid_constant__ const L loc, int mode, int lazy)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
     if (loc_idle(loc, g)) return;
+    if (lazy && !g.dyn->rebuild) return;
     const double dt = g.st.dt;
     const int group = g.st.group, thermostat = g.st.thermostat;
     // half kick dt * 0.5 / m per kind: one binary64 division per kind, not
@@ -374,12 +376,14 @@ __global__ void k_bin_flip(__grid_constant__ const L loc, int mode)
     }
 }
 
-// per-cell binning counters of every system of a pack
+// per-cell binning counters of every system of a pack that refreshes its
+// cells this step
 __global__ void k_bin_clear(__grid_constant__ const LocPack loc)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
     if (loc_idle(loc, g)) return;
+    if (!g.dyn->rebuild) return;
     const int c = bx * blockDim.x + threadIdx.x;
     if (c >= g.ncell) return;
     g.dep_count[c] = 0;
@@ -402,7 +406,7 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
     const LocOne L{g};
     // dep_count, arr_lower, arr_total, bucket_fill are contiguous
     FMDG_CK(cudaMemsetAsync(g.dep_count, 0, sizeof(int) * 4 * (size_t)g.ncell, st));
-    k_bin_classify<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(L, mode);
+    k_bin_classify<<<fmdg_grid(g.cap, 256), 256, 0, st>>>(L, mode, 0);
     k_bin_scan<<<1, 1024, 0, st>>>(L);
     k_bin_cells<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(L);
     k_bin_arrivals<<<fmdg_grid(g.ncell, 128), 128, 0, st>>>(L);
@@ -413,20 +417,26 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
     return FMDG_OK;
 }
 
-// The same refresh (velocity-Verlet start step) for every system of a pack.
+// Step start of every system of a pack: velocity-Verlet start step, slot
+// tables and displacement test (fmdg_skin_launch_start), then the cell
+// refresh of the systems that rebuild their skin list this step (between
+// rebuilds an atom stays within skin/2 of its build position, less than a
+// cell, and the packed kernels address atoms by slot, not by cell).
 // Returns the kernels launched, or minus a status.
 int fmdg_pack_launch_refresh(const fmdg_pack_launch &P)
 {
     cudaStream_t st = P.stream;
     const int nab = P.la.bstart[P.nsys], ncb = P.lc.bstart[P.nsys];
+    int n = fmdg_pack_launch_start(P);
+    if (n < 0) return n;
     k_bin_clear<<<ncb, 128, 0, st>>>(P.lc);
-    k_bin_classify<<<nab, 128, 0, st>>>(P.la, FMDG_REFRESH_VV);
+    k_bin_classify<<<nab, 128, 0, st>>>(P.la, FMDG_REFRESH_ONLY, 1);
     k_bin_scan<<<P.nsys, 1024, 0, st>>>(P.ls);
     k_bin_cells<<<ncb, 128, 0, st>>>(P.lc);
     k_bin_arrivals<<<ncb, 128, 0, st>>>(P.lc);
     k_bin_scatter<<<nab, 128, 0, st>>>(P.la);
-    k_bin_flip<<<P.nsys, 32, 0, st>>>(P.ls, FMDG_REFRESH_VV);
+    k_bin_flip<<<P.nsys, 32, 0, st>>>(P.ls, FMDG_REFRESH_ONLY);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return -fmdg_fail("pack refresh", e);
-    return 7;
+    return n + 7;
 }

@@ -238,7 +238,8 @@ struct fmdg_pack_launch
     LocPack lf;                 // force blocks of fblk threads
     LocPack ls;                 // one block per system
 };
-// both return the number of kernels launched, or minus a status
+// all three return the number of kernels launched, or minus a status
+int fmdg_pack_launch_start(const fmdg_pack_launch &P);
 int fmdg_pack_launch_refresh(const fmdg_pack_launch &P);
 int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases);
 

@@ -459,6 +459,17 @@ int retire(fmdg_server_t *S, Job *j)
         j->fid.resize(n);
         rc = fmdg_download(s, nullptr, j->fx.data(), j->fv.data(), j->fF.data(), nullptr, nullptr, nullptr,
                            j->fid.data());
+        // packed systems refresh their cells on list rebuilds only: an atom
+        // that crossed a periodic face since then is brought back into the
+        // box as a refresh would (x -/+ l)
+        for (int a = 0; a < n && !rc; a++)
+            for (int d = 0; d < 3; d++)
+            {
+                double &x = j->fx[3 * (size_t)a + d];
+                if (!j->pbc[d]) continue;
+                if (x >= j->l[d]) x = x - j->l[d];
+                else if (x < 0.0) x = x + j->l[d];
+            }
     }
     put_event(S, j->ready);
     j->ready = nullptr;

@@ -206,30 +206,11 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
 
 // ---------------------------------------------------------------- kernels
 
-// one thread per current atom index
-template <class L>
-__global__ void k_prep_skin(__grid_constant__ const L loc)
+// Slot t's binary32 position relative to the cell it had at the last build
+// (unwrapped across periodic faces) and the displacement test against its
+// build position: sets the rebuild flag beyond skin/2.
+__device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, const double (&x)[3], float kb)
 {
-    int bx, nb;
-    const Geo &g = loc_geo(loc, bx, nb);
-    if (loc_idle(loc, g)) return;
-    Dyn *dyn = g.dyn;
-    const int i = bx * blockDim.x + threadIdx.x;
-    if (i >= dyn->n) return;
-    const Side S = g.side[dyn->cur];
-    const int cap = g.cap;
-    const int t = S.slot[i];
-    const double x[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
-    const int kind = (int)S.kind[i];
-    const float kb = __int_as_float(kind);
-    g.pos[t] = i;
-    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
-    g.gslot[t] = S.group[i];
-    // relative to the current cell (a rebuild starts from these)
-    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
-    g.xf4[i] = make_float4((float)(x[0] - c.x * g.cellh[0]), (float)(x[1] - c.y * g.cellh[1]),
-                           (float)(x[2] - c.z * g.cellh[2]), kb);
-    // relative to the cell of the last build, unwrapped
     const CellXYZ b = cell_xyz(g, g.cb[t]);
     const int b3[3] = {b.x, b.y, b.z};
     float l3[3];
@@ -247,6 +228,77 @@ __global__ void k_prep_skin(__grid_constant__ const L loc)
     const float4 o = g.xb[t];
     const float dx = l3[0] - o.x, dy = l3[1] - o.y, dz = l3[2] - o.z;
     if (!(dx * dx + dy * dy + dz * dz <= g.half_skin2)) dyn->rebuild = 1;
+}
+
+// Packed systems, every step (one thread per current atom index): the
+// velocity-Verlet start step (src/integrators.c:40-75, the operations of
+// k_bin_classify), the slot tables that change every step and the
+// displacement test; advances the device time by one step.  The cells and
+// the remaining slot tables are refreshed on rebuild steps only.
+template <class L>
+__global__ void k_skin_start(__grid_constant__ const L loc)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    const double dt = g.st.dt;
+    const int group = g.st.group, thermostat = g.st.thermostat;
+    __shared__ double hk[FMDG_MAXK];
+    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = __ddiv_rn(__dmul_rn(dt, 0.5), g.mass[threadIdx.x]);
+    __syncthreads();
+    Dyn *dyn = g.dyn;
+    if (bx == 0 && threadIdx.x == 0) dyn->time += dt;
+    const int i = bx * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    const size_t cap = g.cap;
+    const int kind = (int)S.kind[i];
+    double x[3] = {S.x[i], S.x[cap + i], S.x[2 * cap + i]};
+    if (group < 0 || S.group[i] == group)
+    {
+        const double lam = dyn->lambda;
+        const double coef = hk[kind];
+        for (int d = 0; d < 3; d++)
+        {
+            double vv = S.v[d * cap + i];
+            if (thermostat) vv = __dmul_rn(vv, lam);
+            vv = __dadd_rn(vv, __dmul_rn(coef, g.F[d * cap + i]));
+            S.v[d * cap + i] = vv;
+            x[d] = __dadd_rn(x[d], __dmul_rn(dt, vv));
+            S.x[d * cap + i] = x[d];
+        }
+    }
+    const int t = S.slot[i];
+    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
+    slot_rel_build(g, dyn, t, x, __int_as_float(kind));
+}
+
+// one thread per current atom index; lazy (packed systems): rebuild steps
+// only, after the cell refresh
+template <class L>
+__global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
+{
+    int bx, nb;
+    const Geo &g = loc_geo(loc, bx, nb);
+    if (loc_idle(loc, g)) return;
+    Dyn *dyn = g.dyn;
+    if (lazy && !dyn->rebuild) return;
+    const int i = bx * blockDim.x + threadIdx.x;
+    if (i >= dyn->n) return;
+    const Side S = g.side[dyn->cur];
+    const int cap = g.cap;
+    const int t = S.slot[i];
+    const double x[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+    const int kind = (int)S.kind[i];
+    const float kb = __int_as_float(kind);
+    g.pos[t] = i;
+    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
+    g.gslot[t] = S.group[i];
+    // relative to the current cell (a rebuild starts from these)
+    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
+    g.xf4[i] = make_float4((float)(x[0] - c.x * g.cellh[0]), (float)(x[1] - c.y * g.cellh[1]),
+                           (float)(x[2] - c.z * g.cellh[2]), kb);
+    slot_rel_build(g, dyn, t, x, kb);
 }
 
 // one thread per slot; every block leaves at once when no rebuild is due
@@ -728,6 +780,14 @@ void launch_density_skin(const L &loc, bool mixed, bool hyb, int nb, int blk, cu
 
 } // namespace
 
+int fmdg_pack_launch_start(const fmdg_pack_launch &P)
+{
+    k_skin_start<<<P.la.bstart[P.nsys], 128, 0, P.stream>>>(P.la);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -fmdg_fail("pack start", e);
+    return 1;
+}
+
 // phases: bit 0 slot tables + list (re)build, bit 1 EAM density, bit 2
 // pair forces + finish step (all three for a step).  Returns the kernels
 // launched, or minus a status.
@@ -738,7 +798,7 @@ int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
     int n = 0;
     if (phases & 1)
     {
-        k_prep_skin<<<nab, 128, 0, st>>>(P.la);
+        k_prep_skin<<<nab, 128, 0, st>>>(P.la, 1);
         k_nlist_skin<<<nfb, P.fblk, 0, st>>>(P.lf);
         n += 2;
     }
@@ -764,7 +824,7 @@ int fmdg_pack_launch_forces(const fmdg_pack_launch &P, int phases)
 int fmdg_skin_launch_nlist(fmdg_sys_t *s)
 {
     const LocOne L{s->g};
-    k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L);
+    k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L, 0);
     k_nlist_skin<<<fmdg_force_blocks(s), s->fblk, 0, s->stream>>>(L);
     s->launches += 2;
     FMDG_CK(cudaGetLastError());
