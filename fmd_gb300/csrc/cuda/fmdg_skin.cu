@@ -156,9 +156,11 @@ struct NoRound
 
 // List walk of slot t (four entries per round): f(neighbour slot, its
 // binary32 position, image offset); r(k) after every k entries visited (a
-// round of four, or one).  An atom whose list overflowed scans its
-// candidates directly, with positions relative to the current cells.
-template <typename F, typename R>
+// round of four, or one).  PF: the next round's list rows are prefetched
+// into L1 while this round is processed (the rows stream from DRAM).  An
+// atom whose list overflowed scans its candidates directly, with positions
+// relative to the current cells.
+template <bool PF = false, typename F, typename R>
 __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
                                                    float4 &xi, F &&f, R &&r)
 {
@@ -170,6 +172,8 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
         int k = 0;
         for (; k + 4 <= cnt; k += 4)
         {
+            if (PF && k + 8 <= cnt)
+                for (int q = 4; q < 8; q++) asm volatile("prefetch.global.L1 [%0];" ::"l"(col + (size_t)(k + q) * cap));
             const int e0 = __ldg(col + (size_t)k * cap), e1 = __ldg(col + (size_t)(k + 1) * cap);
             const int e2 = __ldg(col + (size_t)(k + 2) * cap), e3 = __ldg(col + (size_t)(k + 3) * cap);
             const float4 x0 = g.xl[e0 & SLOT_MASK], x1 = g.xl[e1 & SLOT_MASK];
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 const float rc2f = sp.pf[0][2], band = 1e-4f * rc2f;
                 const double rc2 = sp.pairs[0].p[2];
                 Acc32<1> ac;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                     const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     bool in = r2 < rc2f;
@@ -577,12 +581,12 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                 const float4 *tphi = g.pkf_phi + ((size_t)ee * ne + ee) * nint;
                 const float4 *trho = g.pkf_rho + (size_t)ee * nint;
                 Acc32<4> ac;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                for_each_slot_pair<CAT != CAT_EAM>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                     const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     bool in = r2 < rc2f;
                     if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
-                    if (!in) return;
+                    if (CAT == CAT_EAM && !in) return;
                     float fa, e;
                     if (CAT == CAT_LJ)
                     {
@@ -611,6 +615,13 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                         const float rho_d = spl_der(trho[ir2], b, inv_h);
                         fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
                         e = 0.5f * spl_val(tph, b);
+                    }
+                    if (CAT != CAT_EAM)
+                    {
+                        // LJ / Morse: the arithmetic runs for every entry
+                        // (lanes beyond the cutoff contribute zero), no branch
+                        fa = in ? fa : 0.f;
+                        e = in ? e : 0.f;
                     }
                     ac.part[0] += fa * rv.x;
                     ac.part[1] += fa * rv.y;
