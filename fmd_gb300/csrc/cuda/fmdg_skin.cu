@@ -406,25 +406,54 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             }
             else if constexpr (LEAN)
             {
+                // branch-free walk (table rows read for every entry, entries
+                // beyond the cutoff add zero); near-cutoff entries decided in
+                // binary64 after the walk, as in the lean force kernel
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
                 const float4 *trho = g.pkf_rho + (size_t)sp.pairs[0].jloc * nint;
-                const float rc2f = sp.pf[0][2], band = 1e-4f * rc2f;
+                const float rc2f = sp.pf[0][2], band = 2e-5f * rc2f;
                 const double rc2 = sp.pairs[0].p[2];
                 Acc32<1> ac;
+                int npend = 0, pend = 0;
+                float pr2 = 0.f;
                 for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                     const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                    bool in = r2 < rc2f;
-                    if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
-                    if (in)
+                    const bool near = fabsf(r2 - rc2f) <= band;
+                    const bool in = (r2 < rc2f) && !near;
+                    npend += near;
+                    pend = near ? js : pend;
+                    pr2 = near ? r2 : pr2;
+                    float b;
+                    const int ir2 = table_index(r2 * inv_h, kmax, b);
+                    const float v = spl_val(trho[ir2], b);
+                    ac.part[0] += in ? v : 0.f;
+                }, [&](int k) { ac.entries(k); });
+                ac.flush();
+                if (npend == 1)
+                {
+                    if (geom64_mi(g, g.xd[t], g.xd[pend]).r2 < rc2)
                     {
+                        float b;
+                        const int ir2 = table_index(pr2 * inv_h, kmax, b);
+                        ac.part[0] += spl_val(trho[ir2], b);
+                        ac.flush();
+                    }
+                }
+                else if (npend > 1)
+                {
+                    for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                        const float3 rv = rv_of(xi, xj, o);
+                        const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                        if (!(fabsf(r2 - rc2f) <= band)) return;
+                        if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
                         float b;
                         const int ir2 = table_index(r2 * inv_h, kmax, b);
                         ac.part[0] += spl_val(trho[ir2], b);
-                    }
-                }, [&](int k) { ac.entries(k); });
-                ac.flush();
+                    }, [&](int k) { ac.entries(k); });
+                    ac.flush();
+                }
                 rho = ac.total(0);
             }
             else
@@ -568,7 +597,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
             else if constexpr (LEAN)
             {
                 const float4 pq = make_float4(sp.pf[0][0], sp.pf[0][1], sp.pf[0][2], sp.pf[0][3]);
-                const float rc2f = (CAT == CAT_MORSE) ? pq.w : pq.z, band = 1e-4f * rc2f;
+                const float rc2f = (CAT == CAT_MORSE) ? pq.w : pq.z;
                 const double rc2 = (CAT == CAT_MORSE) ? sp.pairs[0].p[3] : sp.pairs[0].p[2];
                 // Morse: 2^((r0 - r) alpha log2 e), force factor 2 alpha D0
                 const float m_c1 = pq.y * 1.44269504f, m_c2 = 2.f * pq.y * pq.x;
@@ -580,14 +609,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                 const int ee = sp.pairs[0].iloc;
                 const float4 *tphi = g.pkf_phi + ((size_t)ee * ne + ee) * nint;
                 const float4 *trho = g.pkf_rho + (size_t)ee * nint;
-                Acc32<4> ac;
-                for_each_slot_pair<CAT != CAT_EAM>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                    const float3 rv = rv_of(xi, xj, o);
-                    const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                    bool in = r2 < rc2f;
-                    if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
-                    if (CAT == CAT_EAM && !in) return;
-                    float fa, e;
+                // LJ / Morse pair: force factor and half energy
+                auto pair_lm = [&](float r2, float &fa, float &e) {
                     if (CAT == CAT_LJ)
                     {
                         const float inv_r2 = rcp_approx(r2);
@@ -597,7 +620,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                         fa = lj_c * inv_r2 * (s12 - 0.5f * s6);
                         e = 0.5f * (pq.x * (s12 - s6));
                     }
-                    else if (CAT == CAT_MORSE)
+                    else
                     {
                         const float inv_r = rsqrt_approx(r2);
                         const float r = r2 * inv_r;
@@ -606,29 +629,91 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__
                         fa = m_c2 * inv_r * (e2 - e1);
                         e = 0.5f * (pq.x * (e2 - 2.f * e1));
                     }
-                    else
-                    {
+                };
+                Acc32<4> ac;
+                if constexpr (CAT == CAT_EAM)
+                {
+                    const float band = 1e-4f * rc2f;
+                    for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                        const float3 rv = rv_of(xi, xj, o);
+                        const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                        bool in = r2 < rc2f;
+                        if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
+                        if (!in) return;
                         float b;
                         const int ir2 = table_index(r2 * inv_h, kmax, b);
                         const float4 tph = tphi[ir2];
                         const float phi_d = spl_der(tph, b, inv_h);
                         const float rho_d = spl_der(trho[ir2], b, inv_h);
-                        fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
-                        e = 0.5f * spl_val(tph, b);
-                    }
-                    if (CAT != CAT_EAM)
-                    {
-                        // LJ / Morse: the arithmetic runs for every entry
-                        // (lanes beyond the cutoff contribute zero), no branch
+                        const float fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
+                        ac.part[0] += fa * rv.x;
+                        ac.part[1] += fa * rv.y;
+                        ac.part[2] += fa * rv.z;
+                        ac.part[3] += 0.5f * spl_val(tph, b);
+                    }, [&](int k) { ac.entries(k); });
+                    ac.flush();
+                }
+                else
+                {
+                    // Branch-free walk: the arithmetic runs for every entry and
+                    // entries beyond the cutoff add zero.  An entry within
+                    // 2e-5 relative of the cutoff (several times the binary32
+                    // error of r^2) is decided in binary64 after the walk: one
+                    // such entry per atom is kept in registers, more (rare)
+                    // send the atom through a second walk over its near
+                    // entries only.
+                    const float band = 2e-5f * rc2f;
+                    int npend = 0, pend = 0;
+                    float3 prv = make_float3(0.f, 0.f, 0.f);
+                    for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                        const float3 rv = rv_of(xi, xj, o);
+                        const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                        const bool near = fabsf(r2 - rc2f) <= band;
+                        const bool in = (r2 < rc2f) && !near;
+                        npend += near;
+                        pend = near ? js : pend;
+                        prv = near ? rv : prv;
+                        float fa, e;
+                        pair_lm(r2, fa, e);
                         fa = in ? fa : 0.f;
                         e = in ? e : 0.f;
+                        ac.part[0] += fa * rv.x;
+                        ac.part[1] += fa * rv.y;
+                        ac.part[2] += fa * rv.z;
+                        ac.part[3] += e;
+                    }, [&](int k) { ac.entries(k); });
+                    ac.flush();
+                    if (npend == 1)
+                    {
+                        if (geom64_mi(g, g.xd[t], g.xd[pend]).r2 < rc2)
+                        {
+                            const float r2 = prv.x * prv.x + prv.y * prv.y + prv.z * prv.z;
+                            float fa, e;
+                            pair_lm(r2, fa, e);
+                            ac.part[0] += fa * prv.x;
+                            ac.part[1] += fa * prv.y;
+                            ac.part[2] += fa * prv.z;
+                            ac.part[3] += e;
+                            ac.flush();
+                        }
                     }
-                    ac.part[0] += fa * rv.x;
-                    ac.part[1] += fa * rv.y;
-                    ac.part[2] += fa * rv.z;
-                    ac.part[3] += e;
-                }, [&](int k) { ac.entries(k); });
-                ac.flush();
+                    else if (npend > 1)
+                    {
+                        for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                            const float3 rv = rv_of(xi, xj, o);
+                            const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                            if (!(fabsf(r2 - rc2f) <= band)) return;
+                            if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
+                            float fa, e;
+                            pair_lm(r2, fa, e);
+                            ac.part[0] += fa * rv.x;
+                            ac.part[1] += fa * rv.y;
+                            ac.part[2] += fa * rv.z;
+                            ac.part[3] += e;
+                        }, [&](int k) { ac.entries(k); });
+                        ac.flush();
+                    }
+                }
                 for (int d = 0; d < 3; d++) f[d] = ac.total(d);
                 pe = ac.total(3);
             }
