@@ -277,8 +277,11 @@ __global__ void k_skin_start(__grid_constant__ const L loc)
     slot_rel_build(g, dyn, t, x, __int_as_float(kind));
 }
 
-// one thread per current atom index; lazy (packed systems): rebuild steps
-// only, after the cell refresh
+// one thread per current atom index.  lazy (packed systems): rebuild steps
+// only, after the cell refresh, and the slots are renumbered in the
+// current (cell) order -- slot = index, so the rebuild walks and writes
+// consecutive atoms of a cell together, and until the next rebuild (no
+// refresh in between) every slot-to-index map is the identity
 template <class L>
 __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
 {
@@ -288,10 +291,15 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     Dyn *dyn = g.dyn;
     if (lazy && !dyn->rebuild) return;
     const int i = bx * blockDim.x + threadIdx.x;
-    if (i >= dyn->n) return;
+    if (i >= dyn->n)
+    {
+        if (lazy && i < g.cap) g.pos[i] = -1;
+        return;
+    }
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
-    const int t = S.slot[i];
+    const int t = lazy ? i : S.slot[i];
+    if (lazy) S.slot[i] = i;
     const double x[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
     const int kind = (int)S.kind[i];
     const float kb = __int_as_float(kind);
@@ -302,7 +310,9 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     const CellXYZ c = cell_xyz(g, S.cell_of[i]);
     g.xf4[i] = make_float4((float)(x[0] - c.x * g.cellh[0]), (float)(x[1] - c.y * g.cellh[1]),
                            (float)(x[2] - c.z * g.cellh[2]), kb);
-    slot_rel_build(g, dyn, t, x, kb);
+    // (renumbered: the build cell and position of slot t are rewritten by
+    // the list build that follows)
+    if (!lazy) slot_rel_build(g, dyn, t, x, kb);
 }
 
 // one thread per slot; every block leaves at once when no rebuild is due
