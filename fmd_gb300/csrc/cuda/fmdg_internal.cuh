@@ -185,6 +185,7 @@ struct LocOne
 {
     static constexpr int max_threads = 128;
     static constexpr int min_blocks = 0;      // 0: register count left to the compiler
+    static constexpr int lean_min_blocks = 7; // lean force kernels: 7 blocks of 128 (72 registers), measured best
     Geo g;
 };
 
@@ -192,6 +193,7 @@ struct LocPack
 {
     static constexpr int max_threads = 256;
     static constexpr int min_blocks = 0;
+    static constexpr int lean_min_blocks = 0; // packed lean force kernels: compiler's choice, measured best
     int nsys;
     int bstart[FMDG_PACK_MAX + 1];
     Geo geos[FMDG_PACK_MAX];

@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
 // group): pair parameters in registers, no per-entry kind or group
 // lookups, hardware exp2 / rsqrt / rcp approximations.
 template <class L, int CAT, bool MIXED, bool LEAN>
-__global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force_skin(__grid_constant__ const L loc, int finish)
+__global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L::min_blocks) k_force_skin(__grid_constant__ const L loc, int finish)
 {
     int bx, nb;
     const Geo &g = loc_geo(loc, bx, nb);
