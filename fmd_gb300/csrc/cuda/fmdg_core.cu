@@ -93,7 +93,7 @@ void drop_eam(fmdg_sys_t *s)
     Geo &g = s->g;
     g.eF = g.eFDD = g.erho = g.erhoDD = g.ephi = g.ephiDD = nullptr;
     g.pk_rho = g.pk_phi = g.pk_F = nullptr;
-    g.pkf_rho = g.pkf_phi = g.pkf_F = nullptr;
+    g.pkf_rho = g.pkf_phi = g.pkf_F = g.pkf_pr = nullptr;
     s->eam_borrowed = false;
 }
 
@@ -231,6 +231,7 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     dfree(s, (void *)s->g.erhoDD); dfree(s, (void *)s->g.ephi); dfree(s, (void *)s->g.ephiDD);
     dfree(s, (void *)s->g.pk_rho); dfree(s, (void *)s->g.pk_phi); dfree(s, (void *)s->g.pk_F);
     dfree(s, (void *)s->g.pkf_rho); dfree(s, (void *)s->g.pkf_phi); dfree(s, (void *)s->g.pkf_F);
+    dfree(s, (void *)s->g.pkf_pr);
     for (int k = 0; k < s->nturi; k++)
     {
         DTuri &t = s->turi[k];
@@ -347,6 +348,7 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     // precision, which the two-sample difference y_k+1 - y_k would not.
     dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
     dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
+    dfree(s, (void *)g.pkf_pr);
     auto pack = [&](const double *y, const double *ydd, double h, int npts, int nfun, const double4_32a **d64,
                     const float4 **d32) -> int {
         const size_t nint = (size_t)npts - 1;
@@ -371,6 +373,21 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     if ((rc = pack(rho, rhoDD, dr2, Nr2, nelem, &g.pk_rho, &g.pkf_rho))) return rc;
     if ((rc = pack(phi, phiDD, dr2, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi))) return rc;
     if ((rc = pack(F, F_DD, drho, Nrho, nelem, &g.pk_F, &g.pkf_F))) return rc;
+    {
+        // the one-element pair rows side by side for the lean force kernels
+        const size_t nint = (size_t)Nr2 - 1;
+        std::vector<float4> phi32(nint * nelem * nelem), rho32(nint * nelem), pr(2 * nint * nelem);
+        FMDG_CK(cudaMemcpy(phi32.data(), g.pkf_phi, phi32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        FMDG_CK(cudaMemcpy(rho32.data(), g.pkf_rho, rho32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int e = 0; e < nelem; e++)
+            for (size_t k = 0; k < nint; k++)
+            {
+                pr[2 * (e * nint + k)] = phi32[((size_t)e * nelem + e) * nint + k];
+                pr[2 * (e * nint + k) + 1] = rho32[(size_t)e * nint + k];
+            }
+        if ((rc = dalloc(s, (float4 **)&g.pkf_pr, pr.size()))) return rc;
+        FMDG_CK(cudaMemcpy((void *)g.pkf_pr, pr.data(), pr.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    }
     invalidate_graph(s);
     return FMDG_OK;
 }
@@ -450,11 +467,12 @@ extern "C" int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner)
         dfree(s, (void *)g.erhoDD); dfree(s, (void *)g.ephi); dfree(s, (void *)g.ephiDD);
         dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
         dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
+        dfree(s, (void *)g.pkf_pr);
     }
     const Geo &o = owner->g;
     g.eF = o.eF; g.eFDD = o.eFDD; g.erho = o.erho; g.erhoDD = o.erhoDD; g.ephi = o.ephi; g.ephiDD = o.ephiDD;
     g.pk_rho = o.pk_rho; g.pk_phi = o.pk_phi; g.pk_F = o.pk_F;
-    g.pkf_rho = o.pkf_rho; g.pkf_phi = o.pkf_phi; g.pkf_F = o.pkf_F;
+    g.pkf_rho = o.pkf_rho; g.pkf_phi = o.pkf_phi; g.pkf_F = o.pkf_F; g.pkf_pr = o.pkf_pr;
     g.nelem = o.nelem; g.Nrho = o.Nrho; g.Nr2 = o.Nr2; g.drho = o.drho; g.dr2 = o.dr2;
     g.inv_dr2 = o.inv_dr2; g.inv_drho = o.inv_drho;
     s->eam_borrowed = true;

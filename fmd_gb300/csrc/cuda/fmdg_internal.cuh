@@ -79,6 +79,7 @@ struct Geo   // passed by value to kernels
     // packed spline tables: per interval k {y_k, y_k+1, y''_k, y''_k+1}
     const double4_32a *pk_rho, *pk_phi, *pk_F;     // binary64
     const float4 *pkf_rho, *pkf_phi, *pkf_F;   // binary32 copies (mixed mode)
+    const float4 *pkf_pr;       // per element e and interval k: {phi_ee, rho_e} side by side (one 32 B row)
     double inv_dr2, inv_drho;
     // binning scratch
     int *bdest;        // destination interior cell, -1 deleted, -2 stays

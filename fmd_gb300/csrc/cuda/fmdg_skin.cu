@@ -617,8 +617,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
                 const int ee = sp.pairs[0].iloc;
-                const float4 *tphi = g.pkf_phi + ((size_t)ee * ne + ee) * nint;
-                const float4 *trho = g.pkf_rho + (size_t)ee * nint;
+                const float4 *tpr = g.pkf_pr + (size_t)ee * nint * 2;
                 // LJ / Morse pair: force factor and half energy
                 auto pair_lm = [&](float r2, float &fa, float &e) {
                     if (CAT == CAT_LJ)
@@ -652,9 +651,9 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         if (!in) return;
                         float b;
                         const int ir2 = table_index(r2 * inv_h, kmax, b);
-                        const float4 tph = tphi[ir2];
+                        const float4 tph = tpr[2 * ir2], trh = tpr[2 * ir2 + 1];
                         const float phi_d = spl_der(tph, b, inv_h);
-                        const float rho_d = spl_der(trho[ir2], b, inv_h);
+                        const float rho_d = spl_der(trh, b, inv_h);
                         const float fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
                         ac.part[0] += fa * rv.x;
                         ac.part[1] += fa * rv.y;
