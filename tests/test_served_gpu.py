@@ -249,3 +249,51 @@ def test_more_jobs_than_one_pack(L, eam):
         for u, w in zip(a, b):
             np.testing.assert_array_equal(u, w)
     srv.close()
+
+
+@pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
+def test_long_hot_run(L, eam, precision):
+    """300 steps of a 1200 K argon gas: atoms cross periodic faces and each
+    packed list is rebuilt many times (cells refreshed on rebuild steps
+    only, slots renumbered at every rebuild).  binary64: positions within
+    1e-8 A (minimum image) of the single-system path, which refreshes its
+    cells every step; both precisions: final forces against the binary64
+    oracle at the pack's own positions (1e-10 / 1e-5 of max |F|)."""
+    import pyoracle
+    x, v, l, kind = _sys("lj", 6, 1200.0, 81)
+    steps = 300
+    srv = serve.Server(L, chunk_steps=16, eam=eam)
+    jid = srv.submit("lj", x, v, l, steps, precision=precision, keep_state=True)
+    srv.drain()
+    r = srv.result(jid)
+    assert r.state == 2 and r.errbits == 0
+    xp, vp, Fp, ids = srv.state(jid, len(x))
+    srv.close()
+    assert xp.min() >= 0.0 and xp.max() < l
+    if precision == serve.PREC_FP64:
+        one = serve.Single(L, "lj", x, v, l, precision=serve.PREC_FP64)
+        one.steps(steps)
+        xs, vs, Fs = _by_id(one.state())
+        one.close()
+        o = np.argsort(ids)
+        d = xs - xp[o]
+        d -= l * np.round(d / l)
+        assert np.abs(d).max() <= 1e-8
+    nc, cellh, order, counts = serve.host_binning3(xp, l, serve.job_rc("lj"))
+    kinds, pots = ORACLE_POTS["lj"]
+    o = pyoracle.Oracle()
+    o.setup(np.broadcast_to(l, (3,)), [1, 1, 1], nc, cellh, kinds, pots, None)
+    n = len(xp)
+    ncell_all = int(np.prod(nc))
+    o.upload(np.repeat(np.arange(ncell_all, dtype=np.int32), counts), xp[order], vp[order], np.zeros(n, np.uint32),
+             np.zeros(n, np.int32), ids[order], ncell_all)
+    o.forces(-1)
+    dd = o.dump()
+    o.close()
+    Fo = np.zeros_like(Fp)
+    Fo[dd["id"]] = dd["F"]
+    Fq = np.zeros_like(Fp)
+    Fq[ids] = Fp
+    tol = 1e-10 if precision == serve.PREC_FP64 else 1e-5
+    err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
+    assert err <= tol, err
