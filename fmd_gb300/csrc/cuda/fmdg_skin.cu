@@ -1,34 +1,42 @@
-// Packed (served) systems: pair kernels over a Verlet-skin neighbour list.
+// Pair kernels over a Verlet-skin neighbour list: packed (served) systems,
+// and single systems in mixed precision whose box allows it.
 //
-// The single-system path rebuilds its list every step in the current
-// (reference cell) order.  Packed systems keep a list of radius
-// rc + skin, indexed by a stable slot number (the atom's position in the
-// upload order, carried through every re-binning), and rebuild it only
-// when an atom has moved more than skin/2 since the last build -- the
-// usual Verlet-list criterion, which keeps every pair that can come within
-// the cutoff in the list.  Pairs are still tested against the exact cutoff
-// at every evaluation, so the list only prunes.
+// Systems on the per-step path rebuild their list every step in the
+// current (reference cell) order.  Skin-list systems keep a list of radius
+// rc + skin indexed by a slot number and rebuild it only when an atom has
+// moved more than skin/2 since the last build -- the usual Verlet-list
+// criterion, which keeps every pair that can come within the cutoff in the
+// list.  Pairs are still tested against the exact cutoff at every
+// evaluation, so the list only prunes.
 //
-// Per step (after the refresh, which is the reference's exact binning):
-//   k_prep_skin     slot tables: position (binary32 relative to the build
-//                   cell, binary64), kind, group, current index;
+// Slots.  A slot starts as the atom's upload position and travels with the
+// atom through every re-binning.  Packed systems renumber the slots in the
+// current cell order at each rebuild (slot = index), and refresh their
+// cells only on rebuild steps, so between rebuilds slot and index coincide.
+//
+// Packed step:
+//   k_skin_start    velocity-Verlet start step, per-step slot positions,
 //                   displacement test -> rebuild flag
-//   k_nlist_skin    (when flagged) stencil scan of the cells within the list
-//                   radius of the atom's current cell
+//   (rebuild steps only) reference-order cell refresh (fmdg_bin.cu),
+//   k_prep_skin     slot tables (renumbered), k_nlist_skin stencil scan of
+//                   the cells within the list radius
 //   k_density_skin  EAM pass 1 + embedding, one thread per slot
 //   k_force_skin    pair forces + velocity-Verlet finish step + thermo
 //                   record, one thread per slot
+// Single-system step: the reference-order refresh every step, then
+// k_prep_skin (stable slots), k_nlist_skin (when flagged), density, forces.
 //
 // Geometry.  An atom's binary32 position is kept relative to the cell it
 // had at the last build (unwrapped across periodic faces: it moves less
 // than skin/2 before the next build), and a list entry holds the stencil
 // offset between the two build cells, so a pair is formed exactly as on the
-// single-system path: x_i - x_j - offset * cellh.  Binary64: the minimum
-// image as the reference's ghost copy forms it (x_j + shift, then x_i minus
-// that, src/md-ghost.c:85-107, src/forces.h:25-34); every periodic box
-// length exceeds twice the list radius, so one image at most lies inside
-// it.  Pair arithmetic, precision modes and the near-cutoff binary64
-// re-test are those of the single-system kernels (fmdg_force.cu).
+// per-step path: x_i - x_j - offset * cellh.  Binary64: the minimum image
+// as the reference's ghost copy forms it (x_j + shift, then x_i minus that,
+// src/md-ghost.c:85-107, src/forces.h:25-34); every periodic box length
+// exceeds twice the list radius, so one image at most lies inside it.
+// Pair arithmetic and precision modes are those of the per-step kernels
+// (fmdg_force.cu); the lean variants (one kind, no group) are described at
+// k_force_skin.
 #include "fmdg_pairs.cuh"
 
 namespace {
