@@ -269,7 +269,9 @@ def run_ours(args):
     value = natoms / (ms_per_step * 1e-3)
     force_ms = phases["force"]
     achieved = natoms * FLOP_FORCE / (force_ms * 1e-3) / 1e12
-    peak = peak64.value if args.precision == "fp64" else peak32.value
+    # both modes issue on the binary32 pipe: binary64 mode evaluates EAM
+    # pairs in double-float arithmetic (fmdg_df.cuh), binary64 accuracy
+    peak = peak32.value
     out = {
         "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -281,9 +283,11 @@ def run_ours(args):
                    "l2": "flushed before every timed step (working set < L2)"},
         "gpu_launches": int(lc1.value - lc0.value),
         "phases_ms": phases,
-        "roofline": {"bound": "fp64-issue" if args.precision == "fp64" else "fp32-issue",
-                     "kernel": "k_force (EAM pair forces + finish step)",
+        "roofline": {"bound": "fp32-issue",
+                     "kernel": ("k_force (EAM pair forces + finish step, double-float binary64 arithmetic)"
+                                if args.precision == "fp64" else "k_force (EAM pair forces + finish step)"),
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "frac_of_fp64_fma_peak": achieved / peak64.value,
                      "peak_source": "measured FMA-chain microkernel (no CUDA-core peak in MEASURED_PEAKS.json)",
                      "traffic": (FORCE_DRAM_BYTES_PER_ATOM["eam_single"] * natoms if args.precision == "mixed"
                                  else None)},

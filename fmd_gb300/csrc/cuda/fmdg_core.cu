@@ -11,6 +11,7 @@
 #include <string.h>
 #include <vector>
 #include "fmdg_internal.cuh"
+#include "fmdg_df.cuh"
 
 static thread_local char g_errmsg[512] = "";
 
@@ -94,6 +95,7 @@ void drop_eam(fmdg_sys_t *s)
     g.eF = g.eFDD = g.erho = g.erhoDD = g.ephi = g.ephiDD = nullptr;
     g.pk_rho = g.pk_phi = g.pk_F = nullptr;
     g.pkf_rho = g.pkf_phi = g.pkf_F = g.pkf_pr = nullptr;
+    g.pkd_rho = g.pkd_phi = nullptr;
     s->eam_borrowed = false;
 }
 
@@ -231,7 +233,7 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     dfree(s, (void *)s->g.erhoDD); dfree(s, (void *)s->g.ephi); dfree(s, (void *)s->g.ephiDD);
     dfree(s, (void *)s->g.pk_rho); dfree(s, (void *)s->g.pk_phi); dfree(s, (void *)s->g.pk_F);
     dfree(s, (void *)s->g.pkf_rho); dfree(s, (void *)s->g.pkf_phi); dfree(s, (void *)s->g.pkf_F);
-    dfree(s, (void *)s->g.pkf_pr);
+    dfree(s, (void *)s->g.pkf_pr); dfree(s, (void *)s->g.pkd_rho); dfree(s, (void *)s->g.pkd_phi);
     for (int k = 0; k < s->nturi; k++)
     {
         DTuri &t = s->turi[k];
@@ -348,12 +350,12 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     // precision, which the two-sample difference y_k+1 - y_k would not.
     dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
     dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
-    dfree(s, (void *)g.pkf_pr);
+    dfree(s, (void *)g.pkf_pr); dfree(s, (void *)g.pkd_rho); dfree(s, (void *)g.pkd_phi);
     auto pack = [&](const double *y, const double *ydd, double h, int npts, int nfun, const double4_32a **d64,
-                    const float4 **d32) -> int {
+                    const float4 **d32, const float4 **ddf) -> int {
         const size_t nint = (size_t)npts - 1;
         std::vector<double4_32a> h64(nint * nfun);
-        std::vector<float4> h32(nint * nfun);
+        std::vector<float4> h32(nint * nfun), hdf(ddf ? 2 * nint * nfun : 0);
         const double hh6 = h * h / 6.0;
         for (int f = 0; f < nfun; f++)
             for (size_t k = 0; k < nint; k++)
@@ -363,16 +365,27 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
                 const double k0 = yy[k], k1 = yy[k + 1] - yy[k] - 2.0 * c0 - c1, k2 = 3.0 * c0, k3 = c1 - c0;
                 h64[f * nint + k] = make_double4_32a(k0, k1, k2, k3);
                 h32[f * nint + k] = make_float4((float)k0, (float)k1, (float)k2, (float)k3);
+                if (ddf)
+                {
+                    const float2 s0 = df_split(k0), s1 = df_split(k1), s2 = df_split(k2), s3 = df_split(k3);
+                    hdf[2 * (f * nint + k)] = make_float4(s0.x, s1.x, s2.x, s3.x);
+                    hdf[2 * (f * nint + k) + 1] = make_float4(s0.y, s1.y, s2.y, s3.y);
+                }
             }
         int rc2;
         if ((rc2 = dalloc(s, (double4_32a **)d64, h64.size())) || (rc2 = dalloc(s, (float4 **)d32, h32.size()))) return rc2;
         FMDG_CK(cudaMemcpy((void *)*d64, h64.data(), h64.size() * sizeof(double4_32a), cudaMemcpyHostToDevice));
         FMDG_CK(cudaMemcpy((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        if (ddf)
+        {
+            if ((rc2 = dalloc(s, (float4 **)ddf, hdf.size()))) return rc2;
+            FMDG_CK(cudaMemcpy((void *)*ddf, hdf.data(), hdf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        }
         return FMDG_OK;
     };
-    if ((rc = pack(rho, rhoDD, dr2, Nr2, nelem, &g.pk_rho, &g.pkf_rho))) return rc;
-    if ((rc = pack(phi, phiDD, dr2, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi))) return rc;
-    if ((rc = pack(F, F_DD, drho, Nrho, nelem, &g.pk_F, &g.pkf_F))) return rc;
+    if ((rc = pack(rho, rhoDD, dr2, Nr2, nelem, &g.pk_rho, &g.pkf_rho, &g.pkd_rho))) return rc;
+    if ((rc = pack(phi, phiDD, dr2, Nr2, nelem * nelem, &g.pk_phi, &g.pkf_phi, &g.pkd_phi))) return rc;
+    if ((rc = pack(F, F_DD, drho, Nrho, nelem, &g.pk_F, &g.pkf_F, nullptr))) return rc;
     {
         // the one-element pair rows side by side for the lean force kernels
         const size_t nint = (size_t)Nr2 - 1;
@@ -433,7 +446,7 @@ int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
 size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
 {
     const size_t cap = n > 0 ? n : 1;
-    const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8;
+    const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8 + 24;
     const size_t per_cell = 2 * 4 + 5 * 4;
     return cap * per_atom + (size_t)ncell * per_cell + 64 * 1024;
 }
@@ -467,12 +480,13 @@ extern "C" int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner)
         dfree(s, (void *)g.erhoDD); dfree(s, (void *)g.ephi); dfree(s, (void *)g.ephiDD);
         dfree(s, (void *)g.pk_rho); dfree(s, (void *)g.pk_phi); dfree(s, (void *)g.pk_F);
         dfree(s, (void *)g.pkf_rho); dfree(s, (void *)g.pkf_phi); dfree(s, (void *)g.pkf_F);
-        dfree(s, (void *)g.pkf_pr);
+        dfree(s, (void *)g.pkf_pr); dfree(s, (void *)g.pkd_rho); dfree(s, (void *)g.pkd_phi);
     }
     const Geo &o = owner->g;
     g.eF = o.eF; g.eFDD = o.eFDD; g.erho = o.erho; g.erhoDD = o.erhoDD; g.ephi = o.ephi; g.ephiDD = o.ephiDD;
     g.pk_rho = o.pk_rho; g.pk_phi = o.pk_phi; g.pk_F = o.pk_F;
     g.pkf_rho = o.pkf_rho; g.pkf_phi = o.pkf_phi; g.pkf_F = o.pkf_F; g.pkf_pr = o.pkf_pr;
+    g.pkd_rho = o.pkd_rho; g.pkd_phi = o.pkd_phi;
     g.nelem = o.nelem; g.Nrho = o.Nrho; g.Nr2 = o.Nr2; g.drho = o.drho; g.dr2 = o.dr2;
     g.inv_dr2 = o.inv_dr2; g.inv_drho = o.inv_drho;
     s->eam_borrowed = true;
@@ -555,6 +569,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         c.take(g.bnewidx, cap); c.take(g.dep_count, 4 * (size_t)ncell); c.take(g.arr_base, (size_t)ncell + 1);
         c.take(g.bucket, cap); c.take(g.arr_slot, cap);
         c.take(g.fpf, cap); c.take(g.xf4, cap); c.take(g.nbr, (size_t)cap * maxnb); c.take(g.nbr_count, cap);
+        c.take(g.xlo4, cap); c.take(g.fpdf, cap);
         c.take(g.partials, (size_t)nb * 9 + 8);
         if (g.skin_on)
         {

@@ -29,14 +29,18 @@
 // by default, and boxes too small for a skin list); packed systems and
 // mixed-precision single systems use the skin-list kernels (fmdg_skin.cu).
 //
-// Precision modes.  FMDG_PREC_FP64: every pair quantity in binary64, the
-// binary32 list only prunes (its margin keeps every pair within the cutoff).
-// FMDG_PREC_MIXED: pair geometry from the binary32 cell-local coordinates,
-// pair/spline/embedding arithmetic in binary32, forces and energies summed
-// in binary64 (binary32 partial sums of at most 8 pair terms are added to
-// binary64 accumulators, every 8 list entries so a warp's lanes flush
-// together).  Pairs within 1e-4 relative of a cutoff are
-// re-tested in binary64 so both modes include exactly the same pairs.
+// Precision modes.  FMDG_PREC_FP64: every pair quantity to binary64
+// accuracy, the binary32 list only prunes (its margin keeps every pair
+// within the cutoff).  LJ, Morse and hybrid pairs are evaluated in binary64;
+// EAM pairs in double-float arithmetic (fmdg_df.cuh: about 48 significant
+// bits on the binary32 pipe, GB300's binary64 rate being 1/64 of it) from
+// double-float cell-local coordinates and tables, with cutoff decisions
+// within 1e-6 relative of the cutoff taken from the reference's binary64
+// geometry.  FMDG_PREC_MIXED: pair geometry from the binary32 cell-local
+// coordinates, pair/spline/embedding arithmetic in binary32, binary32
+// partial sums of at most 8 pair terms accumulated as a TwoSum pair and
+// converted to binary64 per atom.  Pairs within 1e-4 relative of a cutoff
+// are re-tested in binary64 so both modes include exactly the same pairs.
 #include "fmdg_pairs.cuh"
 
 namespace {
@@ -122,6 +126,64 @@ __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i,
     return geom64(g, S, xi, ci, j, code).r2 < rc2;
 }
 
+// double-float pair geometry (binary64 mode, EAM) from the cell-local
+// coordinates hi (xf4) + lo (xlo4): rv = x_i - x_j - offset * cellh, the
+// image shift of a periodic neighbour being offset * cellh in the cell
+// frame; r^2 from exact squares of the hi parts.  Agrees with the
+// reference's binary64 geometry to about 1e-14 relative.
+struct GeomDF { dfl rv[3]; dfl r2; };
+
+__device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, float4 jl4, int code,
+                                          const float2 (&ch)[3])
+{
+    const int o[3] = {off_x(code), off_y(code), off_z(code)};
+    const float ih[3] = {ih4.x, ih4.y, ih4.z}, il[3] = {il4.x, il4.y, il4.z};
+    const float jh[3] = {jh4.x, jh4.y, jh4.z}, jl[3] = {jl4.x, jl4.y, jl4.z};
+    GeomDF p;
+    for (int d = 0; d < 3; d++)
+    {
+        const float oh = (float)o[d] * ch[d].x, ol = (float)o[d] * ch[d].y;
+        const dfl a = two_sum(ih[d], -jh[d]);
+        const dfl b = two_sum(a.hi, -oh);
+        const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(il[d], jl[d]), ol), a.lo), b.lo);
+        p.rv[d] = fast_two_sum(b.hi, lo);
+    }
+    const dfl s0 = two_prod(p.rv[0].hi, p.rv[0].hi), s1 = two_prod(p.rv[1].hi, p.rv[1].hi);
+    const dfl s2 = two_prod(p.rv[2].hi, p.rv[2].hi);
+    const dfl t = two_sum(s0.hi, s1.hi);
+    const dfl u = two_sum(t.hi, s2.hi);
+    float cross = __fmul_rn(p.rv[0].hi, p.rv[0].lo);
+    cross = __fmaf_rn(p.rv[1].hi, p.rv[1].lo, cross);
+    cross = __fmaf_rn(p.rv[2].hi, p.rv[2].lo, cross);
+    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(s0.lo, s1.lo), __fadd_rn(s2.lo, t.lo)),
+                               __fadd_rn(u.lo, __fmul_rn(2.f, cross)));
+    p.r2 = fast_two_sum(u.hi, lo);
+    return p;
+}
+
+// interval k = min(floor(q), kmax) and fraction b = q - k of a double-float
+// table coordinate q >= 0
+__device__ __forceinline__ int df_table_index(dfl q, float kmax, dfl &b)
+{
+    float kf = floorf(q.hi);
+    if (kf == q.hi && q.lo < 0.f) kf -= 1.f;
+    kf = fminf(kf, kmax);
+    b = fast_two_sum(__fsub_rn(q.hi, kf), q.lo);
+    return (int)kf;
+}
+
+// binary64 cutoff decision from the double-float r^2: within 1e-6 relative
+// of the cutoff it is taken from the reference's binary64 geometry
+__device__ __forceinline__ bool within_cut_df(const Geo &g, const Side &S, int i, CellXYZ ci, int j, int code,
+                                              dfl r2, float rc2f, double rc2)
+{
+    const float d = __fsub_rn(r2.hi, rc2f);
+    if (fabsf(d) > 1e-6f * rc2f) return d < 0.f;
+    const int cap = g.cap;
+    const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
+    return geom64(g, S, xi, ci, j, code).r2 < rc2;
+}
+
 // ---------------------------------------------------------------- kernels
 
 template <class L>
@@ -136,10 +198,15 @@ __global__ void k_prep_local(__grid_constant__ const L loc)
     const Side S = g.side[dyn->cur];
     const CellXYZ c = cell_xyz(g, S.cell_of[i]);
     const int cap = g.cap;
-    const float lx = (float)(S.x[i] - c.x * g.cellh[0]);
-    const float ly = (float)(S.x[cap + i] - c.y * g.cellh[1]);
-    const float lz = (float)(S.x[2 * (size_t)cap + i] - c.z * g.cellh[2]);
+    const double ux = S.x[i] - c.x * g.cellh[0];
+    const double uy = S.x[cap + i] - c.y * g.cellh[1];
+    const double uz = S.x[2 * (size_t)cap + i] - c.z * g.cellh[2];
+    const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
     g.xf4[i] = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
+    // binary64 mode: the remainders, so that xf4 + xlo4 is the double-float
+    // cell-local position
+    if (g.prec == FMDG_PREC_FP64)
+        g.xlo4[i] = make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
 }
 
 template <class L>
@@ -227,7 +294,31 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
             const int nk = g.nkinds;
             const int nint = g.Nr2 - 1;
-            if (!MIXED)
+            if (!MIXED && !HYBRID)
+            {
+                // double-float pair arithmetic (fmdg_df.cuh)
+                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                const dfl inv_h = df_of(df_split(g.inv_dr2));
+                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
+                const float kmax = (float)(nint - 1);
+                dfl acc_rho = {0.f, 0.f};
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 jh = g.xf4[j];
+                    const int pidx = ki * nk + __float_as_int(jh.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    if (within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2]))
+                    {
+                        dfl b;
+                        const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
+                        const float4 *row = g.pkd_rho + 2 * ((size_t)pp.jloc * nint + ir2);
+                        acc_rho = df_add(acc_rho, df_spl_val(row[0], row[1], b));
+                    }
+                });
+                rho = df_to_double(acc_rho);
+            }
+            else if (!MIXED)
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double inv_h = g.inv_dr2;
@@ -282,7 +373,9 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             {
                 const double b = qr - irho;
                 const double4_32a t = g.pk_F[(size_t)ei * nrint + irho];
-                g.vaream[i] = spl_der(t, b, g.inv_drho);
+                const double fp = spl_der(t, b, g.inv_drho);
+                g.vaream[i] = fp;
+                if (!HYBRID) g.fpdf[i] = df_split(fp);
                 acc[0] = spl_val(t, b);
             }
             else
@@ -299,6 +392,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
         {
             g.vaream[i] = 0.0;
             if (MIXED) g.fpf[i] = 0.f;
+            else g.fpdf[i] = make_float2(0.f, 0.f);
         }
     }
     block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
@@ -341,7 +435,45 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
             const int nk = g.nkinds;
             const int nint = g.Nr2 - 1;
             const size_t ne = g.nelem;
-            if (!MIXED)
+            if (!MIXED && CAT == CAT_EAM)
+            {
+                // double-float pair arithmetic (fmdg_df.cuh); the forces
+                // and energy as the binary64 branch below forms them
+                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                const dfl fpi = df_of(g.fpdf[i]);
+                const dfl inv_h = df_of(df_split(g.inv_dr2));
+                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
+                const float kmax = (float)(nint - 1);
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 jh = g.xf4[j];
+                    const int pidx = ki * nk + __float_as_int(jh.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2])) return;
+                    dfl b;
+                    const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
+                    const int ei = pp.iloc, ej = pp.jloc;
+                    const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
+                    const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
+                    const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
+                    const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
+                    dfl rho_jp = rho_ip;
+                    if (ei != ej)
+                    {
+                        const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
+                        rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
+                    }
+                    const dfl fpj = df_of(g.fpdf[j]);
+                    const dfl mag = df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fpj, rho_ip)), phi_d), 2.f);
+                    for (int d = 0; d < 3; d++) fs[d] = df_sub(fs[d], df_mul(mag, p.rv[d]));
+                    pes = df_add(pes, df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f));
+                });
+                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
+                pe = df_to_double(pes);
+            }
+            else if (!MIXED)
             {
                 const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
                 const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;

@@ -80,6 +80,12 @@ struct Geo   // passed by value to kernels
     const double4_32a *pk_rho, *pk_phi, *pk_F;     // binary64
     const float4 *pkf_rho, *pkf_phi, *pkf_F;   // binary32 copies (mixed mode)
     const float4 *pkf_pr;       // per element e and interval k: {phi_ee, rho_e} side by side (one 32 B row)
+    // binary64 mode, EAM: double-float forms (fmdg_df.cuh) of the tables
+    // (per interval {hi coefficients, lo coefficients}), of the cell-local
+    // coordinates (lo parts beside xf4) and of F'(rho)
+    const float4 *pkd_rho, *pkd_phi;
+    float4 *xlo4;
+    float2 *fpdf;
     double inv_dr2, inv_drho;
     // binning scratch
     int *bdest;        // destination interior cell, -1 deleted, -2 stays

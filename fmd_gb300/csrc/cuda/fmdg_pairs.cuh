@@ -5,6 +5,7 @@
 #pragma once
 
 #include "fmdg_internal.cuh"
+#include "fmdg_df.cuh"
 
 namespace {
 
