@@ -86,6 +86,47 @@ __device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mu
 
 __device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
 
+// 1 / a: binary32 reciprocal y0, then one Newton step y0 + y0 (1 - a y0)
+// evaluated in double-float (the residual doubles the precision)
+__device__ __forceinline__ dfl df_rcp(dfl a)
+{
+    const float y0 = __frcp_rn(a.hi);
+    const dfl e = df_sub({1.f, 0.f}, df_mul_f(a, y0));
+    return df_add({y0, 0.f}, df_mul_f(e, y0));
+}
+
+// sqrt(a), a > 0: binary32 root r0 = a * rsqrt(a), then one Newton step
+// r0 + (a - r0^2) / (2 r0) with the residual in double-float
+__device__ __forceinline__ dfl df_sqrt(dfl a)
+{
+    const float y0 = __frsqrt_rn(a.hi);
+    const float r0 = __fmul_rn(a.hi, y0);
+    const dfl res = df_sub(a, two_prod(r0, r0));
+    return df_add({r0, 0.f}, df_mul_f(res, __fmul_rn(0.5f, y0)));
+}
+
+// exp(x) for |x| < 80 (the double-double method of Hida, Li and Bailey):
+// x = n ln2 + t with |t| <= ln2/2, exp(t) = (exp(t / 32))^32, the inner
+// exponential by its Taylor series to degree 8 (|t / 32| < 0.011, truncation
+// below 1e-23), five squarings, then the exact scaling by 2^n.  Relative
+// error about 32 x 2^-47.
+__device__ __forceinline__ dfl df_exp(dfl x)
+{
+    // ln2 and 1/k! (k = 2..8) as double-float constants
+    const dfl ln2 = {6.931471825e-01f, -1.904654212e-09f};
+    const dfl c[9] = {{1.f, 0.f}, {1.f, 0.f}, {0.5f, 0.f},
+                      {1.666666716e-01f, -4.967053879e-09f}, {4.166666791e-02f, -1.241763470e-09f},
+                      {8.333333768e-03f, -4.346172033e-10f}, {1.388888923e-03f, -3.363109444e-11f},
+                      {1.984127011e-04f, -2.725596875e-12f}, {2.480158764e-05f, -3.406996094e-13f}};
+    const float n = rintf(__fmul_rn(x.hi, 1.442695041f));
+    const dfl t = df_scale2(df_sub(x, df_mul_f(ln2, n)), 0.03125f);
+    dfl p = c[8];
+    for (int k = 7; k >= 0; k--) p = df_fma(p, t, c[k]);
+    for (int k = 0; k < 5; k++) p = df_mul(p, p);
+    const int e = (int)n;
+    return {ldexpf(p.hi, e), ldexpf(p.lo, e)};
+}
+
 // nearest double-float of a binary64 number (hi = x rounded to binary32,
 // lo = the rounded remainder)
 __host__ __device__ __forceinline__ float2 df_split(double x)

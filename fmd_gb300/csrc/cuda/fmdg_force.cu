@@ -435,7 +435,60 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
             const int nk = g.nkinds;
             const int nint = g.Nr2 - 1;
             const size_t ne = g.nelem;
-            if (!MIXED && CAT == CAT_EAM)
+            if (!MIXED && CAT == CAT_LJ)
+            {
+                // double-float pair arithmetic (fmdg_df.cuh) in the
+                // reference's formula (src/lj.h:35-56)
+                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 jh = g.xf4[j];
+                    const int pidx = ki * nk + __float_as_int(jh.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2])) return;
+                    const dfl eps4 = df_of(sp.pd[pidx][0]), sig2 = df_of(sp.pd[pidx][1]);
+                    const dfl inv_r2 = df_rcp(p.r2);
+                    const dfl s2 = df_mul(sig2, inv_r2);
+                    const dfl s6 = df_mul(df_mul(s2, s2), s2);
+                    const dfl s12 = df_mul(s6, s6);
+                    const dfl factor = df_mul(df_mul(df_mul_f(eps4, 12.f), inv_r2),
+                                              df_sub(s12, df_scale2(s6, 0.5f)));
+                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(p.rv[d], factor));
+                    pes = df_add(pes, df_scale2(df_mul(eps4, df_sub(s12, s6)), 0.5f));
+                });
+                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
+                pe = df_to_double(pes);
+            }
+            else if (!MIXED && CAT == CAT_MORSE)
+            {
+                // double-float pair arithmetic (fmdg_df.cuh) in the
+                // reference's formula (src/morse.h:35-56)
+                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                for_each_pair(g, S, i, ci, [&](int j, int code) {
+                    if (group >= 0 && S.group[j] != group) return;
+                    const float4 jh = g.xf4[j];
+                    const int pidx = ki * nk + __float_as_int(jh.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][3], pp.p[3])) return;
+                    const dfl D0 = df_of(sp.pd[pidx][0]), al = df_of(sp.pd[pidx][1]), r0 = df_of(sp.pd[pidx][2]);
+                    const dfl r = df_sqrt(p.r2);
+                    const dfl inv_r = df_rcp(r);
+                    const dfl e1 = df_exp(df_mul(df_neg(al), df_sub(r, r0)));
+                    const dfl e2 = df_mul(e1, e1);
+                    const dfl factor = df_mul(df_mul(df_scale2(df_mul(al, D0), 2.f), inv_r), df_sub(e2, e1));
+                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(factor, p.rv[d]));
+                    pes = df_add(pes, df_scale2(df_mul(D0, df_sub(e2, df_scale2(e1, 2.f))), 0.5f));
+                });
+                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
+                pe = df_to_double(pes);
+            }
+            else if (!MIXED && CAT == CAT_EAM)
             {
                 // double-float pair arithmetic (fmdg_df.cuh); the forces
                 // and energy as the binary64 branch below forms them

@@ -15,6 +15,7 @@ struct SmemPot
 {
     fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
     float pf[FMDG_MAXK * FMDG_MAXK][4];
+    float2 pd[FMDG_MAXK * FMDG_MAXK][4];   // double-float parameters (binary64 mode)
     double mass[FMDG_MAXK];
     double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
@@ -27,7 +28,11 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
     for (int k = threadIdx.x; k < nk2; k += blockDim.x)
     {
         sp.pairs[k] = g.pairs[k];
-        for (int q = 0; q < 4; q++) sp.pf[k][q] = (float)g.pairs[k].p[q];
+        for (int q = 0; q < 4; q++)
+        {
+            sp.pf[k][q] = (float)g.pairs[k].p[q];
+            sp.pd[k][q] = df_split(g.pairs[k].p[q]);
+        }
     }
     for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
     {
