@@ -280,7 +280,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];
-    const int cap = g.cap;
     const int i = bx * blockDim.x + threadIdx.x;
     double acc[1] = {0.0};
     if (i < n)
@@ -294,7 +293,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
             const int nk = g.nkinds;
             const int nint = g.Nr2 - 1;
-            if (!MIXED && !HYBRID)
+            if (!MIXED)
             {
                 // double-float pair arithmetic (fmdg_df.cuh)
                 const float4 ih = g.xf4[i], il = g.xlo4[i];
@@ -307,6 +306,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     const float4 jh = g.xf4[j];
                     const int pidx = ki * nk + __float_as_int(jh.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
+                    if (HYBRID && pp.cat != FMDG_POT_EAM) return;
                     const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
                     if (within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2]))
                     {
@@ -317,23 +317,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     }
                 });
                 rho = df_to_double(acc_rho);
-            }
-            else if (!MIXED)
-            {
-                const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
-                const double inv_h = g.inv_dr2;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
-                    if (group >= 0 && S.group[j] != group) return;
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
-                    if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                    const Geom64 p = geom64(g, S, xi, ci, j, code);
-                    if (p.r2 < pp.p[2])
-                    {
-                        const double q = p.r2 * inv_h;
-                        const int ir2 = min((int)q, nint - 1);
-                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], q - ir2);
-                    }
-                });
             }
             else
             {
@@ -375,7 +358,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                 const double4_32a t = g.pk_F[(size_t)ei * nrint + irho];
                 const double fp = spl_der(t, b, g.inv_drho);
                 g.vaream[i] = fp;
-                if (!HYBRID) g.fpdf[i] = df_split(fp);
+                g.fpdf[i] = df_split(fp);
                 acc[0] = spl_val(t, b);
             }
             else
@@ -435,67 +418,16 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
             const int nk = g.nkinds;
             const int nint = g.Nr2 - 1;
             const size_t ne = g.nelem;
-            if (!MIXED && CAT == CAT_LJ)
+            if (!MIXED)
             {
-                // double-float pair arithmetic (fmdg_df.cuh) in the
-                // reference's formula (src/lj.h:35-56)
+                // binary64 mode: double-float pair arithmetic (fmdg_df.cuh)
+                // in the reference's formulas -- LJ src/lj.h:35-56, Morse
+                // src/morse.h:35-56, EAM src/eam.h:186-226 -- the category
+                // chosen per pair for hybrid tables (src/forces.c:33-290)
                 const float4 ih = g.xf4[i], il = g.xlo4[i];
                 const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
-                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
-                    if (group >= 0 && S.group[j] != group) return;
-                    const float4 jh = g.xf4[j];
-                    const int pidx = ki * nk + __float_as_int(jh.w);
-                    const fmdg_pair_t &pp = sp.pairs[pidx];
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
-                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2])) return;
-                    const dfl eps4 = df_of(sp.pd[pidx][0]), sig2 = df_of(sp.pd[pidx][1]);
-                    const dfl inv_r2 = df_rcp(p.r2);
-                    const dfl s2 = df_mul(sig2, inv_r2);
-                    const dfl s6 = df_mul(df_mul(s2, s2), s2);
-                    const dfl s12 = df_mul(s6, s6);
-                    const dfl factor = df_mul(df_mul(df_mul_f(eps4, 12.f), inv_r2),
-                                              df_sub(s12, df_scale2(s6, 0.5f)));
-                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(p.rv[d], factor));
-                    pes = df_add(pes, df_scale2(df_mul(eps4, df_sub(s12, s6)), 0.5f));
-                });
-                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
-                pe = df_to_double(pes);
-            }
-            else if (!MIXED && CAT == CAT_MORSE)
-            {
-                // double-float pair arithmetic (fmdg_df.cuh) in the
-                // reference's formula (src/morse.h:35-56)
-                const float4 ih = g.xf4[i], il = g.xlo4[i];
-                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
-                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
-                    if (group >= 0 && S.group[j] != group) return;
-                    const float4 jh = g.xf4[j];
-                    const int pidx = ki * nk + __float_as_int(jh.w);
-                    const fmdg_pair_t &pp = sp.pairs[pidx];
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
-                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][3], pp.p[3])) return;
-                    const dfl D0 = df_of(sp.pd[pidx][0]), al = df_of(sp.pd[pidx][1]), r0 = df_of(sp.pd[pidx][2]);
-                    const dfl r = df_sqrt(p.r2);
-                    const dfl inv_r = df_rcp(r);
-                    const dfl e1 = df_exp(df_mul(df_neg(al), df_sub(r, r0)));
-                    const dfl e2 = df_mul(e1, e1);
-                    const dfl factor = df_mul(df_mul(df_scale2(df_mul(al, D0), 2.f), inv_r), df_sub(e2, e1));
-                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(factor, p.rv[d]));
-                    pes = df_add(pes, df_scale2(df_mul(D0, df_sub(e2, df_scale2(e1, 2.f))), 0.5f));
-                });
-                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
-                pe = df_to_double(pes);
-            }
-            else if (!MIXED && CAT == CAT_EAM)
-            {
-                // double-float pair arithmetic (fmdg_df.cuh); the forces
-                // and energy as the binary64 branch below forms them
-                const float4 ih = g.xf4[i], il = g.xlo4[i];
-                const dfl fpi = df_of(g.fpdf[i]);
+                const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[i]) : dfl{0.f, 0.f};
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
-                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
                 const float kmax = (float)(nint - 1);
                 dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
@@ -503,84 +435,56 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     const float4 jh = g.xf4[j];
                     const int pidx = ki * nk + __float_as_int(jh.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
-                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2])) return;
-                    dfl b;
-                    const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
-                    const int ei = pp.iloc, ej = pp.jloc;
-                    const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
-                    const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
-                    const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
-                    const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
-                    dfl rho_jp = rho_ip;
-                    if (ei != ej)
-                    {
-                        const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
-                        rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
-                    }
-                    const dfl fpj = df_of(g.fpdf[j]);
-                    const dfl mag = df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fpj, rho_ip)), phi_d), 2.f);
-                    for (int d = 0; d < 3; d++) fs[d] = df_sub(fs[d], df_mul(mag, p.rv[d]));
-                    pes = df_add(pes, df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f));
-                });
-                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
-                pe = df_to_double(pes);
-            }
-            else if (!MIXED)
-            {
-                const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
-                const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.vaream[i] : 0.0;
-                const double inv_h = g.inv_dr2;
-                for_each_pair(g, S, i, ci, [&](int j, int code) {
-                    if (group >= 0 && S.group[j] != group) return;
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + S.kind[j]];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
-                    const Geom64 p = geom64(g, S, xi, ci, j, code);
+                    const int rci = (cat == FMDG_POT_MORSE) ? 3 : 2;
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][rci], pp.p[rci])) return;
+                    dfl fa, eh;     // f_i += fa * rv, energy share eh
                     if (cat == FMDG_POT_LJ)
                     {
-                        if (p.r2 < pp.p[2])
-                        {
-                            const double inv_r2 = 1.0 / p.r2;
-                            const double inv_rs2 = pp.p[1] * inv_r2;
-                            const double inv_rs6 = inv_rs2 * inv_rs2 * inv_rs2;
-                            const double inv_rs12 = inv_rs6 * inv_rs6;
-                            const double factor = 12.0 * pp.p[0] * inv_r2 * (inv_rs12 - 0.5 * inv_rs6);
-                            for (int d = 0; d < 3; d++) f[d] += p.rv[d] * factor;
-                            pe += 0.5 * (pp.p[0] * (inv_rs12 - inv_rs6));
-                        }
+                        const dfl eps4 = df_of(sp.pd[pidx][0]), sig2 = df_of(sp.pd[pidx][1]);
+                        const dfl inv_r2 = df_rcp(p.r2);
+                        const dfl s2 = df_mul(sig2, inv_r2);
+                        const dfl s6 = df_mul(df_mul(s2, s2), s2);
+                        const dfl s12 = df_mul(s6, s6);
+                        fa = df_mul(df_mul(df_mul_f(eps4, 12.f), inv_r2), df_sub(s12, df_scale2(s6, 0.5f)));
+                        eh = df_scale2(df_mul(eps4, df_sub(s12, s6)), 0.5f);
                     }
                     else if (cat == FMDG_POT_MORSE)
                     {
-                        if (p.r2 < pp.p[3])
-                        {
-                            const double r = sqrt(p.r2);
-                            const double inv_r = 1.0 / r;
-                            const double e1 = exp(-pp.p[1] * (r - pp.p[2]));
-                            const double e2 = e1 * e1;
-                            const double factor = 2.0 * pp.p[1] * pp.p[0] * inv_r * (e2 - e1);
-                            for (int d = 0; d < 3; d++) f[d] += factor * p.rv[d];
-                            pe += 0.5 * (pp.p[0] * (e2 - 2.0 * e1));
-                        }
+                        const dfl D0 = df_of(sp.pd[pidx][0]), al = df_of(sp.pd[pidx][1]);
+                        const dfl r0 = df_of(sp.pd[pidx][2]);
+                        const dfl r = df_sqrt(p.r2);
+                        const dfl inv_r = df_rcp(r);
+                        const dfl e1 = df_exp(df_mul(df_neg(al), df_sub(r, r0)));
+                        const dfl e2 = df_mul(e1, e1);
+                        fa = df_mul(df_mul(df_scale2(df_mul(al, D0), 2.f), inv_r), df_sub(e2, e1));
+                        eh = df_scale2(df_mul(D0, df_sub(e2, df_scale2(e1, 2.f))), 0.5f);
                     }
-                    else if (cat == FMDG_POT_EAM)
+                    else
                     {
-                        if (p.r2 < pp.p[2])
+                        dfl b;
+                        const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
+                        const int ei = pp.iloc, ej = pp.jloc;
+                        const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
+                        const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
+                        const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
+                        const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
+                        dfl rho_jp = rho_ip;
+                        if (ei != ej)
                         {
-                            const double q = p.r2 * inv_h;
-                            const int ir2 = min((int)q, nint - 1);
-                            const double b = q - ir2;
-                            const int ei = pp.iloc, ej = pp.jloc;
-                            const double4_32a tph = g.pk_phi[((size_t)ei * ne + ej) * nint + ir2];
-                            const double phi_d = spl_der(tph, b, inv_h);
-                            const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], b, inv_h);
-                            const double rho_jp = (ei == ej) ? rho_ip
-                                                : spl_der(g.pk_rho[(size_t)ej * nint + ir2], b, inv_h);
-                            const double mag = 2 * (fpi * rho_jp + g.vaream[j] * rho_ip + phi_d);
-                            for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
-                            pe += 0.5 * spl_val(tph, b);
+                            const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
+                            rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
                         }
+                        const dfl fpj = df_of(g.fpdf[j]);
+                        fa = df_neg(df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fpj, rho_ip)), phi_d), 2.f));
+                        eh = df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f);
                     }
+                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(fa, p.rv[d]));
+                    pes = df_add(pes, eh);
                 });
+                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
+                pe = df_to_double(pes);
             }
             else
             {
