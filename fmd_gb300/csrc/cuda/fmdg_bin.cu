@@ -104,10 +104,10 @@ __global__ void k_bin_classify(__grid_constant__ const L loc, int mode, int lazy
     bool departs = false, outside = false;
     for (int d = 0; d < 3; d++)
     {
-        const double q = floor_div(x[d], g.cellh[d], g.inv_cellh[d]);
+        const int q = cell_floor(x[d], g.cellh[d], g.inv_cellh[d], g.inv_cellh_f[d]);
         // local index including the ghost margin (ic_start = 1)
-        if (!(q >= -1.0 && q <= (double)g.nc[d])) outside = true;
-        jc[d] = outside ? 0 : (int)q + 1;
+        if (!(q >= -1 && q <= g.nc[d])) outside = true;
+        jc[d] = outside ? 0 : q + 1;
         if (jc[d] - 1 != cc[d]) departs = true;
     }
     if (outside)

@@ -264,6 +264,8 @@ extern "C" int fmdg_set_box(fmdg_sys_t *s, const double l[3], const int pbc[3], 
         s->g.nc[d] = nc[d];
         s->g.cellh[d] = cellh[d];
         s->g.inv_cellh[d] = 1.0 / cellh[d];
+        s->g.l_f[d] = (float)l[d];
+        s->g.inv_cellh_f[d] = (float)s->g.inv_cellh[d];
     }
     const long long ncell = (long long)nc[0] * nc[1] * nc[2];
     if (ncell > (1 << 24)) return fmdg_set_error("fmdg_set_box: more than 2^24 cells");
@@ -447,7 +449,7 @@ size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
 {
     const size_t cap = n > 0 ? n : 1;
     const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8 + 24;
-    const size_t per_cell = 2 * 4 + 5 * 4;
+    const size_t per_cell = 2 * 4 + 5 * 4 + 32;
     return cap * per_atom + (size_t)ncell * per_cell + 64 * 1024;
 }
 
@@ -571,6 +573,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         c.take(g.fpf, cap); c.take(g.xf4, cap); c.take(g.nbr, (size_t)cap * maxnb); c.take(g.nbr_count, cap);
         c.take(g.xlo4, cap); c.take(g.fpdf, cap);
         c.take(g.partials, (size_t)nb * 9 + 8);
+        c.take(g.corig, ncell);
         if (g.skin_on)
         {
             c.take(g.pos, cap); c.take(g.cb, cap); c.take(g.xl, cap); c.take(g.xb, cap);
@@ -593,6 +596,8 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         for (int k = 0; k < cap; k++) iota[k] = k;
         FMDG_CK(cudaMemcpyAsync(g.side[0].slot, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice, st));
         FMDG_CK(cudaMemcpyAsync(g.pos, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice, st));
+        // build cells: valid cell indexes before the first build writes them
+        FMDG_CK(cudaMemsetAsync(g.cb, 0, (size_t)cap * 4, st));
         const double rsk = sqrt(rc2max) + g.skin;
         g.rskin2 = (float)(rsk * rsk);
         g.half_skin2 = (float)(0.25 * g.skin * g.skin);
@@ -619,6 +624,16 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         FMDG_CK(cudaMemcpyAsync(S.cell_of, cell_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
     }
     FMDG_CK(cudaMemcpyAsync(S.cell_start, start.data(), ((size_t)ncell + 1) * 4, cudaMemcpyHostToDevice, st));
+    // cell origins (c * cellh per axis, the binary64 products the kernels
+    // would form)
+    std::vector<double4_32a> corig(ncell);
+    for (int c = 0; c < ncell; c++)
+    {
+        const int cx = c / (g.nc[1] * g.nc[2]), cy = (c / g.nc[2]) % g.nc[1], cz = c % g.nc[2];
+        corig[c] = make_double4_32a(cx * g.cellh[0], cy * g.cellh[1], cz * g.cellh[2], 0.0);
+    }
+    FMDG_CK(cudaMemcpyAsync((void *)g.corig, corig.data(), (size_t)ncell * sizeof(double4_32a),
+                            cudaMemcpyHostToDevice, st));
     FMDG_CK(cudaMemsetAsync(g.F, 0, 3 * (size_t)cap * 8, st));
     FMDG_CK(cudaMemsetAsync(g.vaream, 0, (size_t)cap * 8, st));
     const double keep_time = d.time, keep_dt = d.dt;

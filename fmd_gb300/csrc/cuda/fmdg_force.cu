@@ -196,11 +196,11 @@ __global__ void k_prep_local(__grid_constant__ const L loc)
     const int i = bx * blockDim.x + threadIdx.x;
     if (i >= dyn->n) return;
     const Side S = g.side[dyn->cur];
-    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
+    const double4_32a oc = g.corig[S.cell_of[i]];
     const int cap = g.cap;
-    const double ux = S.x[i] - c.x * g.cellh[0];
-    const double uy = S.x[cap + i] - c.y * g.cellh[1];
-    const double uz = S.x[2 * (size_t)cap + i] - c.z * g.cellh[2];
+    const double ux = S.x[i] - oc.x;
+    const double uy = S.x[cap + i] - oc.y;
+    const double uz = S.x[2 * (size_t)cap + i] - oc.z;
     const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
     g.xf4[i] = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
     // binary64 mode: the remainders, so that xf4 + xlo4 is the double-float

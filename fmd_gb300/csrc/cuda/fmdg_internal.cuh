@@ -66,6 +66,8 @@ struct Geo   // passed by value to kernels
     int nc[3];
     int pbc[3];
     double l[3], cellh[3], inv_cellh[3];
+    float l_f[3], inv_cellh_f[3];   // binary32 copies (fast paths with binary64 fallbacks)
+    const double4_32a *corig;       // per cell: origin (cx, cy, cz) * cellh in binary64
     Side side[2];
     double *F, *vaream;
     float *fpf;        // binary32 copy of F'(rho) (mixed-precision EAM force pass)
@@ -299,4 +301,20 @@ __device__ __forceinline__ double floor_div(double x, double h, double inv_h)
     const double tol = 1e-9 * fmax(1.0, fabs(q));
     if (q - f < tol || (f + 1.0) - q < tol) return floor(__ddiv_rn(x, h));
     return f;
+}
+
+// floor_div as an int, through a binary32 estimate when its fraction is
+// clear of an integer by more than its error (then both agree; one binary64
+// instruction instead of a dozen -- binary64 issues at 1/64 of the binary32
+// rate on GB300), else in binary64.  Results below -2 or above 2^30 come
+// back as -2 (callers test against [-1, nc]).
+__device__ __forceinline__ int cell_floor(double x, double h, double inv_h, float inv_hf)
+{
+    const float qf = __fmul_rn((float)x, inv_hf);
+    const float ff = floorf(qf);
+    const float fr = __fsub_rn(qf, ff);
+    const float m = 4e-7f * (fabsf(qf) + 1.f);
+    if (fr > m && fr < 1.f - m && fabsf(qf) < 1.0e6f) return (int)ff;
+    const double q = floor_div(x, h, inv_h);
+    return (q >= -2.0 && q <= 1073741824.0) ? (int)q : -2;
 }

@@ -223,18 +223,21 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
 // build position: sets the rebuild flag beyond skin/2.
 __device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, const double (&x)[3], float kb)
 {
-    const CellXYZ b = cell_xyz(g, g.cb[t]);
-    const int b3[3] = {b.x, b.y, b.z};
+    const double4_32a ob = g.corig[g.cb[t]];
+    const double o3[3] = {ob.x, ob.y, ob.z};
     float l3[3];
     for (int d = 0; d < 3; d++)
     {
-        double u = x[d] - b3[d] * g.cellh[d];
-        if (g.pbc[d])
+        double u = x[d] - o3[d];
+        float uf = (float)u;
+        // unwrap across a periodic face (binary64 test near half a box)
+        if (g.pbc[d] && fabsf(uf) > 0.49f * g.l_f[d])
         {
             if (u > 0.5 * g.l[d]) u -= g.l[d];
             else if (u < -0.5 * g.l[d]) u += g.l[d];
+            uf = (float)u;
         }
-        l3[d] = (float)u;
+        l3[d] = uf;
     }
     g.xl[t] = make_float4(l3[0], l3[1], l3[2], kb);
     const float4 o = g.xb[t];
@@ -281,7 +284,7 @@ __global__ void k_skin_start(__grid_constant__ const L loc)
         }
     }
     const int t = S.slot[i];
-    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
+    g.xd[t] = make_double4_32a(x[0], x[1], x[2], 0.0);
     slot_rel_build(g, dyn, t, x, __int_as_float(kind));
 }
 
@@ -312,15 +315,14 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     const int kind = (int)S.kind[i];
     const float kb = __int_as_float(kind);
     g.pos[t] = i;
-    g.xd[t] = make_double4_32a(x[0], x[1], x[2], (double)kind);
+    g.xd[t] = make_double4_32a(x[0], x[1], x[2], 0.0);
     g.gslot[t] = S.group[i];
     // relative to the current cell (a rebuild starts from these)
-    const CellXYZ c = cell_xyz(g, S.cell_of[i]);
-    g.xf4[i] = make_float4((float)(x[0] - c.x * g.cellh[0]), (float)(x[1] - c.y * g.cellh[1]),
-                           (float)(x[2] - c.z * g.cellh[2]), kb);
-    // (renumbered: the build cell and position of slot t are rewritten by
-    // the list build that follows)
-    if (!lazy) slot_rel_build(g, dyn, t, x, kb);
+    const double4_32a oc = g.corig[S.cell_of[i]];
+    g.xf4[i] = make_float4((float)(x[0] - oc.x), (float)(x[1] - oc.y), (float)(x[2] - oc.z), kb);
+    // (renumbered, or a rebuild already due: the build cell and position of
+    // slot t are rewritten by the list build that follows)
+    if (!lazy && !dyn->rebuild) slot_rel_build(g, dyn, t, x, kb);
 }
 
 // one thread per slot; every block leaves at once when no rebuild is due
@@ -408,10 +410,10 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             {
                 const double4_32a xdi = g.xd[t];
                 const double inv_h = g.inv_dr2;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4, float4) {
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4) {
                     if (group >= 0 && g.gslot[js] != group) return;
                     const double4_32a xj = g.xd[js];
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + __float_as_int(xjf.w)];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
                     const Geom64 p = geom64_mi(g, xdi, xj);
                     if (p.r2 < pp.p[2])
@@ -575,10 +577,10 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 const double4_32a xdi = g.xd[t];
                 const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpd[t] : 0.0;
                 const double inv_h = g.inv_dr2;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4, float4) {
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4) {
                     if (group >= 0 && g.gslot[js] != group) return;
                     const double4_32a xj = g.xd[js];
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + (int)xj.w];
+                    const fmdg_pair_t &pp = sp.pairs[ki * nk + __float_as_int(xjf.w)];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
                     const Geom64 p = geom64_mi(g, xdi, xj);
                     if (cat == FMDG_POT_LJ && p.r2 < pp.p[2])
