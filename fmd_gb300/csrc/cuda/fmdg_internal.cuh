@@ -233,6 +233,13 @@ __device__ __forceinline__ const Geo &loc_geo(const LocPack &L, int &bx, int &nb
 
 __device__ __forceinline__ bool loc_idle(const LocOne &, const Geo &) { return false; }
 __device__ __forceinline__ bool loc_idle(const LocPack &, const Geo &g) { return g.dyn->steps_left <= 0; }
+// does this step produce a thermo record?  Single systems: every step (the
+// fmd.h API reads it at any time).  Packed (served) systems report theirs
+// only after their last step, so only that step forms energies, kinetic
+// energy and momentum (uniform over a system's blocks: steps_left changes
+// only after the last of them has finished)
+__device__ __forceinline__ bool loc_thermo(const LocOne &, const Geo &) { return true; }
+__device__ __forceinline__ bool loc_thermo(const LocPack &, const Geo &g) { return g.dyn->steps_left <= 1; }
 
 // A pack: systems of one pair-category class and precision stepped
 // together; one locator per block shape (its grid is bstart[nsys]).

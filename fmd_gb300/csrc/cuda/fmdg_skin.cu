@@ -37,6 +37,8 @@
 // Pair arithmetic and precision modes are those of the per-step kernels
 // (fmdg_force.cu); the lean variants (one kind, no group) are described at
 // k_force_skin.
+#include <type_traits>
+
 #include "fmdg_pairs.cuh"
 
 namespace {
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             g.fpb[t] = 0.f;
         }
     }
-    block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
+    if (loc_thermo(loc, g)) block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
 }
 
 // Pair forces + velocity-Verlet finish step (src/integrators.c:94-126) and
@@ -558,6 +560,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
     const int t = bx * blockDim.x + threadIdx.x;
+    const bool thermo = loc_thermo(loc, g);
     double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const int i = (t < cap) ? g.pos[t] : -1;
     if (i >= 0)
@@ -649,92 +652,105 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         e = 0.5f * (pq.x * (e2 - 2.f * e1));
                     }
                 };
-                Acc32<4> ac;
-                if constexpr (CAT == CAT_EAM)
-                {
-                    const float band = 1e-4f * rc2f;
-                    for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                        const float3 rv = rv_of(xi, xj, o);
-                        const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                        bool in = r2 < rc2f;
-                        if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
-                        if (!in) return;
-                        float b;
-                        const int ir2 = table_index(r2 * inv_h, kmax, b);
-                        const float4 tph = tpr[2 * ir2], trh = tpr[2 * ir2 + 1];
-                        const float phi_d = spl_der(tph, b, inv_h);
-                        const float rho_d = spl_der(trh, b, inv_h);
-                        const float fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
-                        ac.part[0] += fa * rv.x;
-                        ac.part[1] += fa * rv.y;
-                        ac.part[2] += fa * rv.z;
-                        ac.part[3] += 0.5f * spl_val(tph, b);
-                    }, [&](int k) { ac.entries(k); });
-                    ac.flush();
-                }
-                else
-                {
-                    // Branch-free walk: the arithmetic runs for every entry and
-                    // entries beyond the cutoff add zero.  An entry within
-                    // 2e-5 relative of the cutoff (several times the binary32
-                    // error of r^2) is decided in binary64 after the walk: one
-                    // such entry per atom is kept in registers, more (rare)
-                    // send the atom through a second walk over its near
-                    // entries only.
-                    const float band = 2e-5f * rc2f;
-                    int npend = 0, pend = 0;
-                    float3 prv = make_float3(0.f, 0.f, 0.f);
-                    for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                        const float3 rv = rv_of(xi, xj, o);
-                        const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                        const bool near = fabsf(r2 - rc2f) <= band;
-                        const bool in = (r2 < rc2f) && !near;
-                        npend += near;
-                        pend = near ? js : pend;
-                        prv = near ? rv : prv;
-                        float fa, e;
-                        pair_lm(r2, fa, e);
-                        fa = in ? fa : 0.f;
-                        e = in ? e : 0.f;
-                        ac.part[0] += fa * rv.x;
-                        ac.part[1] += fa * rv.y;
-                        ac.part[2] += fa * rv.z;
-                        ac.part[3] += e;
-                    }, [&](int k) { ac.entries(k); });
-                    ac.flush();
-                    if (npend == 1)
+                // E: this step forms the energy (thermo record); otherwise the
+                // energy terms are dropped from the walk
+                auto walk = [&](auto with_e) {
+                    constexpr bool E = decltype(with_e)::value;
+                    Acc32<E ? 4 : 3> ac;
+                    if constexpr (CAT == CAT_EAM)
                     {
-                        if (geom64_mi(g, g.xd[t], g.xd[pend]).r2 < rc2)
-                        {
-                            const float r2 = prv.x * prv.x + prv.y * prv.y + prv.z * prv.z;
-                            float fa, e;
-                            pair_lm(r2, fa, e);
-                            ac.part[0] += fa * prv.x;
-                            ac.part[1] += fa * prv.y;
-                            ac.part[2] += fa * prv.z;
-                            ac.part[3] += e;
-                            ac.flush();
-                        }
-                    }
-                    else if (npend > 1)
-                    {
+                        const float band = 1e-4f * rc2f;
                         for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                             const float3 rv = rv_of(xi, xj, o);
                             const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
-                            if (!(fabsf(r2 - rc2f) <= band)) return;
-                            if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
-                            float fa, e;
-                            pair_lm(r2, fa, e);
+                            bool in = r2 < rc2f;
+                            if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
+                            if (!in) return;
+                            float b;
+                            const int ir2 = table_index(r2 * inv_h, kmax, b);
+                            const float4 tph = tpr[2 * ir2], trh = tpr[2 * ir2 + 1];
+                            const float phi_d = spl_der(tph, b, inv_h);
+                            const float rho_d = spl_der(trh, b, inv_h);
+                            const float fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
                             ac.part[0] += fa * rv.x;
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
-                            ac.part[3] += e;
+                            if constexpr (E) ac.part[3] += 0.5f * spl_val(tph, b);
                         }, [&](int k) { ac.entries(k); });
                         ac.flush();
                     }
-                }
-                for (int d = 0; d < 3; d++) f[d] = ac.total(d);
-                pe = ac.total(3);
+                    else
+                    {
+                        // Branch-free walk: the arithmetic runs for every entry and
+                        // entries beyond the cutoff add zero.  An entry within
+                        // 2e-5 relative of the cutoff (several times the binary32
+                        // error of r^2) is decided in binary64 after the walk: one
+                        // such entry per atom is kept in registers, more (rare)
+                        // send the atom through a second walk over its near
+                        // entries only.
+                        const float band = 2e-5f * rc2f;
+                        int npend = 0, pend = 0;
+                        float3 prv = make_float3(0.f, 0.f, 0.f);
+                        for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                            const float3 rv = rv_of(xi, xj, o);
+                            const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                            const bool near = fabsf(r2 - rc2f) <= band;
+                            const bool in = (r2 < rc2f) && !near;
+                            npend += near;
+                            pend = near ? js : pend;
+                            prv = near ? rv : prv;
+                            float fa, e;
+                            pair_lm(r2, fa, e);
+                            fa = in ? fa : 0.f;
+                            e = in ? e : 0.f;
+                            ac.part[0] += fa * rv.x;
+                            ac.part[1] += fa * rv.y;
+                            ac.part[2] += fa * rv.z;
+                            if constexpr (E) ac.part[3] += e;
+                        }, [&](int k) { ac.entries(k); });
+                        ac.flush();
+                        if (npend == 1)
+                        {
+                            if (geom64_mi(g, g.xd[t], g.xd[pend]).r2 < rc2)
+                            {
+                                const float r2 = prv.x * prv.x + prv.y * prv.y + prv.z * prv.z;
+                                float fa, e;
+                                pair_lm(r2, fa, e);
+                                ac.part[0] += fa * prv.x;
+                                ac.part[1] += fa * prv.y;
+                                ac.part[2] += fa * prv.z;
+                                if constexpr (E) ac.part[3] += e;
+                                ac.flush();
+                            }
+                        }
+                        else if (npend > 1)
+                        {
+                            for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
+                                const float3 rv = rv_of(xi, xj, o);
+                                const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+                                if (!(fabsf(r2 - rc2f) <= band)) return;
+                                if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
+                                float fa, e;
+                                pair_lm(r2, fa, e);
+                                ac.part[0] += fa * rv.x;
+                                ac.part[1] += fa * rv.y;
+                                ac.part[2] += fa * rv.z;
+                                if constexpr (E) ac.part[3] += e;
+                            }, [&](int k) { ac.entries(k); });
+                            ac.flush();
+                        }
+                    }
+                    for (int d = 0; d < 3; d++) f[d] = ac.total(d);
+                    if constexpr (E) pe = ac.total(3);
+                };
+                // (the EAM walk keeps its energy term: dropping it measured
+                // slower for that kernel)
+                if constexpr (CAT == CAT_EAM)
+                    walk(std::true_type{});
+                else if (thermo)
+                    walk(std::true_type{});
+                else
+                    walk(std::false_type{});
             }
             else
             {
@@ -831,19 +847,23 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                     S.v[(size_t)d * cap + i] = v[d];
                 }
             }
-            acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-            acc[2] = m * v[0];
-            acc[3] = m * v[1];
-            acc[4] = m * v[2];
-            acc[5] = 1.0;
+            if (thermo)
+            {
+                acc[1] = m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                acc[2] = m * v[0];
+                acc[3] = m * v[1];
+                acc[4] = m * v[2];
+                acc[5] = 1.0;
+            }
         }
     }
     __shared__ double blk[6];
     __shared__ unsigned ticket;
-    block_reduce_store<6>(acc, blk);
+    if (thermo) block_reduce_store<6>(acc, blk);
     if (threadIdx.x == 0)
     {
-        for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
+        if (thermo)
+            for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
         __threadfence();
         ticket = atomicAdd(&dyn->blocks_done, 1u);
     }
@@ -851,7 +871,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     if (ticket == (unsigned)nb - 1)
     {
         __threadfence();
-        final_reduce(g, nb, 0, g.has_eam, g.st.thermostat, dt, g.st.tau, g.st.T0);
+        if (thermo) final_reduce(g, nb, 0, g.has_eam, g.st.thermostat, dt, g.st.tau, g.st.T0);
         if (threadIdx.x == 0)
         {
             dyn->blocks_done = 0;
