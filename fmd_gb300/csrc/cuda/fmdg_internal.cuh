@@ -195,6 +195,7 @@ struct LocOne
     static constexpr int max_threads = 128;
     static constexpr int min_blocks = 0;      // 0: register count left to the compiler
     static constexpr int lean_min_blocks = 7; // lean force kernels: 7 blocks of 128 (72 registers), measured best
+    static constexpr bool renumbered = false;  // skin-list slots stay the upload positions
     Geo g;
 };
 
@@ -203,6 +204,7 @@ struct LocPack
     static constexpr int max_threads = 256;
     static constexpr int min_blocks = 0;
     static constexpr int lean_min_blocks = 0; // packed lean force kernels: compiler's choice, measured best
+    static constexpr bool renumbered = true;   // slot = index whenever a list is built
     int nsys;
     int bstart[FMDG_PACK_MAX + 1];
     Geo geos[FMDG_PACK_MAX];

@@ -45,7 +45,9 @@ namespace {
 
 // list entry (read as unsigned): neighbour slot | stencil code << 25; code
 // < 125 over a stencil of radius R (width W = 2R + 1):
-// ((ox + R) W + (oy + R)) W + (oz + R)
+// ((ox + R) W + (oy + R)) W + (oz + R).  Layout: rounds of four entries,
+// int4 row (k / 4) * cap + t holds entries k..k+3 of slot t (one 16-byte
+// access per round; a row is contiguous over consecutive slots).
 constexpr int SLOT_BITS = 25;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
@@ -178,14 +180,13 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
     if (cnt <= g.maxnb)
     {
         const int cap = g.cap;
-        const int *col = g.nbr + t;
+        const int4 *col = reinterpret_cast<const int4 *>(g.nbr) + t;
         int k = 0;
         for (; k + 4 <= cnt; k += 4)
         {
-            if (PF && k + 8 <= cnt)
-                for (int q = 4; q < 8; q++) asm volatile("prefetch.global.L1 [%0];" ::"l"(col + (size_t)(k + q) * cap));
-            const int e0 = __ldg(col + (size_t)k * cap), e1 = __ldg(col + (size_t)(k + 1) * cap);
-            const int e2 = __ldg(col + (size_t)(k + 2) * cap), e3 = __ldg(col + (size_t)(k + 3) * cap);
+            if (PF && k + 8 <= cnt) asm volatile("prefetch.global.L1 [%0];" ::"l"(col + (size_t)((k >> 2) + 1) * cap));
+            const int4 e4 = __ldg(col + (size_t)(k >> 2) * cap);
+            const int e0 = e4.x, e1 = e4.y, e2 = e4.z, e3 = e4.w;
             const float4 x0 = g.xl[e0 & SLOT_MASK], x1 = g.xl[e1 & SLOT_MASK];
             const float4 x2 = g.xl[e2 & SLOT_MASK], x3 = g.xl[e3 & SLOT_MASK];
             f(e0 & SLOT_MASK, x0, so.off[(unsigned)e0 >> SLOT_BITS]);
@@ -194,11 +195,17 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
             f(e3 & SLOT_MASK, x3, so.off[(unsigned)e3 >> SLOT_BITS]);
             r(4);
         }
-        for (; k < cnt; k++)
+        if (k < cnt)
         {
-            const int e = __ldg(col + (size_t)k * cap);
-            f(e & SLOT_MASK, g.xl[e & SLOT_MASK], so.off[(unsigned)e >> SLOT_BITS]);
-            r(1);
+            // the last, partial round (1-3 entries)
+            const int4 e4 = __ldg(col + (size_t)(k >> 2) * cap);
+            const int ee[3] = {e4.x, e4.y, e4.z};
+            for (int q = 0; q < 3 && k + q < cnt; q++)
+            {
+                const int e = ee[q];
+                f(e & SLOT_MASK, g.xl[e & SLOT_MASK], so.off[(unsigned)e >> SLOT_BITS]);
+                r(1);
+            }
         }
     }
     else
@@ -349,14 +356,31 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
             const Side S = g.side[dyn->cur];
             const float4 xi = g.xf4[i];
             const float rl2 = g.rskin2;
+            int4 *row = reinterpret_cast<int4 *>(g.nbr) + t;
+            // hits shift through a four-entry register buffer (in order:
+            // x oldest); every fourth hit writes one 16-byte row; the
+            // buffer update is branch-free (a warp's lanes hit at different
+            // candidates)
+            int4 buf = make_int4(0, 0, 0, 0);
             for_each_candidate(g, S, i, xi, [&](int j, int code) {
                 const float3 d = rv_of(xi, __ldg(g.xf4 + j), so.off[code]);
-                if (d.x * d.x + d.y * d.y + d.z * d.z < rl2)
-                {
-                    if (cnt < maxnb) g.nbr[(size_t)cnt * cap + t] = (int)((unsigned)S.slot[j] | ((unsigned)code << SLOT_BITS));
-                    cnt++;
-                }
+                const bool hit = d.x * d.x + d.y * d.y + d.z * d.z < rl2;
+                const int sj = L::renumbered ? j : (hit ? S.slot[j] : 0);
+                const int e = (int)((unsigned)sj | ((unsigned)code << SLOT_BITS));
+                buf.x = hit ? buf.y : buf.x;
+                buf.y = hit ? buf.z : buf.y;
+                buf.z = hit ? buf.w : buf.z;
+                buf.w = hit ? e : buf.w;
+                cnt += hit;
+                if (hit && (cnt & 3) == 0 && cnt <= maxnb) row[(size_t)((cnt >> 2) - 1) * cap] = buf;
             });
+            const int rem = cnt & 3;
+            if (rem && cnt <= maxnb)
+            {
+                const int4 last = (rem == 1) ? make_int4(buf.w, 0, 0, 0)
+                                : (rem == 2) ? make_int4(buf.z, buf.w, 0, 0) : make_int4(buf.y, buf.z, buf.w, 0);
+                row[(size_t)(cnt >> 2) * cap] = last;
+            }
             g.cb[t] = S.cell_of[i];
             g.xl[t] = xi;
             g.xb[t] = xi;
