@@ -433,10 +433,29 @@ int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
         rc2max = hmin * hmin;
     }
     const double rlist = sqrt(rc2max) + (s->g.skin > 0.0 ? s->g.skin : 1e-2);
+    if (s->list_capacity > 0) return s->list_capacity;
+    return fmdg_capacity_estimate(cell_count, ncell, g.cellh[0] * g.cellh[1] * g.cellh[2], rlist);
+}
+
+// Neighbour-list entries per atom (before fmdg_upload); 0: the estimate.
+extern "C" int fmdg_set_list_capacity(fmdg_sys_t *s, int entries)
+{
+    if (entries < 0 || entries > 1024 || (entries % 8) != 0)
+        return fmdg_set_error("fmdg_set_list_capacity: 0 or a multiple of 8 up to 1024");
+    s->list_capacity = entries;
+    return FMDG_OK;
+}
+
+// Entries per atom a neighbour list of radius rlist holds: 1.3 x the count
+// at the density of the fullest cell + 16, a multiple of 8 in [32, 1024].
+// Atoms beyond it scan their stencil directly, so this is a performance and
+// memory knob only (fmdg_set_list_capacity overrides it).
+int fmdg_capacity_estimate(const int *cell_count, int ncell, double cell_volume, double rlist)
+{
     int maxcell = 0;
     for (int c = 0; c < ncell; c++) maxcell = cell_count[c] > maxcell ? cell_count[c] : maxcell;
-    const double nmax = maxcell / (g.cellh[0] * g.cellh[1] * g.cellh[2]);
-    const double est = 4.0 / 3.0 * 3.14159265358979 * rlist * rlist * rlist * nmax;
+    const double dens = maxcell / cell_volume;
+    const double est = 4.0 / 3.0 * 3.14159265358979 * rlist * rlist * rlist * dens;
     int maxnb = (int)(1.3 * est + 16);
     maxnb = (maxnb + 7) & ~7;
     if (maxnb < 32) maxnb = 32;

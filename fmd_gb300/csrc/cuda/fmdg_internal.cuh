@@ -175,6 +175,7 @@ struct fmdg_sys
     bool eam_borrowed;            // EAM tables belong to another system
     char *arena;                  // one device allocation holding the per-atom and per-cell buffers
     bool skin_set;                // skin chosen by the caller (any precision)
+    int list_capacity;            // neighbour-list entries per atom; 0: estimated at upload
 };
 
 // ---- which system a thread block works on ------------------------------------
@@ -283,6 +284,7 @@ int fmdg_pack_tables(fmdg_sys_t *s);
 int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0);
 int fmdg_launch_thermo(fmdg_sys_t *s, int group, int thermostat, double dt, double tau, double T0);
 int fmdg_force_blocks(const fmdg_sys_t *s);
+int fmdg_capacity_estimate(const int *cell_count, int ncell, double cell_volume, double rlist);
 int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell);
 size_t fmdg_bytes_estimate(int n, int ncell, int maxnb);
 int fmdg_set_steps_left(fmdg_sys_t *s, int steps);

@@ -62,6 +62,7 @@ struct Job
     int prec;
     int keep_state;
     int cats;           // bit mask (1 << FMDG_POT_*) of the pair categories
+    double skin;        // Verlet skin of the job's list (fixed at submission)
     int nc[3];
     double cellh[3];
     double rcmax;
@@ -145,6 +146,7 @@ struct fmdg_server
     int max_jobs, chunk;
     int fixed_fblk = 0;               // 0: autotune
     double skin = 0.8;                // Verlet skin of the packed neighbour lists (A)
+    int list_capacity = 0;            // list entries per atom, 0: estimated per job
     double t0;
     long long next_id = 1, seq = 0;
     std::deque<Job *> queue;
@@ -246,14 +248,8 @@ int setup_job(fmdg_server_t *S, Job *j)
     if (rc) return rc;
     fmdg_sys_t *s = j->sys;
     if ((rc = fmdg_set_box(s, j->l, j->pbc, j->nc, j->cellh))) return rc;
-    // list radius rc + skin below half of every periodic box length and
-    // within two cells (skin <= rc: every cell is at least rc wide); a
-    // radius above the cell width scans the 125-cell stencil, pruned to the
-    // cells within the radius
-    double skin = std::min(S->skin, 0.99 * j->rcmax);
-    for (int d = 0; d < 3; d++)
-        if (j->pbc[d]) skin = std::min(skin, 0.9 * (0.5 * j->l[d] - j->rcmax));
-    if ((rc = fmdg_set_skin(s, skin))) return rc;
+    if ((rc = fmdg_set_skin(s, j->skin))) return rc;
+    if ((rc = fmdg_set_list_capacity(s, S->list_capacity))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
     if (j->cats & (1 << FMDG_POT_EAM))
@@ -631,6 +627,14 @@ extern "C" int fmdg_srv_set_skin(fmdg_server_t *S, double skin)
     return FMDG_OK;
 }
 
+extern "C" int fmdg_srv_set_list_capacity(fmdg_server_t *S, int entries)
+{
+    if (entries < 0 || entries > 1024 || (entries % 8) != 0)
+        return fmdg_set_error("fmdg_srv_set_list_capacity: 0 or a multiple of 8 up to 1024");
+    S->list_capacity = entries;
+    return FMDG_OK;
+}
+
 extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long long *id)
 {
     if (d->nkinds < 1 || d->nkinds > FMDG_MAXK) return fmdg_set_error("fmdg_srv_submit: 1..8 kinds");
@@ -682,15 +686,26 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
     const double rcmax = sqrt(rc2max);
     j->rcmax = rcmax;
     for (int k = 0; k < 3; k++)
-    {
         if (d->pbc[k] && !(d->l[k] > 2.0 * rcmax))
         {
             delete j;
             return fmdg_set_error("fmdg_srv_submit: a periodic box length is not above twice the cutoff");
         }
+    // The job's skin (fixed now): at most 0.99 rc, the list radius rc + skin
+    // below half of every periodic box length.
+    double skin = std::min(S->skin, 0.99 * rcmax);
+    for (int k = 0; k < 3; k++)
+        if (d->pbc[k]) skin = std::min(skin, 0.9 * (0.5 * d->l[k] - rcmax));
+    j->skin = skin;
+    const double rl = rcmax + skin;
+    // Cell grid of the reference (src/misc.c:41-50): nc = (int)(l/rc_max),
+    // cellh = l/nc.  (Cells of half the list radius were measured too: list
+    // builds 20-30% faster, pair forces slower -- their gathers spread over
+    // more, smaller cells -- no net gain.)
+    for (int k = 0; k < 3; k++)
+    {
         j->l[k] = d->l[k];
         j->pbc[k] = d->pbc[k];
-        // src/misc.c:41-50: nc = (int)(l/rc_max), cellh = l/nc
         j->nc[k] = (int)(d->l[k] / rcmax);
         if (j->nc[k] < 1)
         {
@@ -744,13 +759,9 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
     for (int c = 0; c < ncell; c++) start[c + 1] = start[c] + j->cell_count[c];
     j->order.resize(d->n);
     for (int a = 0; a < d->n; a++) j->order[start[cell[a]]++] = a;
-    // device bytes: a probe system gives the list capacity of the same rule
-    int maxcell = 0;
-    for (int c = 0; c < ncell; c++) maxcell = std::max(maxcell, j->cell_count[c]);
-    const double nmax = maxcell / (j->cellh[0] * j->cellh[1] * j->cellh[2]);
-    const double rl = rcmax + 1e-2;
-    int maxnb = (int)(1.3 * (4.0 / 3.0 * 3.14159265358979 * rl * rl * rl * nmax) + 16);
-    maxnb = std::min(1024, std::max(32, (maxnb + 7) & ~7));
+    // device bytes, with the list capacity the system will get
+    const int maxnb = fmdg_capacity_estimate(j->cell_count.data(), ncell,
+                                             j->cellh[0] * j->cellh[1] * j->cellh[2], rl);
     j->bytes = fmdg_bytes_estimate(d->n, ncell, maxnb);
     j->id = S->next_id++;
     j->t_submit = wall_s() - S->t0;

@@ -169,9 +169,14 @@ struct NoRound
 // List walk of slot t (four entries per round): f(neighbour slot, its
 // binary32 position, image offset); r(k) after every k entries visited (a
 // round of four, or one).  PF: the next round's list rows are prefetched
-// into L1 while this round is processed (the rows stream from DRAM).  An
-// atom whose list overflowed scans its candidates directly, with positions
-// relative to the current cells.
+// into L1 while this round is processed (the rows stream from DRAM).
+// An atom whose list overflowed scans the stencil of its cell directly:
+// positions are the current binary64 ones relative to the cells of the
+// last refresh (packed systems refresh their cells only at a rebuild; an
+// atom has moved less than skin/2 since, so the stencil still covers the
+// list radius), and of the occurrences of a neighbour (a cell recurs in the
+// stencil when an axis has fewer than 2R + 1 cells) only the image within
+// the list radius is passed on.
 template <bool PF = false, typename F, typename R>
 __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
                                                    float4 &xi, F &&f, R &&r)
@@ -210,9 +215,18 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
     }
     else
     {
-        xi = g.xf4[i];
+        const double4_32a xdi = g.xd[t], oi = g.corig[S.cell_of[i]];
+        xi = make_float4((float)(xdi.x - oi.x), (float)(xdi.y - oi.y), (float)(xdi.z - oi.z), xi.w);
+        const float lim2 = g.rskin2 * 1.0001f;
         for_each_candidate(g, S, i, xi, [&](int j, int code) {
-            f(S.slot[j], g.xf4[j], so.off[code]);
+            const int js = S.slot[j];
+            const double4_32a xdj = g.xd[js], oj = g.corig[S.cell_of[j]];
+            const float4 xj = make_float4((float)(xdj.x - oj.x), (float)(xdj.y - oj.y), (float)(xdj.z - oj.z),
+                                          g.xf4[j].w);
+            const float4 o = so.off[code];
+            const float3 d = rv_of(xi, xj, o);
+            if (d.x * d.x + d.y * d.y + d.z * d.z > lim2) return;
+            f(js, xj, o);
             r(1);
         });
     }

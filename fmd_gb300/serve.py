@@ -85,7 +85,9 @@ def bind(L):
         "fmdg_last_error": ([], C.c_char_p),
         "fmdg_srv_create": ([P(vp), i, sz, i, i], i), "fmdg_srv_destroy": ([vp], None),
         "fmdg_srv_set_eam": ([vp, i, i, i, d, i, d] + [P(d)] * 6, i),
-        "fmdg_srv_set_tuning": ([vp, i], i), "fmdg_srv_set_skin": ([vp, d], i), "fmdg_srv_submit": ([vp, P(JobDesc), P(C.c_longlong)], i),
+        "fmdg_srv_set_tuning": ([vp, i], i), "fmdg_srv_set_skin": ([vp, d], i),
+        "fmdg_srv_set_list_capacity": ([vp, i], i), "fmdg_set_list_capacity": ([vp, i], i),
+        "fmdg_srv_submit": ([vp, P(JobDesc), P(C.c_longlong)], i),
         "fmdg_srv_progress": ([vp, i, P(i)], i), "fmdg_srv_result": ([vp, C.c_longlong, P(JobResult)], i),
         "fmdg_srv_state": ([vp, C.c_longlong, P(d), P(d), P(d), P(C.c_uint)], i),
         "fmdg_srv_release": ([vp, C.c_longlong], i), "fmdg_srv_now": ([vp, P(d)], i),
@@ -286,6 +288,9 @@ class Server:
     def set_skin(self, skin):
         check(self.L, self.L.fmdg_srv_set_skin(self.h, skin), "fmdg_srv_set_skin")
 
+    def set_list_capacity(self, entries):
+        check(self.L, self.L.fmdg_srv_set_list_capacity(self.h, entries), "fmdg_srv_set_list_capacity")
+
     def submit(self, pot, x, v, l, steps, precision=PREC_MIXED, keep_state=False, dt=None, kind=None):
         """Queue a job of type `pot` (POTENTIALS or HYBRID); `l` a cube edge
         or three box lengths; `kind` per atom (default all 0)."""
@@ -392,7 +397,7 @@ class Single:
     path libfmd.so's fmd_dync_integrate drives): its own system, steps
     replayed from one captured graph, no packing."""
 
-    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0, kind=None):
+    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0, kind=None, list_capacity=0):
         self.L = L
         h = C.c_void_p()
         check(L, L.fmdg_create(C.byref(h), device), "fmdg_create")
@@ -413,6 +418,7 @@ class Single:
                                     _dp(t["F_DD"]), _dp(t["rho"]), _dp(t["rhoDD"]), _dp(t["phi"]),
                                     _dp(t["phiDD"])), "set_eam")
         check(L, L.fmdg_set_precision(h, precision), "set_precision")
+        check(L, L.fmdg_set_list_capacity(h, list_capacity), "set_list_capacity")
         n = len(x)
         xs = np.ascontiguousarray(x[order])
         vs = np.ascontiguousarray(v[order])

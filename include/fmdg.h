@@ -106,6 +106,12 @@ int fmdg_set_precision(fmdg_sys_t *s, int mode);
    mixed precision at upload (environment FMD_SKIN overrides), none in
    binary64 unless set here. */
 int fmdg_set_skin(fmdg_sys_t *s, double skin);
+/* Neighbour-list entries per atom (before fmdg_upload; 0, the default:
+   1.3 x the count at the fullest cell's density + 16).  A multiple of 8 up
+   to 1024.  An atom with more neighbours than the list holds scans its
+   stencil directly (same results, slower), so this bounds list memory
+   only. */
+int fmdg_set_list_capacity(fmdg_sys_t *s, int entries);
 
 /* --- atoms (replaces the distribution of the global grid to the local grid,
        src/matter.c:329-447, and the state gathers of src/misc.c:310-422) -- */
@@ -313,6 +319,9 @@ int  fmdg_srv_set_tuning(fmdg_server_t *srv, int fblk);
    at 0.99 of the cutoff and below half of every periodic box length minus
    the cutoff.  Jobs need periodic box lengths above twice the cutoff. */
 int  fmdg_srv_set_skin(fmdg_server_t *srv, double skin);
+/* list entries per atom of the jobs admitted from now on (as
+   fmdg_set_list_capacity; 0: estimated per job) */
+int  fmdg_srv_set_list_capacity(fmdg_server_t *srv, int entries);
 /* queue a job (the description is copied) */
 int  fmdg_srv_submit(fmdg_server_t *srv, const fmdg_job_desc_t *job, long long *id);
 /* one turn of the serving loop (reap finished chunks, admit, launch);

@@ -297,3 +297,77 @@ def test_long_hot_run(L, eam, precision):
     tol = 1e-10 if precision == serve.PREC_FP64 else 1e-5
     err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
     assert err <= tol, err
+
+
+def _oracle_forces(pot, l, kind, xp, vp, ids):
+    import pyoracle
+    nc, cellh, order, counts = serve.host_binning3(xp, l, serve.job_rc(pot))
+    kinds, pots = ORACLE_POTS[pot]
+    with tempfile.TemporaryDirectory() as work:
+        setfl = workloads.write_analytic_eam(os.path.join(work, "a.eam.alloy"))
+        o = pyoracle.Oracle()
+        o.setup(np.broadcast_to(l, (3,)), [1, 1, 1], nc, cellh, kinds, pots, setfl)
+    n = len(xp)
+    kp = np.zeros(n, np.uint32) if kind is None else kind[ids]
+    ncell_all = int(np.prod(nc))
+    o.upload(np.repeat(np.arange(ncell_all, dtype=np.int32), counts), xp[order], vp[order], kp[order],
+             np.zeros(n, np.int32), ids[order], ncell_all)
+    o.forces(-1)
+    d = o.dump()
+    o.close()
+    Fo = np.zeros_like(xp)
+    Fo[d["id"]] = d["F"]
+    return Fo
+
+
+@pytest.mark.parametrize("pot", ["morse", "cuar"])
+@pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
+def test_list_overflow_fallback(L, eam, pot, precision):
+    """Lists of 32 entries per atom, far fewer than the neighbours: every
+    atom scans its stencil directly (current positions relative to the
+    cells of the last refresh, one image per neighbour -- the hybrid box has
+    two cells along y and z, so cells recur in the stencil).  Against the
+    same job with full lists: binary64 positions within 1e-12 A after 40
+    steps at 1200 K, mixed within 1e-6 A; final forces against the binary64
+    oracle (1e-10 / 1e-5)."""
+    x, v, l, kind = _sys(pot, 6, 1200.0, 91)
+    out = []
+    for cap in (0, 32):
+        srv = serve.Server(L, chunk_steps=8, eam=eam)
+        srv.set_skin(0.3)
+        srv.set_list_capacity(cap)
+        jid = srv.submit(pot, x, v, l, 40, precision=precision, keep_state=True, kind=kind)
+        srv.drain()
+        assert srv.result(jid).state == 2
+        out.append(srv.state(jid, len(x)))
+        srv.close()
+    (xa, va, Fa, ia), (xb, vb, Fb, ib) = out
+    oa, ob = np.argsort(ia), np.argsort(ib)
+    d = xa[oa] - xb[ob]
+    d -= np.broadcast_to(l, (3,)) * np.round(d / np.broadcast_to(l, (3,)))
+    assert np.abs(d).max() <= (1e-12 if precision == serve.PREC_FP64 else 1e-6)
+    Fo = _oracle_forces(pot, l, kind, xb, vb, ib)
+    Fq = np.zeros_like(Fb)
+    Fq[ib] = Fb
+    err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
+    assert err <= (1e-10 if precision == serve.PREC_FP64 else 1e-5), err
+
+
+@pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
+def test_single_list_overflow_fallback(L, eam, precision):
+    """The single-system path with lists of 32 entries: the same pairs in
+    the same order as with full lists, so the same trajectory (binary64
+    bit for bit; mixed within 1e-6 A: partial sums group differently)."""
+    x, v, l, kind = _sys("cuar", 6, 900.0, 93)
+    res = []
+    for cap in (0, 32):
+        one = serve.Single(L, "cuar", x, v, l, precision=precision, eam=eam, kind=kind, list_capacity=cap)
+        one.steps(20)
+        res.append(_by_id(one.state()))
+        one.close()
+    (xa, va, Fa), (xb, vb, Fb) = res
+    if precision == serve.PREC_FP64:
+        np.testing.assert_array_equal(xa, xb)
+        np.testing.assert_array_equal(Fa, Fb)
+    else:
+        assert np.abs(xa - xb).max() <= 1e-6
