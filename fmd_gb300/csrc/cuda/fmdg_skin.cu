@@ -374,11 +374,17 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
             // hits shift through a four-entry register buffer (in order:
             // x oldest); every fourth hit writes one 16-byte row; the
             // buffer update is branch-free (a warp's lanes hit at different
-            // candidates)
+            // candidates).  The stencil walk is for_each_candidate's, with
+            // the cell's image offset folded into the atom's position once
+            // per cell and the self test only in the atom's own cell; the
+            // radius is widened by 1e-5 relative so the folded rounding can
+            // only add entries.
             int4 buf = make_int4(0, 0, 0, 0);
-            for_each_candidate(g, S, i, xi, [&](int j, int code) {
-                const float3 d = rv_of(xi, __ldg(g.xf4 + j), so.off[code]);
-                const bool hit = d.x * d.x + d.y * d.y + d.z * d.z < rl2;
+            const float rb2 = rl2 * 1.00001f;
+            auto take = [&](int j, int code, float ax, float ay, float az) {
+                const float4 xj = __ldg(g.xf4 + j);
+                const float dx = ax - xj.x, dy = ay - xj.y, dz = az - xj.z;
+                const bool hit = dx * dx + dy * dy + dz * dz < rb2;
                 const int sj = L::renumbered ? j : (hit ? S.slot[j] : 0);
                 const int e = (int)((unsigned)sj | ((unsigned)code << SLOT_BITS));
                 buf.x = hit ? buf.y : buf.x;
@@ -387,7 +393,55 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
                 buf.w = hit ? e : buf.w;
                 cnt += hit;
                 if (hit && (cnt & 3) == 0 && cnt <= maxnb) row[(size_t)((cnt >> 2) - 1) * cap] = buf;
-            });
+            };
+            const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
+            const int R = g.srad, W = 2 * R + 1;
+            const float lim2 = g.rskin2 * 1.0001f;
+            for (int ox = -R; ox <= R; ox++)
+            {
+                const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
+                if (gx * gx > lim2) continue;
+                int cx = ci.x + ox;
+                if (cx < 0 || cx >= g.nc[0])
+                {
+                    if (!g.pbc[0]) continue;
+                    cx = (cx + 2 * g.nc[0]) % g.nc[0];
+                }
+                for (int oy = -R; oy <= R; oy++)
+                {
+                    const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
+                    if (gx * gx + gy * gy > lim2) continue;
+                    int cy = ci.y + oy;
+                    if (cy < 0 || cy >= g.nc[1])
+                    {
+                        if (!g.pbc[1]) continue;
+                        cy = (cy + 2 * g.nc[1]) % g.nc[1];
+                    }
+                    for (int oz = -R; oz <= R; oz++)
+                    {
+                        const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
+                        if (gx * gx + gy * gy + gz * gz > lim2) continue;
+                        int cz = ci.z + oz;
+                        if (cz < 0 || cz >= g.nc[2])
+                        {
+                            if (!g.pbc[2]) continue;
+                            cz = (cz + 2 * g.nc[2]) % g.nc[2];
+                        }
+                        const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
+                        const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
+                        const float4 o = so.off[code];
+                        const float ax = xi.x - o.x, ay = xi.y - o.y, az = xi.z - o.z;
+                        const int jb = S.cell_start[c], je = S.cell_start[c + 1];
+                        if (ox == 0 && oy == 0 && oz == 0)
+                        {
+                            for (int j = jb; j < i; j++) take(j, code, ax, ay, az);
+                            for (int j = i + 1; j < je; j++) take(j, code, ax, ay, az);
+                        }
+                        else
+                            for (int j = jb; j < je; j++) take(j, code, ax, ay, az);
+                    }
+                }
+            }
             const int rem = cnt & 3;
             if (rem && cnt <= maxnb)
             {
