@@ -86,11 +86,28 @@ __device__ __forceinline__ dfl df_fma(dfl a, dfl b, dfl c) { return df_add(df_mu
 
 __device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
 
+// Hardware approximations (PTX rcp.approx / rsqrt.approx, relative error
+// about 2^-22) as Newton starting points; conversion and rounding
+// instructions are avoided in the pair loops (they issue at the binary64
+// rate on GB300).
+__device__ __forceinline__ float rcp_start(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_start(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // 1 / a: binary32 reciprocal y0, then one Newton step y0 + y0 (1 - a y0)
 // evaluated in double-float (the residual doubles the precision)
 __device__ __forceinline__ dfl df_rcp(dfl a)
 {
-    const float y0 = __frcp_rn(a.hi);
+    const float y0 = rcp_start(a.hi);
     const dfl e = df_sub({1.f, 0.f}, df_mul_f(a, y0));
     return df_add({y0, 0.f}, df_mul_f(e, y0));
 }
@@ -99,7 +116,7 @@ __device__ __forceinline__ dfl df_rcp(dfl a)
 // r0 + (a - r0^2) / (2 r0) with the residual in double-float
 __device__ __forceinline__ dfl df_sqrt(dfl a)
 {
-    const float y0 = __frsqrt_rn(a.hi);
+    const float y0 = rsqrt_start(a.hi);
     const float r0 = __fmul_rn(a.hi, y0);
     const dfl res = df_sub(a, two_prod(r0, r0));
     return df_add({r0, 0.f}, df_mul_f(res, __fmul_rn(0.5f, y0)));
@@ -118,13 +135,17 @@ __device__ __forceinline__ dfl df_exp(dfl x)
                       {1.666666716e-01f, -4.967053879e-09f}, {4.166666791e-02f, -1.241763470e-09f},
                       {8.333333768e-03f, -4.346172033e-10f}, {1.388888923e-03f, -3.363109444e-11f},
                       {1.984127011e-04f, -2.725596875e-12f}, {2.480158764e-05f, -3.406996094e-13f}};
-    const float n = rintf(__fmul_rn(x.hi, 1.442695041f));
+    // n = x log2(e) rounded to an integer (|n| < 126) by the 1.5 * 2^23
+    // addition; 2^n assembled from its exponent bits
+    const float big = 12582912.f;
+    const float nb = __fadd_rn(__fmul_rn(x.hi, 1.442695041f), big);
+    const float n = __fsub_rn(nb, big);
     const dfl t = df_scale2(df_sub(x, df_mul_f(ln2, n)), 0.03125f);
     dfl p = c[8];
     for (int k = 7; k >= 0; k--) p = df_fma(p, t, c[k]);
     for (int k = 0; k < 5; k++) p = df_mul(p, p);
-    const int e = (int)n;
-    return {ldexpf(p.hi, e), ldexpf(p.lo, e)};
+    const float s = __int_as_float((__float_as_int(nb) - 0x4B400000 + 127) << 23);
+    return {__fmul_rn(p.hi, s), __fmul_rn(p.lo, s)};
 }
 
 // nearest double-float of a binary64 number (hi = x rounded to binary32,

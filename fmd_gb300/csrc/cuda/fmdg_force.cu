@@ -133,16 +133,15 @@ __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i,
 // reference's binary64 geometry to about 1e-14 relative.
 struct GeomDF { dfl rv[3]; dfl r2; };
 
-__device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, float4 jl4, int code,
-                                          const float2 (&ch)[3])
+__device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, float4 jl4, float4 oh4, float4 ol4)
 {
-    const int o[3] = {off_x(code), off_y(code), off_z(code)};
     const float ih[3] = {ih4.x, ih4.y, ih4.z}, il[3] = {il4.x, il4.y, il4.z};
     const float jh[3] = {jh4.x, jh4.y, jh4.z}, jl[3] = {jl4.x, jl4.y, jl4.z};
+    const float oha[3] = {oh4.x, oh4.y, oh4.z}, ola[3] = {ol4.x, ol4.y, ol4.z};
     GeomDF p;
     for (int d = 0; d < 3; d++)
     {
-        const float oh = (float)o[d] * ch[d].x, ol = (float)o[d] * ch[d].y;
+        const float oh = oha[d], ol = ola[d];
         const dfl a = two_sum(ih[d], -jh[d]);
         const dfl b = two_sum(a.hi, -oh);
         const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(il[d], jl[d]), ol), a.lo), b.lo);
@@ -162,14 +161,16 @@ __device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, fl
 }
 
 // interval k = min(floor(q), kmax) and fraction b = q - k of a double-float
-// table coordinate q >= 0
+// table coordinate 0 <= q < 2^22, without conversion instructions (they
+// issue at the binary64 rate on GB300): adding 2^23 rounding towards minus
+// infinity leaves floor(q.hi) in the significand
 __device__ __forceinline__ int df_table_index(dfl q, float kmax, dfl &b)
 {
-    float kf = floorf(q.hi);
+    float kf = __fadd_rd(q.hi, 8388608.f) - 8388608.f;
     if (kf == q.hi && q.lo < 0.f) kf -= 1.f;
     kf = fminf(kf, kmax);
     b = fast_two_sum(__fsub_rn(q.hi, kf), q.lo);
-    return (int)kf;
+    return __float_as_int(kf + 8388608.f) - 0x4B000000;
 }
 
 // binary64 cutoff decision from the double-float r^2: within 1e-6 relative
@@ -298,7 +299,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                 // double-float pair arithmetic (fmdg_df.cuh)
                 const float4 ih = g.xf4[i], il = g.xlo4[i];
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
-                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
                 const float kmax = (float)(nint - 1);
                 dfl acc_rho = {0.f, 0.f};
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     const int pidx = ki * nk + __float_as_int(jh.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
                     if (within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2]))
                     {
                         dfl b;
@@ -425,7 +425,6 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 // src/morse.h:35-56, EAM src/eam.h:186-226 -- the category
                 // chosen per pair for hybrid tables (src/forces.c:33-290)
                 const float4 ih = g.xf4[i], il = g.xlo4[i];
-                const float2 ch[3] = {df_split(g.cellh[0]), df_split(g.cellh[1]), df_split(g.cellh[2])};
                 const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[i]) : dfl{0.f, 0.f};
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
                 const float kmax = (float)(nint - 1);
@@ -437,7 +436,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
                     const int rci = (cat == FMDG_POT_MORSE) ? 3 : 2;
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], code, ch);
+                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
                     if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][rci], pp.p[rci])) return;
                     dfl fa, eh;     // f_i += fa * rv, energy share eh
                     if (cat == FMDG_POT_LJ)

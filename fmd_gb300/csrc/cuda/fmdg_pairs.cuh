@@ -20,6 +20,7 @@ struct SmemPot
     double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
     float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
+    float4 offl[27];    // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
 };
 
 __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
@@ -41,8 +42,13 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
         sp.elem[k] = g.eam_elem[k];
     }
     for (int c = threadIdx.x; c < 27; c += blockDim.x)
-        sp.off[c] = make_float4((float)(c / 9 - 1) * g.cellh_f[0], (float)((c / 3) % 3 - 1) * g.cellh_f[1],
-                                (float)(c % 3 - 1) * g.cellh_f[2], 0.f);
+    {
+        const float ox = (float)(c / 9 - 1), oy = (float)((c / 3) % 3 - 1), oz = (float)(c % 3 - 1);
+        sp.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], 0.f);
+        sp.offl[c] = make_float4(ox * (float)(g.cellh[0] - (double)g.cellh_f[0]),
+                                 oy * (float)(g.cellh[1] - (double)g.cellh_f[1]),
+                                 oz * (float)(g.cellh[2] - (double)g.cellh_f[2]), 0.f);
+    }
     __syncthreads();
 }
 
