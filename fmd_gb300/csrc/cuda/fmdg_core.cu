@@ -563,8 +563,9 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     // a skin list needs the list radius below half of every periodic box
     // length (one image inside it) and within two cells; otherwise the
     // exact stencil list is rebuilt every step
-    // (default: mixed precision only -- binary64 kernels are bound by the
-    // binary64 pipe and lose more on the longer list than the rebuilds cost)
+    // (default: mixed precision only -- in binary64 mode the double-float
+    // pair arithmetic costs more on the longer list than the rebuilds save:
+    // EAM 256k 3.0e8 vs 3.5e8 atom-steps/s; LJ and Morse gain 7-8%)
     g.skin_on = 0;
     if (g.skin > 0.0 && cap < (1 << 25) && (s->skin_set || g.prec == FMDG_PREC_MIXED))
     {
@@ -597,6 +598,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         {
             c.take(g.pos, cap); c.take(g.cb, cap); c.take(g.xl, cap); c.take(g.xb, cap);
             c.take(g.xd, cap); c.take(g.gslot, cap); c.take(g.fpb, cap); c.take(g.fpd, cap);
+            c.take(g.xll, cap);
         }
     };
     Carver measure{nullptr, 0};

@@ -87,7 +87,6 @@ __device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i
 
 // binary64 pair geometry: rv = x_i - (x_j + image shift), r2 summed without
 // fused multiply-adds as the reference does (src/forces.h:25-34)
-struct Geom64 { double rv[3]; double r2; };
 
 __device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const double xi[3], CellXYZ ci, int j, int code)
 {
@@ -124,53 +123,6 @@ __device__ __forceinline__ bool within_cut32(const Geo &g, const Side &S, int i,
     const int cap = g.cap;
     const double xi[3] = {S.x[i], S.x[cap + i], S.x[2 * (size_t)cap + i]};
     return geom64(g, S, xi, ci, j, code).r2 < rc2;
-}
-
-// double-float pair geometry (binary64 mode, EAM) from the cell-local
-// coordinates hi (xf4) + lo (xlo4): rv = x_i - x_j - offset * cellh, the
-// image shift of a periodic neighbour being offset * cellh in the cell
-// frame; r^2 from exact squares of the hi parts.  Agrees with the
-// reference's binary64 geometry to about 1e-14 relative.
-struct GeomDF { dfl rv[3]; dfl r2; };
-
-__device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, float4 jl4, float4 oh4, float4 ol4)
-{
-    const float ih[3] = {ih4.x, ih4.y, ih4.z}, il[3] = {il4.x, il4.y, il4.z};
-    const float jh[3] = {jh4.x, jh4.y, jh4.z}, jl[3] = {jl4.x, jl4.y, jl4.z};
-    const float oha[3] = {oh4.x, oh4.y, oh4.z}, ola[3] = {ol4.x, ol4.y, ol4.z};
-    GeomDF p;
-    for (int d = 0; d < 3; d++)
-    {
-        const float oh = oha[d], ol = ola[d];
-        const dfl a = two_sum(ih[d], -jh[d]);
-        const dfl b = two_sum(a.hi, -oh);
-        const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(il[d], jl[d]), ol), a.lo), b.lo);
-        p.rv[d] = fast_two_sum(b.hi, lo);
-    }
-    const dfl s0 = two_prod(p.rv[0].hi, p.rv[0].hi), s1 = two_prod(p.rv[1].hi, p.rv[1].hi);
-    const dfl s2 = two_prod(p.rv[2].hi, p.rv[2].hi);
-    const dfl t = two_sum(s0.hi, s1.hi);
-    const dfl u = two_sum(t.hi, s2.hi);
-    float cross = __fmul_rn(p.rv[0].hi, p.rv[0].lo);
-    cross = __fmaf_rn(p.rv[1].hi, p.rv[1].lo, cross);
-    cross = __fmaf_rn(p.rv[2].hi, p.rv[2].lo, cross);
-    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(s0.lo, s1.lo), __fadd_rn(s2.lo, t.lo)),
-                               __fadd_rn(u.lo, __fmul_rn(2.f, cross)));
-    p.r2 = fast_two_sum(u.hi, lo);
-    return p;
-}
-
-// interval k = min(floor(q), kmax) and fraction b = q - k of a double-float
-// table coordinate 0 <= q < 2^22, without conversion instructions (they
-// issue at the binary64 rate on GB300): adding 2^23 rounding towards minus
-// infinity leaves floor(q.hi) in the significand
-__device__ __forceinline__ int df_table_index(dfl q, float kmax, dfl &b)
-{
-    float kf = __fadd_rd(q.hi, 8388608.f) - 8388608.f;
-    if (kf == q.hi && q.lo < 0.f) kf -= 1.f;
-    kf = fminf(kf, kmax);
-    b = fast_two_sum(__fsub_rn(q.hi, kf), q.lo);
-    return __float_as_int(kf + 8388608.f) - 0x4B000000;
 }
 
 // binary64 cutoff decision from the double-float r^2: within 1e-6 relative
@@ -309,12 +261,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
                     const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
                     if (within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2]))
-                    {
-                        dfl b;
-                        const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
-                        const float4 *row = g.pkd_rho + 2 * ((size_t)pp.jloc * nint + ir2);
-                        acc_rho = df_add(acc_rho, df_spl_val(row[0], row[1], b));
-                    }
+                        acc_rho = df_add(acc_rho, df_rho(g, pp, p, inv_h, kmax, nint));
                 });
                 rho = df_to_double(acc_rho);
             }
@@ -439,46 +386,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                     const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
                     if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][rci], pp.p[rci])) return;
                     dfl fa, eh;     // f_i += fa * rv, energy share eh
-                    if (cat == FMDG_POT_LJ)
-                    {
-                        const dfl eps4 = df_of(sp.pd[pidx][0]), sig2 = df_of(sp.pd[pidx][1]);
-                        const dfl inv_r2 = df_rcp(p.r2);
-                        const dfl s2 = df_mul(sig2, inv_r2);
-                        const dfl s6 = df_mul(df_mul(s2, s2), s2);
-                        const dfl s12 = df_mul(s6, s6);
-                        fa = df_mul(df_mul(df_mul_f(eps4, 12.f), inv_r2), df_sub(s12, df_scale2(s6, 0.5f)));
-                        eh = df_scale2(df_mul(eps4, df_sub(s12, s6)), 0.5f);
-                    }
-                    else if (cat == FMDG_POT_MORSE)
-                    {
-                        const dfl D0 = df_of(sp.pd[pidx][0]), al = df_of(sp.pd[pidx][1]);
-                        const dfl r0 = df_of(sp.pd[pidx][2]);
-                        const dfl r = df_sqrt(p.r2);
-                        const dfl inv_r = df_rcp(r);
-                        const dfl e1 = df_exp(df_mul(df_neg(al), df_sub(r, r0)));
-                        const dfl e2 = df_mul(e1, e1);
-                        fa = df_mul(df_mul(df_scale2(df_mul(al, D0), 2.f), inv_r), df_sub(e2, e1));
-                        eh = df_scale2(df_mul(D0, df_sub(e2, df_scale2(e1, 2.f))), 0.5f);
-                    }
-                    else
-                    {
-                        dfl b;
-                        const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
-                        const int ei = pp.iloc, ej = pp.jloc;
-                        const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
-                        const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
-                        const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
-                        const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
-                        dfl rho_jp = rho_ip;
-                        if (ei != ej)
-                        {
-                            const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
-                            rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
-                        }
-                        const dfl fpj = df_of(g.fpdf[j]);
-                        fa = df_neg(df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fpj, rho_ip)), phi_d), 2.f));
-                        eh = df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f);
-                    }
+                    df_pair(g, sp, pidx, pp, cat, p, fpi, inv_h, kmax, nint, ne, [&]() { return df_of(g.fpdf[j]); },
+                            fa, eh);
                     for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(fa, p.rv[d]));
                     pes = df_add(pes, eh);
                 });

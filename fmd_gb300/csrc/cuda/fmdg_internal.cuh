@@ -88,6 +88,7 @@ struct Geo   // passed by value to kernels
     const float4 *pkd_rho, *pkd_phi;
     float4 *xlo4;
     float2 *fpdf;
+    float4 *xll;       // skin lists, binary64 mode: lo parts of xl (double-float build-frame positions)
     double inv_dr2, inv_drho;
     // binning scratch
     int *bdest;        // destination interior cell, -1 deleted, -2 stays

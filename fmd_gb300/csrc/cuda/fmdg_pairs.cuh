@@ -120,6 +120,127 @@ __device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
     return ((3.f * t.w * b + 2.f * t.z) * b + t.y) * inv_h;
 }
 
+// binary64 pair geometry: rv = x_i - (x_j + image shift), r2 summed without
+// fused multiply-adds as the reference does (src/forces.h:25-34)
+struct Geom64 { double rv[3]; double r2; };
+
+// double-float pair geometry (binary64 mode) from cell-local
+// coordinates hi (xf4) + lo (xlo4): rv = x_i - x_j - offset * cellh, the
+// image shift of a periodic neighbour being offset * cellh in the cell
+// frame; r^2 from exact squares of the hi parts.  Agrees with the
+// reference's binary64 geometry to about 1e-14 relative.
+struct GeomDF { dfl rv[3]; dfl r2; };
+
+__device__ __forceinline__ GeomDF geom_df(float4 ih4, float4 il4, float4 jh4, float4 jl4, float4 oh4, float4 ol4)
+{
+    const float ih[3] = {ih4.x, ih4.y, ih4.z}, il[3] = {il4.x, il4.y, il4.z};
+    const float jh[3] = {jh4.x, jh4.y, jh4.z}, jl[3] = {jl4.x, jl4.y, jl4.z};
+    const float oha[3] = {oh4.x, oh4.y, oh4.z}, ola[3] = {ol4.x, ol4.y, ol4.z};
+    GeomDF p;
+    for (int d = 0; d < 3; d++)
+    {
+        const float oh = oha[d], ol = ola[d];
+        const dfl a = two_sum(ih[d], -jh[d]);
+        const dfl b = two_sum(a.hi, -oh);
+        const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(il[d], jl[d]), ol), a.lo), b.lo);
+        p.rv[d] = fast_two_sum(b.hi, lo);
+    }
+    const dfl s0 = two_prod(p.rv[0].hi, p.rv[0].hi), s1 = two_prod(p.rv[1].hi, p.rv[1].hi);
+    const dfl s2 = two_prod(p.rv[2].hi, p.rv[2].hi);
+    const dfl t = two_sum(s0.hi, s1.hi);
+    const dfl u = two_sum(t.hi, s2.hi);
+    float cross = __fmul_rn(p.rv[0].hi, p.rv[0].lo);
+    cross = __fmaf_rn(p.rv[1].hi, p.rv[1].lo, cross);
+    cross = __fmaf_rn(p.rv[2].hi, p.rv[2].lo, cross);
+    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(s0.lo, s1.lo), __fadd_rn(s2.lo, t.lo)),
+                               __fadd_rn(u.lo, __fmul_rn(2.f, cross)));
+    p.r2 = fast_two_sum(u.hi, lo);
+    return p;
+}
+
+// interval k = min(floor(q), kmax) and fraction b = q - k of a double-float
+// table coordinate 0 <= q < 2^22, without conversion instructions (they
+// issue at the binary64 rate on GB300): adding 2^23 rounding towards minus
+// infinity leaves floor(q.hi) in the significand
+__device__ __forceinline__ int df_table_index(dfl q, float kmax, dfl &b)
+{
+    float kf = __fadd_rd(q.hi, 8388608.f) - 8388608.f;
+    if (kf == q.hi && q.lo < 0.f) kf -= 1.f;
+    kf = fminf(kf, kmax);
+    b = fast_two_sum(__fsub_rn(q.hi, kf), q.lo);
+    return __float_as_int(kf + 8388608.f) - 0x4B000000;
+}
+
+// a binary64 pair geometry as double-float (exact splits)
+__device__ __forceinline__ GeomDF geom_df_of64(const Geom64 &q)
+{
+    GeomDF p;
+    for (int d = 0; d < 3; d++) p.rv[d] = df_of(df_split(q.rv[d]));
+    p.r2 = df_of(df_split(q.r2));
+    return p;
+}
+
+// Binary64-mode pair arithmetic in double-float, in the reference's formulas
+// -- LJ src/lj.h:35-56, Morse src/morse.h:35-56, EAM src/eam.h:186-226 --
+// for a pair of category cat: f_i += fa * rv, energy share eh.  fpj() gives
+// F'(rho_j) as a double-float; it is called for EAM pairs only.
+template <typename FPJ>
+__device__ __forceinline__ void df_pair(const Geo &g, const SmemPot &sp, int pidx, const fmdg_pair_t &pp, int cat,
+                                        const GeomDF &p, dfl fpi, dfl inv_h, float kmax, int nint, size_t ne,
+                                        FPJ &&fpj, dfl &fa, dfl &eh)
+{
+    if (cat == FMDG_POT_LJ)
+    {
+        const dfl eps4 = df_of(sp.pd[pidx][0]), sig2 = df_of(sp.pd[pidx][1]);
+        const dfl inv_r2 = df_rcp(p.r2);
+        const dfl s2 = df_mul(sig2, inv_r2);
+        const dfl s6 = df_mul(df_mul(s2, s2), s2);
+        const dfl s12 = df_mul(s6, s6);
+        fa = df_mul(df_mul(df_mul_f(eps4, 12.f), inv_r2), df_sub(s12, df_scale2(s6, 0.5f)));
+        eh = df_scale2(df_mul(eps4, df_sub(s12, s6)), 0.5f);
+    }
+    else if (cat == FMDG_POT_MORSE)
+    {
+        const dfl D0 = df_of(sp.pd[pidx][0]), al = df_of(sp.pd[pidx][1]);
+        const dfl r0 = df_of(sp.pd[pidx][2]);
+        const dfl r = df_sqrt(p.r2);
+        const dfl inv_r = df_rcp(r);
+        const dfl e1 = df_exp(df_mul(df_neg(al), df_sub(r, r0)));
+        const dfl e2 = df_mul(e1, e1);
+        fa = df_mul(df_mul(df_scale2(df_mul(al, D0), 2.f), inv_r), df_sub(e2, e1));
+        eh = df_scale2(df_mul(D0, df_sub(e2, df_scale2(e1, 2.f))), 0.5f);
+    }
+    else
+    {
+        dfl b;
+        const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
+        const int ei = pp.iloc, ej = pp.jloc;
+        const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
+        const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
+        const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
+        const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
+        dfl rho_jp = rho_ip;
+        if (ei != ej)
+        {
+            const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
+            rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
+        }
+        const dfl fj = fpj();
+        fa = df_neg(df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fj, rho_ip)), phi_d), 2.f));
+        eh = df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f);
+    }
+}
+
+// EAM density term f_elem(j)(r^2) of an EAM pair (src/eam.h:278-300)
+__device__ __forceinline__ dfl df_rho(const Geo &g, const fmdg_pair_t &pp, const GeomDF &p, dfl inv_h, float kmax,
+                                      int nint)
+{
+    dfl b;
+    const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
+    const float4 *row = g.pkd_rho + 2 * ((size_t)pp.jloc * nint + ir2);
+    return df_spl_val(row[0], row[1], b);
+}
+
 // Sum over the 32 lanes of a warp of v[0..NV), NV <= 8, by a transposing
 // butterfly: each exchange halves the values a lane carries (v padded to 8),
 // 4 + 2 + 1 + 1 + 1 additions per lane instead of 5 NV.  Value k ends in

@@ -53,15 +53,21 @@ constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
 struct SkinOff
 {
-    float4 off[125];    // image offset of each stencil code, binary32
+    float4 off[125];    // image offset of each stencil code, binary32; .w: the code's bits
+    float4 offl[125];   // the remainders (binary64 offset - off): off + offl in double-float
 };
 
 __device__ __forceinline__ void load_offsets(const Geo &g, SkinOff &so)
 {
     const int R = g.srad, W = 2 * R + 1;
     for (int c = threadIdx.x; c < W * W * W; c += blockDim.x)
-        so.off[c] = make_float4((float)(c / (W * W) - R) * g.cellh_f[0], (float)((c / W) % W - R) * g.cellh_f[1],
-                                (float)(c % W - R) * g.cellh_f[2], 0.f);
+    {
+        const float ox = (float)(c / (W * W) - R), oy = (float)((c / W) % W - R), oz = (float)(c % W - R);
+        so.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], __int_as_float(c));
+        so.offl[c] = make_float4(ox * (float)(g.cellh[0] - (double)g.cellh_f[0]),
+                                 oy * (float)(g.cellh[1] - (double)g.cellh_f[1]),
+                                 oz * (float)(g.cellh[2] - (double)g.cellh_f[2]), 0.f);
+    }
     __syncthreads();
 }
 
@@ -70,7 +76,6 @@ __device__ __forceinline__ float3 rv_of(float4 xi, float4 xj, float4 o)
     return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
 }
 
-struct Geom64 { double rv[3]; double r2; };
 
 // binary64 minimum-image geometry rv = x_a - (x_b + shift)
 __device__ __forceinline__ Geom64 geom64_mi(const Geo &g, double4_32a a, double4_32a b)
@@ -106,6 +111,26 @@ __device__ __forceinline__ bool within_cut_skin(const Geo &g, int ta, int tb, fl
 __device__ __forceinline__ float axis_gap(int o, float u, float h)
 {
     return o > 0 ? fmaxf(0.f, (float)o * h - u) : (o < 0 ? fmaxf(0.f, u + (float)(-o - 1) * h) : 0.f);
+}
+
+// Binary64 mode: double-float geometry of a list entry (build frame: slot
+// positions xl + xll and the entry's stencil offset) or of an overflow
+// fallback occurrence (code < 0 in o.w: current-cell frame, formed from the
+// binary64 positions); the cutoff decision within 1e-6 relative of the
+// cutoff is the binary64 minimum-image one.
+__device__ __forceinline__ GeomDF skin_geom_df(const Geo &g, const SkinOff &so, int t, float4 ih, float4 il, int js,
+                                               float4 xj, float4 o)
+{
+    const int code = __float_as_int(o.w);
+    if (code >= 0) return geom_df(ih, il, xj, g.xll[js], o, so.offl[code]);
+    return geom_df_of64(geom64_mi(g, g.xd[t], g.xd[js]));
+}
+
+__device__ __forceinline__ bool within_cut_df_mi(const Geo &g, int t, int js, dfl r2, float rc2f, double rc2)
+{
+    const float d = __fsub_rn(r2.hi, rc2f);
+    if (fabsf(d) > 1e-6f * rc2f) return d < 0.f;
+    return geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
 }
 
 // Every (j, code) of the stencil of radius R around i's current cell, j
@@ -223,9 +248,10 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
             const double4_32a xdj = g.xd[js], oj = g.corig[S.cell_of[j]];
             const float4 xj = make_float4((float)(xdj.x - oj.x), (float)(xdj.y - oj.y), (float)(xdj.z - oj.z),
                                           g.xf4[j].w);
-            const float4 o = so.off[code];
+            float4 o = so.off[code];
             const float3 d = rv_of(xi, xj, o);
             if (d.x * d.x + d.y * d.y + d.z * d.z > lim2) return;
+            o.w = __int_as_float(-1 - code);    // current-cell frame, not the build frame
             f(js, xj, o);
             r(1);
         });
@@ -249,6 +275,7 @@ __device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, co
     const double4_32a ob = g.corig[g.cb[t]];
     const double o3[3] = {ob.x, ob.y, ob.z};
     float l3[3];
+    double u3[3];
     for (int d = 0; d < 3; d++)
     {
         double u = x[d] - o3[d];
@@ -261,8 +288,12 @@ __device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, co
             uf = (float)u;
         }
         l3[d] = uf;
+        u3[d] = u;
     }
     g.xl[t] = make_float4(l3[0], l3[1], l3[2], kb);
+    if (g.prec == FMDG_PREC_FP64)
+        g.xll[t] = make_float4((float)(u3[0] - (double)l3[0]), (float)(u3[1] - (double)l3[1]),
+                               (float)(u3[2] - (double)l3[2]), 0.f);
     const float4 o = g.xb[t];
     const float dx = l3[0] - o.x, dy = l3[1] - o.y, dz = l3[2] - o.z;
     if (!(dx * dx + dy * dy + dz * dz <= g.half_skin2)) dyn->rebuild = 1;
@@ -342,7 +373,11 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     g.gslot[t] = S.group[i];
     // relative to the current cell (a rebuild starts from these)
     const double4_32a oc = g.corig[S.cell_of[i]];
-    g.xf4[i] = make_float4((float)(x[0] - oc.x), (float)(x[1] - oc.y), (float)(x[2] - oc.z), kb);
+    const double ux = x[0] - oc.x, uy = x[1] - oc.y, uz = x[2] - oc.z;
+    const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
+    g.xf4[i] = make_float4(lx, ly, lz, kb);
+    if (g.prec == FMDG_PREC_FP64)
+        g.xlo4[i] = make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
     // (renumbered, or a rebuild already due: the build cell and position of
     // slot t are rewritten by the list build that follows)
     if (!lazy && !dyn->rebuild) slot_rel_build(g, dyn, t, x, kb);
@@ -452,6 +487,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
             g.cb[t] = S.cell_of[i];
             g.xl[t] = xi;
             g.xb[t] = xi;
+            if (g.prec == FMDG_PREC_FP64) g.xll[t] = g.xlo4[i];
         }
         g.nbr_count[t] = cnt;
     }
@@ -502,21 +538,21 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
         {
             if (!MIXED)
             {
-                const double4_32a xdi = g.xd[t];
-                const double inv_h = g.inv_dr2;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4) {
+                // double-float pair arithmetic (fmdg_df.cuh)
+                const float4 ih = g.xl[t], il = g.xll[t];
+                const dfl inv_h = df_of(df_split(g.inv_dr2));
+                const float kmax = (float)(nint - 1);
+                dfl acc_rho = {0.f, 0.f};
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4 o) {
                     if (group >= 0 && g.gslot[js] != group) return;
-                    const double4_32a xj = g.xd[js];
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + __float_as_int(xjf.w)];
+                    const int pidx = ki * nk + __float_as_int(xjf.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                    const Geom64 p = geom64_mi(g, xdi, xj);
-                    if (p.r2 < pp.p[2])
-                    {
-                        const double q = p.r2 * inv_h;
-                        const int ir2 = min((int)q, nint - 1);
-                        rho += spl_val(g.pk_rho[(size_t)pp.jloc * nint + ir2], q - ir2);
-                    }
+                    const GeomDF p = skin_geom_df(g, so, t, ih, il, js, xjf, o);
+                    if (within_cut_df_mi(g, t, js, p.r2, sp.pf[pidx][2], pp.p[2]))
+                        acc_rho = df_add(acc_rho, df_rho(g, pp, p, inv_h, kmax, nint));
                 });
+                rho = df_to_double(acc_rho);
             }
             else if constexpr (LEAN)
             {
@@ -620,12 +656,14 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             }
             g.vaream[i] = fp;
             g.fpd[t] = fp;
+            if (!MIXED) g.fpdf[t] = df_split(fp);
         }
         else
         {
             g.vaream[i] = 0.0;
             g.fpd[t] = 0.0;
             g.fpb[t] = 0.f;
+            if (!MIXED) g.fpdf[t] = make_float2(0.f, 0.f);
         }
     }
     if (loc_thermo(loc, g)) block_reduce_store<1>(acc, g.partials + (size_t)nb * 8 + bx);
@@ -669,45 +707,28 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
             const size_t ne = g.nelem;
             if (!MIXED)
             {
-                const double4_32a xdi = g.xd[t];
-                const double fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpd[t] : 0.0;
-                const double inv_h = g.inv_dr2;
-                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4) {
+                // double-float pair arithmetic (fmdg_df.cuh, df_pair)
+                const float4 ih = g.xl[t], il = g.xll[t];
+                const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[t]) : dfl{0.f, 0.f};
+                const dfl inv_h = df_of(df_split(g.inv_dr2));
+                const float kmax = (float)(nint - 1);
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4 o) {
                     if (group >= 0 && g.gslot[js] != group) return;
-                    const double4_32a xj = g.xd[js];
-                    const fmdg_pair_t &pp = sp.pairs[ki * nk + __float_as_int(xjf.w)];
+                    const int pidx = ki * nk + __float_as_int(xjf.w);
+                    const fmdg_pair_t &pp = sp.pairs[pidx];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
-                    const Geom64 p = geom64_mi(g, xdi, xj);
-                    if (cat == FMDG_POT_LJ && p.r2 < pp.p[2])
-                    {
-                        double fa, e;
-                        lj_pair(p.r2, pp, fa, e);
-                        for (int d = 0; d < 3; d++) f[d] += p.rv[d] * fa;
-                        pe += e;
-                    }
-                    else if (cat == FMDG_POT_MORSE && p.r2 < pp.p[3])
-                    {
-                        double fa, e;
-                        morse_pair(p.r2, pp, fa, e);
-                        for (int d = 0; d < 3; d++) f[d] += fa * p.rv[d];
-                        pe += e;
-                    }
-                    else if (cat == FMDG_POT_EAM && p.r2 < pp.p[2])
-                    {
-                        const double q = p.r2 * inv_h;
-                        const int ir2 = min((int)q, nint - 1);
-                        const double b = q - ir2;
-                        const int ei = pp.iloc, ej = pp.jloc;
-                        const double4_32a tph = g.pk_phi[((size_t)ei * ne + ej) * nint + ir2];
-                        const double phi_d = spl_der(tph, b, inv_h);
-                        const double rho_ip = spl_der(g.pk_rho[(size_t)ei * nint + ir2], b, inv_h);
-                        const double rho_jp = (ei == ej) ? rho_ip
-                                            : spl_der(g.pk_rho[(size_t)ej * nint + ir2], b, inv_h);
-                        const double mag = 2 * (fpi * rho_jp + g.fpd[js] * rho_ip + phi_d);
-                        for (int d = 0; d < 3; d++) f[d] -= mag * p.rv[d];
-                        pe += 0.5 * spl_val(tph, b);
-                    }
+                    const int rci = (cat == FMDG_POT_MORSE) ? 3 : 2;
+                    const GeomDF p = skin_geom_df(g, so, t, ih, il, js, xjf, o);
+                    if (!within_cut_df_mi(g, t, js, p.r2, sp.pf[pidx][rci], pp.p[rci])) return;
+                    dfl fa, eh;
+                    df_pair(g, sp, pidx, pp, cat, p, fpi, inv_h, kmax, nint, ne, [&]() { return df_of(g.fpdf[js]); },
+                            fa, eh);
+                    for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(fa, p.rv[d]));
+                    pes = df_add(pes, eh);
                 });
+                for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
+                pe = df_to_double(pes);
             }
             else if constexpr (LEAN)
             {
