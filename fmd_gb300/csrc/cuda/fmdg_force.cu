@@ -31,10 +31,10 @@
 //
 // Precision modes.  FMDG_PREC_FP64: every pair quantity to binary64
 // accuracy, the binary32 list only prunes (its margin keeps every pair
-// within the cutoff).  LJ, Morse and hybrid pairs are evaluated in binary64;
-// EAM pairs in double-float arithmetic (fmdg_df.cuh: about 48 significant
-// bits on the binary32 pipe, GB300's binary64 rate being 1/64 of it) from
-// double-float cell-local coordinates and tables, with cutoff decisions
+// within the cutoff).  LJ, Morse, EAM and hybrid pairs are evaluated in
+// double-float arithmetic (fmdg_df.cuh: about 48 significant bits on the
+// binary32 pipe, GB300's binary64 rate being 1/64 of it) from double-float
+// cell-local coordinates, parameters and tables, with cutoff decisions
 // within 1e-6 relative of the cutoff taken from the reference's binary64
 // geometry.  FMDG_PREC_MIXED: pair geometry from the binary32 cell-local
 // coordinates, pair/spline/embedding arithmetic in binary32, binary32
@@ -85,9 +85,8 @@ __device__ __forceinline__ void for_each_pair(const Geo &g, const Side &S, int i
         scan_stencil(g, S, i, ci, f);
 }
 
-// binary64 pair geometry: rv = x_i - (x_j + image shift), r2 summed without
-// fused multiply-adds as the reference does (src/forces.h:25-34)
-
+// binary64 pair geometry of a stencil entry (Geom64, fmdg_pairs.cuh): the
+// reference's ghost shift of the neighbour, then x_i minus it
 __device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const double xi[3], CellXYZ ci, int j, int code)
 {
     Geom64 p;

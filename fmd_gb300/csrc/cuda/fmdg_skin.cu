@@ -76,7 +76,6 @@ __device__ __forceinline__ float3 rv_of(float4 xi, float4 xj, float4 o)
     return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
 }
 
-
 // binary64 minimum-image geometry rv = x_a - (x_b + shift)
 __device__ __forceinline__ Geom64 geom64_mi(const Geo &g, double4_32a a, double4_32a b)
 {
