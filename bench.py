@@ -536,12 +536,14 @@ def run_reference(args):
     if args.workload == "served":
         jobs = served_jobs(args)
         vals, sample = [], ""
+        for _ in range(args.warmup):            # untimed, short
+            cpu_port_jobs(jobs, cores, budget_s=1.0)
         for _ in range(max(1, min(args.steps, 3))):
             v, sample = cpu_port_jobs(jobs, cores, budget_s=8.0)
             vals.append(v)
         value = float(np.median(vals))
         out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s",
-               "n_gpus": 0, "steps": len(vals), "warmup": 0, "higher_is_better": True, "scaling": "weak",
+               "n_gpus": 0, "steps": len(vals), "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": served_config(args),
                "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
                                 "sample": f"median of {len(vals)} samples; each: {sample}"},
@@ -549,13 +551,15 @@ def run_reference(args):
         print(json.dumps(out))
         return
     vals = []
+    for _ in range(args.warmup):                # untimed, short
+        cpu_port_run(cores, target_s=1.0, max_steps=1)
     for _ in range(max(1, min(args.steps, 3))):
         v, k = cpu_port_run(cores, target_s=8.0, max_steps=10)
         vals.append(v)
     value = float(np.median(vals))
     w = WORKLOAD
     out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 0,
-           "steps": len(vals), "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "steps": len(vals), "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic",
            "config": {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
                                   "300 K, dt 1 fs, NVE", "atoms": int(np.prod(w["cells"])) * 4},

@@ -185,18 +185,20 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist(__grid_
         if (jx < 0 || jy < 0 || jz < 0) continue;
         const int c = jz + g.nc[2] * (jy + g.nc[1] * jx);
         const int jb = S.cell_start[c], je = S.cell_start[c + 1];
-        // i's position in the neighbour cell's frame
-        const float qx = xi.x - (float)off_x(code) * g.cellh_f[0];
-        const float qy = xi.y - (float)off_y(code) * g.cellh_f[1];
-        const float qz = xi.z - (float)off_z(code) * g.cellh_f[2];
+        // i's position in the neighbour cell's frame (offsets of -1, 0, 1
+        // cell selected, not converted: conversions issue at the binary64
+        // rate on GB300)
+        auto shift = [](int o, float h) { return o == 0 ? 0.f : (o > 0 ? h : -h); };
+        const float qx = xi.x - shift(off_x(code), g.cellh_f[0]);
+        const float qy = xi.y - shift(off_y(code), g.cellh_f[1]);
+        const float qz = xi.z - shift(off_z(code), g.cellh_f[2]);
         const int tag = code << 26;
+        // branch-free: a warp's lanes hit at different candidates
         auto test = [&](int j, float4 xj) {
             const float dx = qx - xj.x, dy = qy - xj.y, dz = qz - xj.z;
-            if (dx * dx + dy * dy + dz * dz < rl2)
-            {
-                if (cnt < maxnb) g.nbr[(size_t)cnt * cap + i] = j | tag;
-                cnt++;
-            }
+            const bool hit = dx * dx + dy * dy + dz * dz < rl2;
+            if (hit && cnt < maxnb) g.nbr[(size_t)cnt * cap + i] = j | tag;
+            cnt += hit;
         };
         int j = jb;
         if (code != 13)
