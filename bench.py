@@ -67,19 +67,60 @@ SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0
 FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 145.13e6 / 149616, "eam_single": 100.30e6 / 256000}
 
 
-def clocks_sampler(stop, out):
-    cmd = ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
-           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-           "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]]
-    while not stop.is_set():
-        try:
-            r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=5)
-            if r.returncode == 0 and r.stdout.strip():
-                out.append([p.strip() for p in r.stdout.strip().split(",")])
-        except Exception:
-            pass
-        stop.wait(0.2)
+class ClockSampler:
+    """nvidia-smi clock and throttle readings around a timed region: one
+    query after another (~50 ms apart) from before the region starts until
+    it ends; a reading counts when its query overlapped the region."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.readings = []          # (t_query_start, t_query_end, fields)
+        self.stop_ev = threading.Event()
+        self.first = threading.Event()
+        self.t0 = self.t1 = None
+        self.th = None
+
+    def _loop(self):
+        cmd = ["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+               "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]]
+        while not self.stop_ev.is_set():
+            ta = time.monotonic()
+            try:
+                r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=5)
+                if r.returncode == 0 and r.stdout.strip():
+                    self.readings.append((ta, time.monotonic(), [p.strip() for p in r.stdout.strip().split(",")]))
+                    self.first.set()
+            except Exception:
+                self.first.set()
+                return
+            self.stop_ev.wait(0.05)
+
+    def start(self):
+        """Start sampling; returns once the first reading is in (at most 10 s)."""
+        import shutil
+        if shutil.which("nvidia-smi"):
+            self.th = threading.Thread(target=self._loop, daemon=True)
+            self.th.start()
+            self.first.wait(timeout=10)
+        self.t0 = time.monotonic()
+
+    def stop(self):
+        self.t1 = time.monotonic()
+        self.stop_ev.set()
+        if self.th is not None:
+            self.th.join(timeout=6)
+        return self.summary()
+
+    def summary(self):
+        inside = [f for a, b, f in self.readings if b >= self.t0 and a <= self.t1]
+        if not inside and self.readings:     # region shorter than one query: the nearest reading
+            inside = [min(self.readings, key=lambda r: abs(r[1] - self.t1))[2]]
+        out = summarize_clocks(inside)
+        out["region_s"] = round(self.t1 - self.t0, 3)
+        return out
 
 
 def summarize_clocks(samples):
@@ -203,10 +244,8 @@ def run_ours(args):
 
         ck(L.fmdg_vv_steps(dev, args.warmup, dt, -1, 0, 1.0, 0.0), "warmup")
         ck(L.fmdg_sync(dev), "sync")
-        stop = threading.Event()
-        samples = []
-        th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
-        th.start()
+        sampler = ClockSampler()
+        sampler.start()
         lc0 = C.c_longlong(0)
         L.fmdg_launch_count(dev, C.byref(lc0))
         total_ms = 0.0
@@ -219,9 +258,7 @@ def run_ours(args):
             total_ms += ms.value
         lc1 = C.c_longlong(0)
         L.fmdg_launch_count(dev, C.byref(lc1))
-        stop.set()
-        th.join(timeout=5)
-        clocks = summarize_clocks(samples)
+        clocks = sampler.stop()
         # per-phase device time (separate launches between events)
         ck(L.fmdg_set_profiling(dev, 1), "prof")
         nprof = max(3, min(10, args.steps))
@@ -384,16 +421,12 @@ def run_served(args):
     assert st.running == len(jobs), "the sample does not fit the fleet budget"
     for _ in range(W):              # warm-up; the autotuner picks block sizes here
         fleet.run_resident(1)
-    stop = threading.Event()
-    samples = []
-    th = threading.Thread(target=clocks_sampler, args=(stop, samples), daemon=True)
-    th.start()
+    sampler = ClockSampler()
+    sampler.start()
     k0 = fleet.stats().kernels
     ms = fleet.run_resident(K)
     k1 = fleet.stats().kernels
-    stop.set()
-    th.join(timeout=5)
-    clocks = summarize_clocks(samples)
+    clocks = sampler.stop()
     tuned = {p: fleet.stats().pack_fblk[serve.POTENTIALS[p]["cat"]][1] for p in serve.POT_NAMES}
     phases = {}
     for p in serve.POT_NAMES:
@@ -572,7 +605,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])

@@ -229,6 +229,7 @@ extern "C" void fmdg_destroy(fmdg_sys_t *s)
     free_atoms(s);
     if (s->eam_borrowed) drop_eam(s);
     dfree(s, (void *)s->g.pairs); dfree(s, (void *)s->g.mass); dfree(s, (void *)s->g.eam_elem);
+    dfree(s, (void *)s->g.pairf); dfree(s, (void *)s->g.paird);
     dfree(s, (void *)s->g.eF); dfree(s, (void *)s->g.eFDD); dfree(s, (void *)s->g.erho);
     dfree(s, (void *)s->g.erhoDD); dfree(s, (void *)s->g.ephi); dfree(s, (void *)s->g.ephiDD);
     dfree(s, (void *)s->g.pk_rho); dfree(s, (void *)s->g.pk_phi); dfree(s, (void *)s->g.pk_F);
@@ -292,6 +293,10 @@ extern "C" int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, con
         if (rc) return rc;
         rc = dalloc(s, (fmdg_pair_t **)&s->g.pairs, FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
+        rc = dalloc(s, (float4 **)&s->g.pairf, FMDG_MAXK * FMDG_MAXK);
+        if (rc) return rc;
+        rc = dalloc(s, (float2 **)&s->g.paird, 4 * FMDG_MAXK * FMDG_MAXK);
+        if (rc) return rc;
     }
     FMDG_CK(cudaMemcpy((void *)s->g.mass, s->h_mass, sizeof(double) * nkinds, cudaMemcpyHostToDevice));
     FMDG_CK(cudaMemcpy((void *)s->g.eam_elem, s->h_eam_elem, sizeof(int) * nkinds, cudaMemcpyHostToDevice));
@@ -313,6 +318,18 @@ extern "C" int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table)
         s->cats |= 1 << c;
     }
     FMDG_CK(cudaMemcpy((void *)s->g.pairs, s->h_pairs, sizeof(fmdg_pair_t) * nk2, cudaMemcpyHostToDevice));
+    // binary32 and double-float copies of the parameters, formed here so
+    // that kernel prologues do no binary64 or conversion work
+    float4 pf[FMDG_MAXK * FMDG_MAXK];
+    float2 pd[4 * FMDG_MAXK * FMDG_MAXK];
+    for (int k = 0; k < nk2; k++)
+    {
+        const double *p = s->h_pairs[k].p;
+        pf[k] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
+        for (int q = 0; q < 4; q++) pd[4 * k + q] = df_split(p[q]);
+    }
+    FMDG_CK(cudaMemcpy((void *)s->g.pairf, pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpy((void *)s->g.paird, pd, sizeof(float2) * 4 * nk2, cudaMemcpyHostToDevice));
     s->g.has_eam = (s->cats >> FMDG_POT_EAM) & 1;
     invalidate_graph(s);
     return FMDG_OK;
@@ -559,7 +576,11 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     g.rlist2 = (float)(rlist * rlist);
     const int maxnb = fmdg_list_capacity(s, cell_count, ncell);
     g.maxnb = maxnb;
-    for (int d3 = 0; d3 < 3; d3++) g.cellh_f[d3] = (float)g.cellh[d3];
+    for (int d3 = 0; d3 < 3; d3++)
+    {
+        g.cellh_f[d3] = (float)g.cellh[d3];
+        g.cellh_l[d3] = (float)(g.cellh[d3] - (double)g.cellh_f[d3]);
+    }
     // a skin list needs the list radius below half of every periodic box
     // length (one image inside it) and within two cells; otherwise the
     // exact stencil list is rebuilt every step

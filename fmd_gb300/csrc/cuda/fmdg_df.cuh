@@ -122,29 +122,45 @@ __device__ __forceinline__ dfl df_sqrt(dfl a)
     return df_add({r0, 0.f}, df_mul_f(res, __fmul_rn(0.5f, y0)));
 }
 
-// exp(x) for |x| < 80 (the double-double method of Hida, Li and Bailey):
-// x = n ln2 + t with |t| <= ln2/2, exp(t) = (exp(t / 32))^32, the inner
-// exponential by its Taylor series to degree 8 (|t / 32| < 0.011, truncation
-// below 1e-23), five squarings, then the exact scaling by 2^n.  Relative
-// error about 32 x 2^-47.
+// 2^(j/32), j = 0..31, as double-float (hi, lo): each rounded from a
+// 200-bit value (relative error below 2^-49)
+static __device__ const float2 df_exp2_tab[32] = {
+    {0x1.p+0f, 0.f}, {0x1.059b0ep+0f, -0x1.9d4f52p-25f}, {0x1.0b5586p+0f, 0x1.9f3122p-25f}, {0x1.11301ep+0f, -0x1.fdb496p-25f},
+    {0x1.172b84p+0f, -0x1.c15742p-27f}, {0x1.1d4874p+0f, -0x1.d2e8cap-25f}, {0x1.2387a6p+0f, 0x1.ceac48p-25f}, {0x1.29e9e0p+0f, -0x1.5c0424p-25f},
+    {0x1.306fe0p+0f, 0x1.4636e2p-25f}, {0x1.371a74p+0f, -0x1.18aac6p-25f}, {0x1.3dea64p+0f, 0x1.824684p-25f}, {0x1.44e086p+0f, 0x1.8624b4p-30f},
+    {0x1.4bfdaep+0f, -0x1.593abcp-25f}, {0x1.5342b6p+0f, -0x1.2c5610p-25f}, {0x1.5ab07ep+0f, -0x1.5bd5ecp-27f}, {0x1.6247ecp+0f, -0x1.f8b550p-25f},
+    {0x1.6a09e6p+0f, 0x1.9fcef4p-26f}, {0x1.71f75ep+0f, 0x1.1d8beep-25f}, {0x1.7a1148p+0f, -0x1.829fd0p-25f}, {0x1.82589ap+0f, -0x1.accc7cp-26f},
+    {0x1.8ace54p+0f, 0x1.15506ep-27f}, {0x1.93737cp+0f, -0x1.e64744p-25f}, {0x1.9c4918p+0f, 0x1.51f848p-27f}, {0x1.a5503cp+0f, -0x1.b83b54p-25f},
+    {0x1.ae89fap+0f, -0x1.a94b14p-26f}, {0x1.b7f770p+0f, -0x1.a09438p-25f}, {0x1.c199bep+0f, -0x1.3d56b2p-27f}, {0x1.cb720ep+0f, -0x1.8837ccp-27f},
+    {0x1.d5818ep+0f, -0x1.822dbcp-27f}, {0x1.dfc974p+0f, -0x1.908c94p-25f}, {0x1.ea4afap+0f, 0x1.52486cp-27f}, {0x1.f50766p+0f, -0x1.246eb0p-26f}};
+
+// exp(x) for |x| < 80, table-driven (Tang's method, ACM TOMS 15(2), 1989,
+// in double-float): x = (32 m + j) ln2/32 + r with |r| <= ln2/64, so
+// exp(x) = 2^m 2^(j/32) exp(r); exp(r) by its Taylor series to degree 6
+// (truncation below 4e-18), the terms from r^4 on summed in binary32 (they
+// enter multiplied by r^3 < 1.3e-6); 2^m assembled from exponent bits.
+// Relative error about 1e-13 for |x| <= 30, dominated by the rounding of x
+// itself.
 __device__ __forceinline__ dfl df_exp(dfl x)
 {
-    // ln2 and 1/k! (k = 2..8) as double-float constants
-    const dfl ln2 = {6.931471825e-01f, -1.904654212e-09f};
-    const dfl c[9] = {{1.f, 0.f}, {1.f, 0.f}, {0.5f, 0.f},
-                      {1.666666716e-01f, -4.967053879e-09f}, {4.166666791e-02f, -1.241763470e-09f},
-                      {8.333333768e-03f, -4.346172033e-10f}, {1.388888923e-03f, -3.363109444e-11f},
-                      {1.984127011e-04f, -2.725596875e-12f}, {2.480158764e-05f, -3.406996094e-13f}};
-    // n = x log2(e) rounded to an integer (|n| < 126) by the 1.5 * 2^23
-    // addition; 2^n assembled from its exponent bits
+    const dfl ln2_32 = {0x1.62e43p-6f, -0x1.05c61p-34f};
+    const dfl c3 = {0x1.555556p-3f, -0x1.555556p-28f};   // 1/6
+    // n = x 32/ln2 rounded to an integer (|n| < 2^12) by the 1.5 * 2^23
+    // addition: no conversion instruction
     const float big = 12582912.f;
-    const float nb = __fadd_rn(__fmul_rn(x.hi, 1.442695041f), big);
+    const float nb = __fadd_rn(__fmul_rn(x.hi, 46.16624f), big);
     const float n = __fsub_rn(nb, big);
-    const dfl t = df_scale2(df_sub(x, df_mul_f(ln2, n)), 0.03125f);
-    dfl p = c[8];
-    for (int k = 7; k >= 0; k--) p = df_fma(p, t, c[k]);
-    for (int k = 0; k < 5; k++) p = df_mul(p, p);
-    const float s = __int_as_float((__float_as_int(nb) - 0x4B400000 + 127) << 23);
+    const int ni = __float_as_int(nb) - 0x4B400000;
+    const dfl r = df_sub(x, df_mul_f(ln2_32, n));
+    const float rh = r.hi;
+    const float t = __fmul_rn(rh, __fmaf_rn(rh, __fmaf_rn(rh, 1.f / 720.f, 1.f / 120.f), 1.f / 24.f));
+    dfl p = df_add(c3, {t, 0.f});
+    p = df_add({0.5f, 0.f}, df_mul(r, p));
+    p = df_add({1.f, 0.f}, df_mul(r, p));
+    p = df_add({1.f, 0.f}, df_mul(r, p));
+    const float2 tj = df_exp2_tab[ni & 31];
+    p = df_mul(p, {tj.x, tj.y});
+    const float s = __int_as_float(((ni >> 5) + 127) << 23);
     return {__fmul_rn(p.hi, s), __fmul_rn(p.lo, s)};
 }
 

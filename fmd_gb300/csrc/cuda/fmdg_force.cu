@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
     __shared__ SmemPot sp;
-    load_pot(g, sp);
+    load_pot<!MIXED>(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
     const int group = g.st.group;
     const double dt = g.st.dt;
     __shared__ SmemPot sp;
-    load_pot(g, sp);
+    load_pot<!MIXED>(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];

@@ -78,6 +78,7 @@ struct Geo   // passed by value to kernels
     int maxnb;
     float rlist2;      // binary32 prefilter radius^2 (largest cutoff + margin)
     float cellh_f[3];
+    float cellh_l[3];  // binary32 remainders cellh - cellh_f (cellh_f + cellh_l in double-float)
     // packed spline tables: per interval k {y_k, y_k+1, y''_k, y''_k+1}
     const double4_32a *pk_rho, *pk_phi, *pk_F;     // binary64
     const float4 *pkf_rho, *pkf_phi, *pkf_F;   // binary32 copies (mixed mode)
@@ -103,6 +104,8 @@ struct Geo   // passed by value to kernels
     // potentials
     int nkinds;
     const fmdg_pair_t *pairs;     // nkinds*nkinds, device copy
+    const float4 *pairf;          // nkinds*nkinds: p[0..3] rounded to binary32
+    const float2 *paird;          // nkinds*nkinds*4: p[0..3] as double-float (hi, lo)
     const double *mass;           // nkinds
     const int *eam_elem;          // nkinds
     int nelem, Nrho, Nr2;

@@ -23,17 +23,25 @@ struct SmemPot
     float4 offl[27];    // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
 };
 
+// small integer v (|v| < 2^22) as binary32 without a conversion
+// instruction (conversions issue at the binary64 rate on GB300)
+__device__ __forceinline__ float small_int_f(int v) { return __int_as_float(0x4B400000 + v) - 12582912.f; }
+
+// Block prologue: pair parameters, per-kind constants and the 27 stencil
+// offsets into shared memory.  DF: also the double-float parameters and
+// offset remainders (binary64 mode).  Only the kick coefficient is formed in
+// binary64 here; everything else was formed on the host.
+template <bool DF>
 __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
 {
     const int nk2 = g.nkinds * g.nkinds;
     for (int k = threadIdx.x; k < nk2; k += blockDim.x)
     {
         sp.pairs[k] = g.pairs[k];
-        for (int q = 0; q < 4; q++)
-        {
-            sp.pf[k][q] = (float)g.pairs[k].p[q];
-            sp.pd[k][q] = df_split(g.pairs[k].p[q]);
-        }
+        const float4 f = g.pairf[k];
+        sp.pf[k][0] = f.x; sp.pf[k][1] = f.y; sp.pf[k][2] = f.z; sp.pf[k][3] = f.w;
+        if (DF)
+            for (int q = 0; q < 4; q++) sp.pd[k][q] = g.paird[4 * k + q];
     }
     for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
     {
@@ -43,11 +51,9 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
     }
     for (int c = threadIdx.x; c < 27; c += blockDim.x)
     {
-        const float ox = (float)(c / 9 - 1), oy = (float)((c / 3) % 3 - 1), oz = (float)(c % 3 - 1);
+        const float ox = small_int_f(c / 9 - 1), oy = small_int_f((c / 3) % 3 - 1), oz = small_int_f(c % 3 - 1);
         sp.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], 0.f);
-        sp.offl[c] = make_float4(ox * (float)(g.cellh[0] - (double)g.cellh_f[0]),
-                                 oy * (float)(g.cellh[1] - (double)g.cellh_f[1]),
-                                 oz * (float)(g.cellh[2] - (double)g.cellh_f[2]), 0.f);
+        if (DF) sp.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
     }
     __syncthreads();
 }

@@ -57,16 +57,15 @@ struct SkinOff
     float4 offl[125];   // the remainders (binary64 offset - off): off + offl in double-float
 };
 
+template <bool DF>
 __device__ __forceinline__ void load_offsets(const Geo &g, SkinOff &so)
 {
     const int R = g.srad, W = 2 * R + 1;
     for (int c = threadIdx.x; c < W * W * W; c += blockDim.x)
     {
-        const float ox = (float)(c / (W * W) - R), oy = (float)((c / W) % W - R), oz = (float)(c % W - R);
+        const float ox = small_int_f(c / (W * W) - R), oy = small_int_f((c / W) % W - R), oz = small_int_f(c % W - R);
         so.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], __int_as_float(c));
-        so.offl[c] = make_float4(ox * (float)(g.cellh[0] - (double)g.cellh_f[0]),
-                                 oy * (float)(g.cellh[1] - (double)g.cellh_f[1]),
-                                 oz * (float)(g.cellh[2] - (double)g.cellh_f[2]), 0.f);
+        if (DF) so.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
     }
     __syncthreads();
 }
@@ -392,7 +391,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
     Dyn *dyn = g.dyn;
     if (!dyn->rebuild) return;
     __shared__ SkinOff so;
-    load_offsets(g, so);
+    load_offsets<false>(g, so);
     const int cap = g.cap, maxnb = g.maxnb;
     const int t = bx * blockDim.x + threadIdx.x;
     if (t < cap)
@@ -518,8 +517,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
     const int group = g.st.group;
     __shared__ SmemPot sp;
     __shared__ SkinOff so;
-    load_pot(g, sp);
-    load_offsets(g, so);
+    load_pot<!MIXED>(g, sp);
+    load_offsets<!MIXED>(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
     const int t = bx * blockDim.x + threadIdx.x;
@@ -683,8 +682,8 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     const double dt = g.st.dt;
     __shared__ SmemPot sp;
     __shared__ SkinOff so;
-    load_pot(g, sp);
-    load_offsets(g, so);
+    load_pot<!MIXED>(g, sp);
+    load_offsets<!MIXED>(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
