@@ -107,7 +107,8 @@ __device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const doub
 }
 
 // binary32 pair geometry from cell-local coordinates
-__device__ __forceinline__ float3 geom32(const SmemPot &sp, float4 xi, float4 xj, int code)
+template <bool DF>
+__device__ __forceinline__ float3 geom32(const SmemPotT<DF> &sp, float4 xi, float4 xj, int code)
 {
     const float4 o = sp.off[code];
     return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
@@ -229,8 +230,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
     const Geo &g = loc_geo(loc, bx, nb);
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
-    __shared__ SmemPot sp;
-    load_pot<!MIXED>(g, sp);
+    __shared__ SmemPotT<!MIXED> sp;
+    load_pot(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];
@@ -345,8 +346,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
     const double dt = g.st.dt;
-    __shared__ SmemPot sp;
-    load_pot<!MIXED>(g, sp);
+    __shared__ SmemPotT<!MIXED> sp;
+    load_pot(g, sp);
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
     const Side S = g.side[dyn->cur];

@@ -11,16 +11,25 @@ namespace {
 
 enum { CAT_LJ = 1, CAT_EAM = 2, CAT_MORSE = 3, CAT_HYBRID = 4 };
 
-struct SmemPot
+// Shared per-block potential data.  DF (binary64 mode) adds the
+// double-float parameters and offset remainders; ONE (kernels for systems
+// of one kind) holds the single pair.  The binary32 kernels carry
+// one-element placeholders so that they keep a small shared footprint: the
+// rest of the SM's 256 KB of L1/shared stays L1 cache for the list and
+// position gathers.
+template <bool DF, bool ONE = false>
+struct SmemPotT
 {
-    fmdg_pair_t pairs[FMDG_MAXK * FMDG_MAXK];
-    float pf[FMDG_MAXK * FMDG_MAXK][4];
-    float2 pd[FMDG_MAXK * FMDG_MAXK][4];   // double-float parameters (binary64 mode)
+    static constexpr int NP = ONE ? 1 : FMDG_MAXK * FMDG_MAXK;
+    static constexpr int NPD = DF ? NP : 1;
+    fmdg_pair_t pairs[NP];
+    float pf[NP][4];
+    float2 pd[NPD][4];  // double-float parameters (binary64 mode)
     double mass[FMDG_MAXK];
     double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
     float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
-    float4 offl[27];    // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
+    float4 offl[DF ? 27 : 1];   // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
 };
 
 // small integer v (|v| < 2^22) as binary32 without a conversion
@@ -31,10 +40,10 @@ __device__ __forceinline__ float small_int_f(int v) { return __int_as_float(0x4B
 // offsets into shared memory.  DF: also the double-float parameters and
 // offset remainders (binary64 mode).  Only the kick coefficient is formed in
 // binary64 here; everything else was formed on the host.
-template <bool DF>
-__device__ __forceinline__ void load_pot(const Geo &g, SmemPot &sp)
+template <bool DF, bool ONE>
+__device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
 {
-    const int nk2 = g.nkinds * g.nkinds;
+    const int nk2 = ONE ? 1 : g.nkinds * g.nkinds;
     for (int k = threadIdx.x; k < nk2; k += blockDim.x)
     {
         sp.pairs[k] = g.pairs[k];
@@ -190,8 +199,8 @@ __device__ __forceinline__ GeomDF geom_df_of64(const Geom64 &q)
 // -- LJ src/lj.h:35-56, Morse src/morse.h:35-56, EAM src/eam.h:186-226 --
 // for a pair of category cat: f_i += fa * rv, energy share eh.  fpj() gives
 // F'(rho_j) as a double-float; it is called for EAM pairs only.
-template <typename FPJ>
-__device__ __forceinline__ void df_pair(const Geo &g, const SmemPot &sp, int pidx, const fmdg_pair_t &pp, int cat,
+template <typename FPJ, bool DF, bool ONE>
+__device__ __forceinline__ void df_pair(const Geo &g, const SmemPotT<DF, ONE> &sp, int pidx, const fmdg_pair_t &pp, int cat,
                                         const GeomDF &p, dfl fpi, dfl inv_h, float kmax, int nint, size_t ne,
                                         FPJ &&fpj, dfl &fa, dfl &eh)
 {

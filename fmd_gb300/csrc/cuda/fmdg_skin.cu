@@ -51,14 +51,15 @@ namespace {
 constexpr int SLOT_BITS = 25;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
-struct SkinOff
+template <bool DF>   // DF: binary64 mode (the remainders); else a placeholder
+struct SkinOffT
 {
     float4 off[125];    // image offset of each stencil code, binary32; .w: the code's bits
-    float4 offl[125];   // the remainders (binary64 offset - off): off + offl in double-float
+    float4 offl[DF ? 125 : 1];   // the remainders (binary64 offset - off): off + offl in double-float
 };
 
 template <bool DF>
-__device__ __forceinline__ void load_offsets(const Geo &g, SkinOff &so)
+__device__ __forceinline__ void load_offsets(const Geo &g, SkinOffT<DF> &so)
 {
     const int R = g.srad, W = 2 * R + 1;
     for (int c = threadIdx.x; c < W * W * W; c += blockDim.x)
@@ -116,7 +117,8 @@ __device__ __forceinline__ float axis_gap(int o, float u, float h)
 // fallback occurrence (code < 0 in o.w: current-cell frame, formed from the
 // binary64 positions); the cutoff decision within 1e-6 relative of the
 // cutoff is the binary64 minimum-image one.
-__device__ __forceinline__ GeomDF skin_geom_df(const Geo &g, const SkinOff &so, int t, float4 ih, float4 il, int js,
+template <bool DF>
+__device__ __forceinline__ GeomDF skin_geom_df(const Geo &g, const SkinOffT<DF> &so, int t, float4 ih, float4 il, int js,
                                                float4 xj, float4 o)
 {
     const int code = __float_as_int(o.w);
@@ -200,8 +202,8 @@ struct NoRound
 // list radius), and of the occurrences of a neighbour (a cell recurs in the
 // stencil when an axis has fewer than 2R + 1 cells) only the image within
 // the list radius is passed on.
-template <bool PF = false, typename F, typename R>
-__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
+template <bool PF = false, typename F, typename R, bool DF>
+__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOffT<DF> &so, int t, int i,
                                                    float4 &xi, F &&f, R &&r)
 {
     const int cnt = g.nbr_count[t];
@@ -256,8 +258,8 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
     }
 }
 
-template <typename F>
-__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOff &so, int t, int i,
+template <typename F, bool DF>
+__device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, const SkinOffT<DF> &so, int t, int i,
                                                    float4 &xi, F &&f)
 {
     for_each_slot_pair(g, S, so, t, i, xi, f, NoRound{});
@@ -390,8 +392,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
     if (loc_idle(loc, g)) return;
     Dyn *dyn = g.dyn;
     if (!dyn->rebuild) return;
-    __shared__ SkinOff so;
-    load_offsets<false>(g, so);
+    __shared__ SkinOffT<false> so;
+    load_offsets(g, so);
     const int cap = g.cap, maxnb = g.maxnb;
     const int t = bx * blockDim.x + threadIdx.x;
     if (t < cap)
@@ -515,10 +517,10 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
     const Geo &g = loc_geo(loc, bx, nb);
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
-    __shared__ SmemPot sp;
-    __shared__ SkinOff so;
-    load_pot<!MIXED>(g, sp);
-    load_offsets<!MIXED>(g, so);
+    __shared__ SmemPotT<!MIXED, LEAN> sp;
+    __shared__ SkinOffT<!MIXED> so;
+    load_pot(g, sp);
+    load_offsets(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
     const int t = bx * blockDim.x + threadIdx.x;
@@ -680,10 +682,10 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
     const double dt = g.st.dt;
-    __shared__ SmemPot sp;
-    __shared__ SkinOff so;
-    load_pot<!MIXED>(g, sp);
-    load_offsets<!MIXED>(g, so);
+    __shared__ SmemPotT<!MIXED, LEAN> sp;
+    __shared__ SkinOffT<!MIXED> so;
+    load_pot(g, sp);
+    load_offsets(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
