@@ -180,6 +180,7 @@ struct fmdg_sys
     char *arena;                  // one device allocation holding the per-atom and per-cell buffers
     bool skin_set;                // skin chosen by the caller (any precision)
     int list_capacity;            // neighbour-list entries per atom; 0: estimated at upload
+    int build_lanes;              // threads per atom of a skin-list build; 0: by size
 };
 
 // ---- which system a thread block works on ------------------------------------

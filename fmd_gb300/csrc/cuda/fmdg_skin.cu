@@ -383,6 +383,83 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     if (!lazy && !dyn->rebuild) slot_rel_build(g, dyn, t, x, kb);
 }
 
+// The pruned stencil walk of a list build: f(code, c, ax, ay, az) for every
+// cell c of the stencil within the list radius of xi (by the axis gaps of
+// xi to the cell's faces), in stencil order, with the cell's image offset
+// folded into the atom's position once per cell (ax, ay, az).
+template <typename F>
+__device__ __forceinline__ void for_each_build_cell(const Geo &g, const SkinOffT<false> &so, CellXYZ ci, float4 xi,
+                                                    F &&f)
+{
+    const int R = g.srad, W = 2 * R + 1;
+    const float lim2 = g.rskin2 * 1.0001f;
+    for (int ox = -R; ox <= R; ox++)
+    {
+        const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
+        if (gx * gx > lim2) continue;
+        int cx = ci.x + ox;
+        if (cx < 0 || cx >= g.nc[0])
+        {
+            if (!g.pbc[0]) continue;
+            cx = (cx + 2 * g.nc[0]) % g.nc[0];
+        }
+        for (int oy = -R; oy <= R; oy++)
+        {
+            const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
+            if (gx * gx + gy * gy > lim2) continue;
+            int cy = ci.y + oy;
+            if (cy < 0 || cy >= g.nc[1])
+            {
+                if (!g.pbc[1]) continue;
+                cy = (cy + 2 * g.nc[1]) % g.nc[1];
+            }
+            for (int oz = -R; oz <= R; oz++)
+            {
+                const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
+                if (gx * gx + gy * gy + gz * gz > lim2) continue;
+                int cz = ci.z + oz;
+                if (cz < 0 || cz >= g.nc[2])
+                {
+                    if (!g.pbc[2]) continue;
+                    cz = (cz + 2 * g.nc[2]) % g.nc[2];
+                }
+                const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
+                const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
+                const float4 o = so.off[code];
+                f(code, c, xi.x - o.x, xi.y - o.y, xi.z - o.z);
+            }
+        }
+    }
+}
+
+// per-slot state recorded with a new list: build cell and build-frame
+// position (+ its double-float remainder in binary64 mode)
+__device__ __forceinline__ void record_build(const Geo &g, const Side &S, int t, int i, float4 xi)
+{
+    g.cb[t] = S.cell_of[i];
+    g.xl[t] = xi;
+    g.xb[t] = xi;
+    if (g.prec == FMDG_PREC_FP64) g.xll[t] = g.xlo4[i];
+}
+
+// the last block of a build to finish clears the system's rebuild flag
+__device__ __forceinline__ void finish_build(Dyn *dyn, int nb)
+{
+    __shared__ unsigned ticket;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        __threadfence();
+        ticket = atomicAdd(&dyn->nl_done, 1u);
+    }
+    __syncthreads();
+    if (ticket == (unsigned)nb - 1 && threadIdx.x == 0)
+    {
+        dyn->nl_done = 0;
+        dyn->rebuild = 0;
+    }
+}
+
 // one thread per slot; every block leaves at once when no rebuild is due
 template <class L>
 __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__grid_constant__ const L loc)
@@ -409,11 +486,9 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
             // hits shift through a four-entry register buffer (in order:
             // x oldest); every fourth hit writes one 16-byte row; the
             // buffer update is branch-free (a warp's lanes hit at different
-            // candidates).  The stencil walk is for_each_candidate's, with
-            // the cell's image offset folded into the atom's position once
-            // per cell and the self test only in the atom's own cell; the
-            // radius is widened by 1e-5 relative so the folded rounding can
-            // only add entries.
+            // candidates).  The self test is only in the atom's own cell;
+            // the radius is widened by 1e-5 relative so the folded rounding
+            // of the cell offsets can only add entries.
             int4 buf = make_int4(0, 0, 0, 0);
             const float rb2 = rl2 * 1.00001f;
             auto take = [&](int j, int code, float ax, float ay, float az) {
@@ -429,54 +504,18 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
                 cnt += hit;
                 if (hit && (cnt & 3) == 0 && cnt <= maxnb) row[(size_t)((cnt >> 2) - 1) * cap] = buf;
             };
-            const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
             const int R = g.srad, W = 2 * R + 1;
-            const float lim2 = g.rskin2 * 1.0001f;
-            for (int ox = -R; ox <= R; ox++)
-            {
-                const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
-                if (gx * gx > lim2) continue;
-                int cx = ci.x + ox;
-                if (cx < 0 || cx >= g.nc[0])
+            const int center = (R * W + R) * W + R;
+            for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
+                const int jb = S.cell_start[c], je = S.cell_start[c + 1];
+                if (code == center)
                 {
-                    if (!g.pbc[0]) continue;
-                    cx = (cx + 2 * g.nc[0]) % g.nc[0];
+                    for (int j = jb; j < i; j++) take(j, code, ax, ay, az);
+                    for (int j = i + 1; j < je; j++) take(j, code, ax, ay, az);
                 }
-                for (int oy = -R; oy <= R; oy++)
-                {
-                    const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
-                    if (gx * gx + gy * gy > lim2) continue;
-                    int cy = ci.y + oy;
-                    if (cy < 0 || cy >= g.nc[1])
-                    {
-                        if (!g.pbc[1]) continue;
-                        cy = (cy + 2 * g.nc[1]) % g.nc[1];
-                    }
-                    for (int oz = -R; oz <= R; oz++)
-                    {
-                        const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
-                        if (gx * gx + gy * gy + gz * gz > lim2) continue;
-                        int cz = ci.z + oz;
-                        if (cz < 0 || cz >= g.nc[2])
-                        {
-                            if (!g.pbc[2]) continue;
-                            cz = (cz + 2 * g.nc[2]) % g.nc[2];
-                        }
-                        const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
-                        const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
-                        const float4 o = so.off[code];
-                        const float ax = xi.x - o.x, ay = xi.y - o.y, az = xi.z - o.z;
-                        const int jb = S.cell_start[c], je = S.cell_start[c + 1];
-                        if (ox == 0 && oy == 0 && oz == 0)
-                        {
-                            for (int j = jb; j < i; j++) take(j, code, ax, ay, az);
-                            for (int j = i + 1; j < je; j++) take(j, code, ax, ay, az);
-                        }
-                        else
-                            for (int j = jb; j < je; j++) take(j, code, ax, ay, az);
-                    }
-                }
-            }
+                else
+                    for (int j = jb; j < je; j++) take(j, code, ax, ay, az);
+            });
             const int rem = cnt & 3;
             if (rem && cnt <= maxnb)
             {
@@ -484,27 +523,76 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
                                 : (rem == 2) ? make_int4(buf.z, buf.w, 0, 0) : make_int4(buf.y, buf.z, buf.w, 0);
                 row[(size_t)(cnt >> 2) * cap] = last;
             }
-            g.cb[t] = S.cell_of[i];
-            g.xl[t] = xi;
-            g.xb[t] = xi;
-            if (g.prec == FMDG_PREC_FP64) g.xll[t] = g.xlo4[i];
+            record_build(g, S, t, i, xi);
         }
         g.nbr_count[t] = cnt;
     }
-    // the last block to finish clears the flag
-    __shared__ unsigned ticket;
-    __syncthreads();
-    if (threadIdx.x == 0)
+    finish_build(dyn, nb);
+}
+
+// Single-system build (a served job's admission, the fmd.h path) with G
+// lanes per slot: a system of 10^4-10^5 atoms gives one thread per slot too
+// few warps to hide the gather latency of its long candidate walk.  The G
+// lanes of a slot test G consecutive candidates of a cell together and
+// place their hits in candidate order (ballot + prefix count), so the list
+// is the one-thread build's, entry for entry.
+template <int G>
+__global__ void __launch_bounds__(128) k_nlist_skin_grp(__grid_constant__ const LocOne loc)
+{
+    static_assert(G >= 2 && G <= 32 && (G & (G - 1)) == 0, "G: a power of two up to the warp");
+    const Geo &g = loc.g;
+    Dyn *dyn = g.dyn;
+    if (!dyn->rebuild) return;
+    __shared__ SkinOffT<false> so;
+    load_offsets(g, so);
+    const int cap = g.cap, maxnb = g.maxnb;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) / G;   // uniform over a group
+    const int gl = threadIdx.x & (G - 1);
+    const int gbase = threadIdx.x & 31 & ~(G - 1);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : ((1u << G) - 1u) << gbase;
+    if (t < cap)
     {
-        __threadfence();
-        ticket = atomicAdd(&dyn->nl_done, 1u);
+        int cnt = 0;
+        const int i = g.pos[t];
+        if (i >= 0)
+        {
+            const Side S = g.side[dyn->cur];
+            const float4 xi = g.xf4[i];
+            const float rb2 = g.rskin2 * 1.00001f;   // as in k_nlist_skin
+            int *ent = g.nbr;   // entry k of slot t: int4 row (k / 4) * cap + t, component k % 4
+            const int R = g.srad, W = 2 * R + 1;
+            const int center = (R * W + R) * W + R;
+            // the group's control flow depends on its slot only: every
+            // ballot has all of the group's lanes
+            for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
+                const int jb = S.cell_start[c], je = S.cell_start[c + 1];
+                const bool self = code == center;
+                for (int base = jb; base < je; base += G)
+                {
+                    const int j = base + gl;
+                    bool hit = false;
+                    if (j < je && !(self && j == i))
+                    {
+                        const float4 xj = __ldg(g.xf4 + j);
+                        const float dx = ax - xj.x, dy = ay - xj.y, dz = az - xj.z;
+                        hit = dx * dx + dy * dy + dz * dz < rb2;
+                    }
+                    const unsigned m = __ballot_sync(gmask, hit) >> gbase;
+                    if (hit)
+                    {
+                        const int k = cnt + __popc(m & ((1u << gl) - 1u));
+                        if (k < maxnb)
+                            ent[((size_t)(k >> 2) * cap + t) * 4 + (k & 3)] =
+                                (int)((unsigned)S.slot[j] | ((unsigned)code << SLOT_BITS));
+                    }
+                    cnt += __popc(m);
+                }
+            });
+            if (gl == 0) record_build(g, S, t, i, xi);
+        }
+        if (gl == 0) g.nbr_count[t] = cnt;
     }
-    __syncthreads();
-    if (ticket == (unsigned)nb - 1 && threadIdx.x == 0)
-    {
-        dyn->nl_done = 0;
-        dyn->rebuild = 0;
-    }
+    finish_build(dyn, gridDim.x);
 }
 
 // EAM pass 1 + embedding (src/eam.h:270-406, src/eam.c:160-179), one
@@ -1073,7 +1161,24 @@ int fmdg_skin_launch_nlist(fmdg_sys_t *s)
 {
     const LocOne L{s->g};
     k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L, 0);
-    k_nlist_skin<<<fmdg_force_blocks(s), s->fblk, 0, s->stream>>>(L);
+    // below ~2^18 slots the build runs G lanes per slot (at least 2^18
+    // threads, G <= 16); larger systems fill the device with one per slot
+    const int cap = s->g.cap;
+    int G = s->build_lanes;
+    if (G == 0)
+    {
+        G = 1;
+        while (G < 16 && (long long)cap * G < (1 << 18)) G *= 2;
+    }
+    const int nbg = fmdg_grid(cap > 0 ? cap * G : 1, 128);
+    switch (G)
+    {
+    case 2: k_nlist_skin_grp<2><<<nbg, 128, 0, s->stream>>>(L); break;
+    case 4: k_nlist_skin_grp<4><<<nbg, 128, 0, s->stream>>>(L); break;
+    case 8: k_nlist_skin_grp<8><<<nbg, 128, 0, s->stream>>>(L); break;
+    case 16: k_nlist_skin_grp<16><<<nbg, 128, 0, s->stream>>>(L); break;
+    default: k_nlist_skin<<<fmdg_force_blocks(s), s->fblk, 0, s->stream>>>(L); break;
+    }
     s->launches += 2;
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;

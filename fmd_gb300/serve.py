@@ -87,6 +87,7 @@ def bind(L):
         "fmdg_srv_set_eam": ([vp, i, i, i, d, i, d] + [P(d)] * 6, i),
         "fmdg_srv_set_tuning": ([vp, i], i), "fmdg_srv_set_skin": ([vp, d], i),
         "fmdg_srv_set_list_capacity": ([vp, i], i), "fmdg_set_list_capacity": ([vp, i], i),
+        "fmdg_set_build_lanes": ([vp, i], i),
         "fmdg_srv_submit": ([vp, P(JobDesc), P(C.c_longlong)], i),
         "fmdg_srv_progress": ([vp, i, P(i)], i), "fmdg_srv_result": ([vp, C.c_longlong, P(JobResult)], i),
         "fmdg_srv_state": ([vp, C.c_longlong, P(d), P(d), P(d), P(C.c_uint)], i),
@@ -397,7 +398,8 @@ class Single:
     path libfmd.so's fmd_dync_integrate drives): its own system, steps
     replayed from one captured graph, no packing."""
 
-    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0, kind=None, list_capacity=0):
+    def __init__(self, L, pot, x, v, l, precision=PREC_FP64, eam=None, device=0, kind=None, list_capacity=0,
+                 build_lanes=0):
         self.L = L
         h = C.c_void_p()
         check(L, L.fmdg_create(C.byref(h), device), "fmdg_create")
@@ -419,6 +421,7 @@ class Single:
                                     _dp(t["phiDD"])), "set_eam")
         check(L, L.fmdg_set_precision(h, precision), "set_precision")
         check(L, L.fmdg_set_list_capacity(h, list_capacity), "set_list_capacity")
+        check(L, L.fmdg_set_build_lanes(h, build_lanes), "set_build_lanes")
         n = len(x)
         xs = np.ascontiguousarray(x[order])
         vs = np.ascontiguousarray(v[order])

@@ -353,6 +353,25 @@ def test_list_overflow_fallback(L, eam, pot, precision):
     assert err <= (1e-10 if precision == serve.PREC_FP64 else 1e-5), err
 
 
+@pytest.mark.parametrize("pot,cap", [("lj", 0), ("morse", 0), ("eam", 0), ("cuar", 0), ("cuar", 32)])
+def test_single_build_lanes_same_list(L, eam, pot, cap):
+    """Skin-list builds with 1, 2, 4, 8 and 16 threads per atom build the
+    same list, entry for entry (also when it overflows): the same trajectory
+    bit for bit, the binary32 partial sums flushing at the same entries.
+    60 steps at 900 K include list rebuilds after the first build."""
+    x, v, l, kind = _sys(pot, 6, 900.0, 95)
+    res = []
+    for lanes in (1, 2, 4, 8, 16):
+        one = serve.Single(L, pot, x, v, l, precision=serve.PREC_MIXED, eam=eam, kind=kind, list_capacity=cap,
+                           build_lanes=lanes)
+        one.steps(60)
+        res.append(_by_id(one.state()))
+        one.close()
+    for r in res[1:]:
+        for a, b in zip(res[0], r):
+            np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("precision", [serve.PREC_FP64, serve.PREC_MIXED])
 def test_single_list_overflow_fallback(L, eam, precision):
     """The single-system path with lists of 32 entries: the same pairs in
