@@ -200,8 +200,14 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     fmdg_sys_t *s = (fmdg_sys_t *)calloc(1, sizeof(fmdg_sys_t));
     if (!s) return FMDG_E_NOMEM;
     s->device = device;
-    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { free(s); return fmdg_fail("cudaStreamCreate", e); }
+    // a system's own stream has the device's highest priority: a served
+    // job's set-up (first list, forces, thermo record) then takes SM slots
+    // ahead of the packed chunks already queued instead of waiting behind
+    // them (a lone fmd.h system has no other stream to compete with)
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    cudaError_t e = cudaStreamCreateWithPriority(&s->stream, cudaStreamNonBlocking, prio_greatest);
+    if (e != cudaSuccess) { free(s); return fmdg_fail("cudaStreamCreateWithPriority", e); }
     FMDG_CK(cudaEventCreate(&s->ev0));
     FMDG_CK(cudaEventCreate(&s->ev1));
     for (int k = 0; k < 6; k++) FMDG_CK(cudaEventCreate(&s->pev[k]));
