@@ -54,10 +54,10 @@ __global__ void k_bin_classify(__grid_constant__ const L loc, int mode, int lazy
     if (lazy && !g.dyn->rebuild) return;
     const double dt = g.st.dt;
     const int group = g.st.group, thermostat = g.st.thermostat;
-    // half kick dt * 0.5 / m per kind: one binary64 division per kind, not
-    // per atom (the same operations, so the same bits)
+    // half kick dt * 0.5 / m per kind, formed on the host (set_step_dt):
+    // the reference's operations, so the same bits as per atom
     __shared__ double hk[FMDG_MAXK];
-    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = __ddiv_rn(__dmul_rn(dt, 0.5), g.mass[threadIdx.x]);
+    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = g.st.hk[threadIdx.x];
     __syncthreads();
     Dyn *dyn = g.dyn;
     const int n = dyn->n;
@@ -400,7 +400,7 @@ int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int therm
 {
     Geo &g = s->g;
     cudaStream_t st = s->stream;
-    g.st.dt = dt;
+    set_step_dt(s, dt);
     g.st.group = group;
     g.st.thermostat = thermostat;
     const LocOne L{g};

@@ -629,7 +629,7 @@ int fmdg_launch_pair_forces(fmdg_sys_t *s, int group, int finish, double dt, int
 {
     StepArgs &a = s->g.st;
     a.group = group;
-    a.dt = dt;
+    set_step_dt(s, dt);
     a.thermostat = thermostat;
     a.tau = tau;
     a.T0 = T0;

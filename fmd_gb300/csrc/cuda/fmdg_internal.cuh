@@ -57,6 +57,7 @@ struct StepArgs
 {
     double dt, tau, T0;
     int group, thermostat;
+    double hk[FMDG_MAXK];   // half-kick coefficient dt * 0.5 / m of each kind (set_step_dt)
 };
 
 struct Geo   // passed by value to kernels
@@ -182,6 +183,16 @@ struct fmdg_sys
     int list_capacity;            // neighbour-list entries per atom; 0: estimated at upload
     int build_lanes;              // threads per atom of a skin-list build; 0: by size
 };
+
+// time step of the next launches and the half-kick coefficients
+// dt * 0.5 / m of every kind, in binary64 as the reference forms them
+// (src/integrators.c:104-106); formed here once instead of by a binary64
+// division at the start of every thread block
+inline void set_step_dt(fmdg_sys_t *s, double dt)
+{
+    s->g.st.dt = dt;
+    for (int k = 0; k < FMDG_MAXK; k++) s->g.st.hk[k] = k < s->nkinds ? dt * 0.5 / s->h_mass[k] : 0.0;
+}
 
 // ---- which system a thread block works on ------------------------------------
 // The step kernels are templates over a locator.

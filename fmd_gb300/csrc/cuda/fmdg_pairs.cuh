@@ -38,8 +38,8 @@ __device__ __forceinline__ float small_int_f(int v) { return __int_as_float(0x4B
 
 // Block prologue: pair parameters, per-kind constants and the 27 stencil
 // offsets into shared memory.  DF: also the double-float parameters and
-// offset remainders (binary64 mode).  Only the kick coefficient is formed in
-// binary64 here; everything else was formed on the host.
+// offset remainders (binary64 mode).  Everything was formed on the host
+// (no binary64 or conversion work here).
 template <bool DF, bool ONE>
 __device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
 {
@@ -55,7 +55,7 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
     for (int k = threadIdx.x; k < g.nkinds; k += blockDim.x)
     {
         sp.mass[k] = g.mass[k];
-        sp.hk[k] = __ddiv_rn(__dmul_rn(g.st.dt, 0.5), g.mass[k]);
+        sp.hk[k] = g.st.hk[k];
         sp.elem[k] = g.eam_elem[k];
     }
     for (int c = threadIdx.x; c < 27; c += blockDim.x)

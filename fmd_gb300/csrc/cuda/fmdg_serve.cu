@@ -280,7 +280,7 @@ int setup_job(fmdg_server_t *S, Job *j)
     if ((rc = fmdg_compute_forces(s, -1))) return rc;
     if ((rc = fmdg_thermo(s, -1, &j->th0))) return rc;
     if ((rc = fmdg_set_steps_left(s, j->steps))) return rc;
-    s->g.st.dt = j->dt;
+    set_step_dt(s, j->dt);
     s->g.st.tau = 1.0;
     s->g.st.T0 = 0.0;
     s->g.st.group = -1;

@@ -313,7 +313,7 @@ __global__ void k_skin_start(__grid_constant__ const L loc)
     const double dt = g.st.dt;
     const int group = g.st.group, thermostat = g.st.thermostat;
     __shared__ double hk[FMDG_MAXK];
-    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = __ddiv_rn(__dmul_rn(dt, 0.5), g.mass[threadIdx.x]);
+    if (threadIdx.x < g.nkinds) hk[threadIdx.x] = g.st.hk[threadIdx.x];
     __syncthreads();
     Dyn *dyn = g.dyn;
     if (bx == 0 && threadIdx.x == 0) dyn->time += dt;
@@ -1161,14 +1161,15 @@ int fmdg_skin_launch_nlist(fmdg_sys_t *s)
 {
     const LocOne L{s->g};
     k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L, 0);
-    // below ~2^18 slots the build runs G lanes per slot (at least 2^18
-    // threads, G <= 16); larger systems fill the device with one per slot
+    // up to 2^17 slots the build runs G lanes per slot (G <= 16, the
+    // largest with cap * G <= 2^18 threads); larger systems fill the device
+    // with one thread per slot
     const int cap = s->g.cap;
     int G = s->build_lanes;
     if (G == 0)
     {
         G = 1;
-        while (G < 16 && (long long)cap * G < (1 << 18)) G *= 2;
+        while (G < 16 && (long long)cap * G * 2 <= (1 << 18)) G *= 2;
     }
     const int nbg = fmdg_grid(cap > 0 ? cap * G : 1, 128);
     switch (G)
