@@ -64,7 +64,7 @@ SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0
 # divided by the atoms of the launch): packed Morse on a 149616-atom pack,
 # single-system mixed EAM on the 256000-atom system (both skin lists); the traffic
 # grows with the atoms (the neighbour list dominates it)
-FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 145.13e6 / 149616, "eam_single": 100.30e6 / 256000}
+FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 144.87e6 / 149616, "eam_single": 100.40e6 / 256000}
 
 
 class ClockSampler:
@@ -451,7 +451,7 @@ def run_served(args):
     achieved = fl / (phases[dom]["force_ms"] * 1e-3) / 1e12
 
     # --- e2e: the sample streamed through the request loop ---------------
-    srv = serve.Server(L, budget_bytes=64 << 30, max_jobs=1024, chunk_steps=16, eam=eam)
+    srv = serve.Server(L, budget_bytes=64 << 30, max_jobs=1024, chunk_steps=32, eam=eam)
     ids = [None] * len(jobs)
     nxt = 0
     t0 = srv.now()

@@ -76,6 +76,7 @@ struct Job
     int fail_code = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
     fmdg_thermo_t th0, th1;
+    fmdg_thermo_t *th0_pin = nullptr;   // pinned landing place of th0 until retirement
     unsigned errs = 0;
     cudaEvent_t ready = nullptr;
     std::vector<double> fx, fv, fF;
@@ -156,6 +157,8 @@ struct fmdg_server
     Tuner tuners[4][2];
     std::map<int, fmdg_sys_t *> eam_owner;   // shared EAM tables by key
     std::vector<cudaEvent_t> free_events;
+    std::vector<fmdg_thermo_t *> free_pins;   // pinned host thermo records (admission)
+    std::vector<void *> pin_blocks;
     long long admitted = 0, finished = 0, failed = 0;
     long long kernels = 0;            // kernels launched (graph replays included)
     double atom_steps_done = 0.0;
@@ -179,6 +182,30 @@ cudaEvent_t get_event(fmdg_server_t *S)
 }
 
 void put_event(fmdg_server_t *S, cudaEvent_t e) { if (e) S->free_events.push_back(e); }
+
+// pinned host records, allocated 256 at a time (cudaMallocHost is slow)
+fmdg_thermo_t *get_pin(fmdg_server_t *S)
+{
+    if (S->free_pins.empty())
+    {
+        void *b = nullptr;
+        if (cudaMallocHost(&b, 256 * sizeof(fmdg_thermo_t)) != cudaSuccess) return nullptr;
+        S->pin_blocks.push_back(b);
+        for (int k = 255; k >= 0; k--) S->free_pins.push_back((fmdg_thermo_t *)b + k);
+    }
+    fmdg_thermo_t *p = S->free_pins.back();
+    S->free_pins.pop_back();
+    return p;
+}
+
+// the job's initial thermo record, once its stream has drained
+void take_th0(fmdg_server_t *S, Job *j)
+{
+    if (!j->th0_pin) return;
+    j->th0 = *j->th0_pin;
+    S->free_pins.push_back(j->th0_pin);
+    j->th0_pin = nullptr;
+}
 
 template <typename F>
 void each_pack(fmdg_server_t *S, F f)
@@ -223,9 +250,10 @@ int fail_job(fmdg_server_t *S, Job *j, int code, bool admitted)
     j->t_done = wall_s() - S->t0;
     if (j->sys)
     {
-        fmdg_destroy(j->sys);
+        fmdg_destroy(j->sys);   // (drains the job's stream)
         j->sys = nullptr;
     }
+    take_th0(S, j);
     if (j->ready)
     {
         put_event(S, j->ready);
@@ -278,7 +306,12 @@ int setup_job(fmdg_server_t *S, Job *j)
     // the packed kernels walk skin lists only
     if (!s->g.skin_on) return fmdg_set_error("fmdg_srv: the job's box admits no skin list");
     if ((rc = fmdg_compute_forces(s, -1))) return rc;
-    if ((rc = fmdg_thermo(s, -1, &j->th0))) return rc;
+    // the initial thermo record lands in pinned host memory on the job's
+    // stream and is read at retirement: admission never waits for the GPU,
+    // which is busy with the packed chunks
+    if ((rc = fmdg_launch_thermo(s, -1, 0, 0.0, 1.0, 0.0))) return rc;
+    if (!(j->th0_pin = get_pin(S))) return fmdg_set_error("fmdg_srv: cannot allocate pinned host memory");
+    FMDG_CK(cudaMemcpyAsync(j->th0_pin, s->g.thermo, sizeof(fmdg_thermo_t), cudaMemcpyDeviceToHost, s->stream));
     if ((rc = fmdg_set_steps_left(s, j->steps))) return rc;
     set_step_dt(s, j->dt);
     s->g.st.tau = 1.0;
@@ -443,7 +476,8 @@ int launch_chunk(fmdg_server_t *S, Pack &p)
 int retire(fmdg_server_t *S, Job *j)
 {
     fmdg_sys_t *s = j->sys;
-    int rc = fmdg_get_thermo(s, &j->th1);
+    int rc = fmdg_get_thermo(s, &j->th1);   // (drains the job's stream)
+    take_th0(S, j);
     if (!rc) rc = fmdg_get_errors(s, &j->errs, 0);
     if (!rc && j->keep_state)
     {
@@ -588,6 +622,7 @@ extern "C" void fmdg_srv_destroy(fmdg_server_t *S)
     }
     for (auto &kv : S->eam_owner) fmdg_destroy(kv.second);
     for (cudaEvent_t e : S->free_events) cudaEventDestroy(e);
+    for (void *b : S->pin_blocks) cudaFreeHost(b);
     if (S->join) cudaStreamDestroy(S->join);
     if (S->jev0) cudaEventDestroy(S->jev0);
     if (S->jev1) cudaEventDestroy(S->jev1);

@@ -292,7 +292,8 @@ typedef struct
     int error;                /* FMDG_E_* of a failed job */
     int n, steps;
     double t_submit, t_start, t_done;   /* seconds on the server clock */
-    fmdg_thermo_t first, last;          /* before the first step, after the last */
+    fmdg_thermo_t first, last;          /* before the first step, after the last
+                                           (both filled once the job is done) */
     unsigned errbits;                   /* sticky device error bits */
     unsigned pad;
     double device_bytes;                /* admission estimate */
