@@ -174,6 +174,26 @@ def test_alone_vs_mix(L, eam):
     srv.close()
 
 
+@pytest.mark.parametrize("pot", ["lj", "morse", "eam", "cuar"])
+def test_first_thermo_record(L, eam, pot):
+    """A served job's record before its first step (formed at admission,
+    read back at retirement) equals the single-system path's initial record
+    of the same atoms."""
+    x, v, l, kind = _sys(pot, 6, 600.0, 97)
+    srv = serve.Server(L, chunk_steps=8, eam=eam)
+    jid = srv.submit(pot, x, v, l, 10, precision=serve.PREC_FP64, kind=kind)
+    srv.drain()
+    r = srv.result(jid)
+    srv.close()
+    one = serve.Single(L, pot, x, v, l, precision=serve.PREC_FP64, eam=eam, kind=kind)
+    th0 = one.th0
+    one.close()
+    assert r.state == 2 and r.first.kinetic > 0 and r.first.potential != 0
+    for f in ("kinetic", "potential"):
+        a, b = getattr(r.first, f), getattr(th0, f)
+        assert abs(a - b) <= 1e-10 * max(abs(a), abs(b)), (f, a, b)
+
+
 def test_admission_budget(L, eam):
     """A budget that holds about two jobs: every job still finishes, the
     admission accounting never exceeds the budget, results equal an
