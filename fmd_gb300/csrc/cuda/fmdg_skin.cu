@@ -133,16 +133,15 @@ __device__ __forceinline__ bool within_cut_df_mi(const Geo &g, int t, int js, df
     return geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
 }
 
-// Every (j, code) of the stencil of radius R around i's current cell, j
-// the current index, in a fixed order; on a periodic axis shorter than the
+// Every cell c of the stencil of radius R around cell ci, with its stencil
+// code, in a fixed order: f(code, c).  On a periodic axis shorter than the
 // stencil a cell recurs with another image (at most one image of a pair
-// lies within the list radius).  xi: i's binary32 position relative to its
-// current cell; a cell whose box lies farther than the list radius from xi
+// lies within the list radius).  xi: the atom's binary32 position relative
+// to cell ci; a cell whose box lies farther than the list radius from xi
 // (plus 1e-4 relative) holds no candidate and is skipped.
 template <typename F>
-__device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, int i, float4 xi, F &&f)
+__device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, float4 xi, F &&f)
 {
-    const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
     const int R = g.srad, W = 2 * R + 1;
     const float lim2 = g.rskin2 * 1.0001f;
     for (int ox = -R; ox <= R; ox++)
@@ -175,15 +174,30 @@ __device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, 
                     if (!g.pbc[2]) continue;
                     cz = (cz + 2 * g.nc[2]) % g.nc[2];
                 }
-                const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
-                const bool home = (ox == 0 && oy == 0 && oz == 0);
-                const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
-                const int je = S.cell_start[c + 1];
-                for (int j = S.cell_start[c]; j < je; j++)
-                    if (!(home && j == i)) f(j, code);
+                f(((ox + R) * W + (oy + R)) * W + (oz + R), cz + g.nc[2] * (cy + g.nc[1] * cx));
             }
         }
     }
+}
+
+// the stencil code of the atom's own cell
+__device__ __forceinline__ int home_code(const Geo &g)
+{
+    const int R = g.srad, W = 2 * R + 1;
+    return (R * W + R) * W + R;
+}
+
+// every (j, code) of the stencil around i's current cell, j the current
+// index, i itself left out
+template <typename F>
+__device__ __forceinline__ void for_each_candidate(const Geo &g, const Side &S, int i, float4 xi, F &&f)
+{
+    const int home = home_code(g);
+    for_each_stencil_cell(g, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c) {
+        const int je = S.cell_start[c + 1];
+        for (int j = S.cell_start[c]; j < je; j++)
+            if (!(code == home && j == i)) f(j, code);
+    });
 }
 
 struct NoRound
@@ -383,53 +397,17 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     if (!lazy && !dyn->rebuild) slot_rel_build(g, dyn, t, x, kb);
 }
 
-// The pruned stencil walk of a list build: f(code, c, ax, ay, az) for every
-// cell c of the stencil within the list radius of xi (by the axis gaps of
-// xi to the cell's faces), in stencil order, with the cell's image offset
-// folded into the atom's position once per cell (ax, ay, az).
+// The stencil walk of a list build: f(code, c, ax, ay, az) for every cell
+// of for_each_stencil_cell, with the cell's image offset folded into the
+// atom's position once per cell (ax, ay, az).
 template <typename F>
 __device__ __forceinline__ void for_each_build_cell(const Geo &g, const SkinOffT<false> &so, CellXYZ ci, float4 xi,
                                                     F &&f)
 {
-    const int R = g.srad, W = 2 * R + 1;
-    const float lim2 = g.rskin2 * 1.0001f;
-    for (int ox = -R; ox <= R; ox++)
-    {
-        const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
-        if (gx * gx > lim2) continue;
-        int cx = ci.x + ox;
-        if (cx < 0 || cx >= g.nc[0])
-        {
-            if (!g.pbc[0]) continue;
-            cx = (cx + 2 * g.nc[0]) % g.nc[0];
-        }
-        for (int oy = -R; oy <= R; oy++)
-        {
-            const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
-            if (gx * gx + gy * gy > lim2) continue;
-            int cy = ci.y + oy;
-            if (cy < 0 || cy >= g.nc[1])
-            {
-                if (!g.pbc[1]) continue;
-                cy = (cy + 2 * g.nc[1]) % g.nc[1];
-            }
-            for (int oz = -R; oz <= R; oz++)
-            {
-                const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
-                if (gx * gx + gy * gy + gz * gz > lim2) continue;
-                int cz = ci.z + oz;
-                if (cz < 0 || cz >= g.nc[2])
-                {
-                    if (!g.pbc[2]) continue;
-                    cz = (cz + 2 * g.nc[2]) % g.nc[2];
-                }
-                const int code = ((ox + R) * W + (oy + R)) * W + (oz + R);
-                const int c = cz + g.nc[2] * (cy + g.nc[1] * cx);
-                const float4 o = so.off[code];
-                f(code, c, xi.x - o.x, xi.y - o.y, xi.z - o.z);
-            }
-        }
-    }
+    for_each_stencil_cell(g, ci, xi, [&](int code, int c) {
+        const float4 o = so.off[code];
+        f(code, c, xi.x - o.x, xi.y - o.y, xi.z - o.z);
+    });
 }
 
 // per-slot state recorded with a new list: build cell and build-frame
@@ -504,8 +482,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
                 cnt += hit;
                 if (hit && (cnt & 3) == 0 && cnt <= maxnb) row[(size_t)((cnt >> 2) - 1) * cap] = buf;
             };
-            const int R = g.srad, W = 2 * R + 1;
-            const int center = (R * W + R) * W + R;
+            const int center = home_code(g);
             for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
                 const int jb = S.cell_start[c], je = S.cell_start[c + 1];
                 if (code == center)
@@ -560,8 +537,7 @@ __global__ void __launch_bounds__(128) k_nlist_skin_grp(__grid_constant__ const 
             const float4 xi = g.xf4[i];
             const float rb2 = g.rskin2 * 1.00001f;   // as in k_nlist_skin
             int *ent = g.nbr;   // entry k of slot t: int4 row (k / 4) * cap + t, component k % 4
-            const int R = g.srad, W = 2 * R + 1;
-            const int center = (R * W + R) * W + R;
+            const int center = home_code(g);
             // the group's control flow depends on its slot only: every
             // ballot has all of the group's lanes
             for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
