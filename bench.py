@@ -123,6 +123,26 @@ class ClockSampler:
         return out
 
 
+def hbm_peak_gbs():
+    """The measured HBM copy bandwidth (MEASURED_PEAKS.json beside this
+    file), else the fallback figure; returns (GB/s, source)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback (6.8 TB/s)"
+
+
+def hbm_side(traffic_bytes, kernel_ms):
+    """The same kernel against the HBM roof: its DRAM bytes per launch
+    (ncu) over its event-timed duration, as a fraction of the copy peak."""
+    if not traffic_bytes or not kernel_ms:
+        return {}
+    peak, src = hbm_peak_gbs()
+    gbs = traffic_bytes / (kernel_ms * 1e-3) / 1e9
+    return {"dram_gbs": gbs, "frac_of_hbm": gbs / peak, "hbm_peak_gbs": peak, "hbm_peak_source": src}
+
+
 def summarize_clocks(samples):
     if not samples:
         return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -327,7 +347,9 @@ def run_ours(args):
                      "frac_of_fp64_fma_peak": achieved / peak64.value,
                      "peak_source": "measured FMA-chain microkernel (no CUDA-core peak in MEASURED_PEAKS.json)",
                      "traffic": (FORCE_DRAM_BYTES_PER_ATOM["eam_single"] * natoms if args.precision == "mixed"
-                                 else None)},
+                                 else None),
+                     **hbm_side(FORCE_DRAM_BYTES_PER_ATOM["eam_single"] * natoms if args.precision == "mixed"
+                                else None, phases["force"])},
         "clocks": clocks,
         "device_errors": errs.value,
         "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 2 * 3 * natoms * 8,
@@ -548,7 +570,9 @@ def run_served(args):
                      "traffic": (FORCE_DRAM_BYTES_PER_ATOM["morse_pack"] * phases[dom]["atoms"] if dom == "morse"
                                  else None),
                      "traffic_note": "DRAM bytes of the force phase of this category per step (all its packs), "
-                                     "scaled by atoms from an ncu capture of a 149616-atom Morse pack"},
+                                     "scaled by atoms from an ncu capture of a 149616-atom Morse pack",
+                     **hbm_side(FORCE_DRAM_BYTES_PER_ATOM["morse_pack"] * phases[dom]["atoms"] if dom == "morse"
+                                else None, phases[dom]["force_ms"])},
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "atom-steps/s",
                 "h2d_bytes_per_step": h2d / total_steps, "d2h_bytes_per_step": d2h / total_steps,
