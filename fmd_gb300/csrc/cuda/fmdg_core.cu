@@ -463,8 +463,8 @@ int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
 // Neighbour-list entries per atom (before fmdg_upload); 0: the estimate.
 extern "C" int fmdg_set_build_lanes(fmdg_sys_t *s, int lanes)
 {
-    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16)
-        return fmdg_set_error("fmdg_set_build_lanes: 0, 1, 2, 4, 8 or 16");
+    if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+        return fmdg_set_error("fmdg_set_build_lanes: 0, 1, 2, 4, 8, 16 or 32");
     s->build_lanes = lanes;
     return FMDG_OK;
 }

@@ -1137,16 +1137,14 @@ int fmdg_skin_launch_nlist(fmdg_sys_t *s)
 {
     const LocOne L{s->g};
     k_prep_skin<<<fmdg_grid(s->g.cap, 128), 128, 0, s->stream>>>(L, 0);
-    // up to 2^17 slots the build runs G lanes per slot (G <= 16, the
-    // largest with cap * G <= 2^18 threads); larger systems fill the device
-    // with one thread per slot
+    // lanes per slot by size, from build times measured on GB300 (LJ,
+    // Morse, EAM jobs of 2k-190k atoms): 16 up to 2^14 slots, 8 up to 2^16,
+    // then one thread per slot (enough warps; a group's ballots cost more
+    // than they hide).  Groups of 2 or 4 lanes never won: the lanes of
+    // different groups in a warp diverge and serialise.
     const int cap = s->g.cap;
     int G = s->build_lanes;
-    if (G == 0)
-    {
-        G = 1;
-        while (G < 16 && (long long)cap * G * 2 <= (1 << 18)) G *= 2;
-    }
+    if (G == 0) G = cap <= (1 << 14) ? 16 : (cap <= (1 << 16) ? 8 : 1);
     const int nbg = fmdg_grid(cap > 0 ? cap * G : 1, 128);
     switch (G)
     {
@@ -1154,6 +1152,7 @@ int fmdg_skin_launch_nlist(fmdg_sys_t *s)
     case 4: k_nlist_skin_grp<4><<<nbg, 128, 0, s->stream>>>(L); break;
     case 8: k_nlist_skin_grp<8><<<nbg, 128, 0, s->stream>>>(L); break;
     case 16: k_nlist_skin_grp<16><<<nbg, 128, 0, s->stream>>>(L); break;
+    case 32: k_nlist_skin_grp<32><<<nbg, 128, 0, s->stream>>>(L); break;
     default: k_nlist_skin<<<fmdg_force_blocks(s), s->fblk, 0, s->stream>>>(L); break;
     }
     s->launches += 2;

@@ -113,7 +113,8 @@ int fmdg_set_skin(fmdg_sys_t *s, double skin);
    only. */
 int fmdg_set_list_capacity(fmdg_sys_t *s, int entries);
 /* Threads per atom of this system's skin-list builds: 0 (default) picks
-   them by size (2-16 up to 2^17 atoms, else 1); 1, 2, 4, 8 or 16 fix them.
+   them by size (16 up to 2^14 atoms, 8 up to 2^16, else 1); 1, 2, 4, 8,
+   16 or 32 fix them.
    Every choice builds the same list, entry for entry. */
 int fmdg_set_build_lanes(fmdg_sys_t *s, int lanes);
 

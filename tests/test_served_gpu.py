@@ -375,13 +375,13 @@ def test_list_overflow_fallback(L, eam, pot, precision):
 
 @pytest.mark.parametrize("pot,cap", [("lj", 0), ("morse", 0), ("eam", 0), ("cuar", 0), ("cuar", 32)])
 def test_single_build_lanes_same_list(L, eam, pot, cap):
-    """Skin-list builds with 1, 2, 4, 8 and 16 threads per atom build the
+    """Skin-list builds with 1, 2, 4, 8, 16 and 32 threads per atom build the
     same list, entry for entry (also when it overflows): the same trajectory
     bit for bit, the binary32 partial sums flushing at the same entries.
     60 steps at 900 K include list rebuilds after the first build."""
     x, v, l, kind = _sys(pot, 6, 900.0, 95)
     res = []
-    for lanes in (1, 2, 4, 8, 16):
+    for lanes in (1, 2, 4, 8, 16, 32):
         one = serve.Single(L, pot, x, v, l, precision=serve.PREC_MIXED, eam=eam, kind=kind, list_capacity=cap,
                            build_lanes=lanes)
         one.steps(60)
