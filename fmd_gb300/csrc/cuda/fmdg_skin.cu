@@ -513,6 +513,57 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_nlist_skin(__
 // lanes of a slot test G consecutive candidates of a cell together and
 // place their hits in candidate order (ballot + prefix count), so the list
 // is the one-thread build's, entry for entry.
+// The list of slot t built by the G lanes of a group (gl: this lane's
+// index in it, gbase: the group's first lane in the warp): the lanes test
+// G consecutive candidates of a cell together and place their hits in
+// candidate order (ballot + prefix count), so the list is the one-thread
+// build's, entry for entry.  Every lane of the group must call it (its
+// control flow depends on the slot only).
+__device__ __forceinline__ void build_slot_grouped(const Geo &g, const Side &S, const SkinOffT<false> &so, int t,
+                                                   int G, int gl, int gbase)
+{
+    const int cap = g.cap, maxnb = g.maxnb;
+    const unsigned gmask = (G == 32) ? 0xffffffffu : ((1u << G) - 1u) << gbase;
+    int cnt = 0;
+    const int i = g.pos[t];
+    if (i >= 0)
+    {
+        const float4 xi = g.xf4[i];
+        const float rb2 = g.rskin2 * 1.00001f;   // as in k_nlist_skin
+        int *ent = g.nbr;   // entry k of slot t: int4 row (k / 4) * cap + t, component k % 4
+        const int center = home_code(g);
+        for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
+            const int jb = S.cell_start[c], je = S.cell_start[c + 1];
+            const bool self = code == center;
+            for (int base = jb; base < je; base += G)
+            {
+                const int j = base + gl;
+                bool hit = false;
+                if (j < je && !(self && j == i))
+                {
+                    const float4 xj = __ldg(g.xf4 + j);
+                    const float dx = ax - xj.x, dy = ay - xj.y, dz = az - xj.z;
+                    hit = dx * dx + dy * dy + dz * dz < rb2;
+                }
+                const unsigned m = __ballot_sync(gmask, hit) >> gbase;
+                if (hit)
+                {
+                    const int k = cnt + __popc(m & ((1u << gl) - 1u));
+                    if (k < maxnb)
+                        ent[((size_t)(k >> 2) * cap + t) * 4 + (k & 3)] =
+                            (int)((unsigned)S.slot[j] | ((unsigned)code << SLOT_BITS));
+                }
+                cnt += __popc(m);
+            }
+        });
+        if (gl == 0) record_build(g, S, t, i, xi);
+    }
+    if (gl == 0) g.nbr_count[t] = cnt;
+}
+
+// Single-system build (a served job's admission, the fmd.h path) with G
+// lanes per slot: a system of 10^3-10^5 atoms gives one thread per slot too
+// few warps to hide the gather latency of its long candidate walk.
 template <int G>
 __global__ void __launch_bounds__(128) k_nlist_skin_grp(__grid_constant__ const LocOne loc)
 {
@@ -522,52 +573,8 @@ __global__ void __launch_bounds__(128) k_nlist_skin_grp(__grid_constant__ const 
     if (!dyn->rebuild) return;
     __shared__ SkinOffT<false> so;
     load_offsets(g, so);
-    const int cap = g.cap, maxnb = g.maxnb;
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) / G;   // uniform over a group
-    const int gl = threadIdx.x & (G - 1);
-    const int gbase = threadIdx.x & 31 & ~(G - 1);
-    const unsigned gmask = (G == 32) ? 0xffffffffu : ((1u << G) - 1u) << gbase;
-    if (t < cap)
-    {
-        int cnt = 0;
-        const int i = g.pos[t];
-        if (i >= 0)
-        {
-            const Side S = g.side[dyn->cur];
-            const float4 xi = g.xf4[i];
-            const float rb2 = g.rskin2 * 1.00001f;   // as in k_nlist_skin
-            int *ent = g.nbr;   // entry k of slot t: int4 row (k / 4) * cap + t, component k % 4
-            const int center = home_code(g);
-            // the group's control flow depends on its slot only: every
-            // ballot has all of the group's lanes
-            for_each_build_cell(g, so, cell_xyz(g, S.cell_of[i]), xi, [&](int code, int c, float ax, float ay, float az) {
-                const int jb = S.cell_start[c], je = S.cell_start[c + 1];
-                const bool self = code == center;
-                for (int base = jb; base < je; base += G)
-                {
-                    const int j = base + gl;
-                    bool hit = false;
-                    if (j < je && !(self && j == i))
-                    {
-                        const float4 xj = __ldg(g.xf4 + j);
-                        const float dx = ax - xj.x, dy = ay - xj.y, dz = az - xj.z;
-                        hit = dx * dx + dy * dy + dz * dz < rb2;
-                    }
-                    const unsigned m = __ballot_sync(gmask, hit) >> gbase;
-                    if (hit)
-                    {
-                        const int k = cnt + __popc(m & ((1u << gl) - 1u));
-                        if (k < maxnb)
-                            ent[((size_t)(k >> 2) * cap + t) * 4 + (k & 3)] =
-                                (int)((unsigned)S.slot[j] | ((unsigned)code << SLOT_BITS));
-                    }
-                    cnt += __popc(m);
-                }
-            });
-            if (gl == 0) record_build(g, S, t, i, xi);
-        }
-        if (gl == 0) g.nbr_count[t] = cnt;
-    }
+    if (t < g.cap) build_slot_grouped(g, g.side[dyn->cur], so, t, G, threadIdx.x & (G - 1), threadIdx.x & 31 & ~(G - 1));
     finish_build(dyn, gridDim.x);
 }
 
