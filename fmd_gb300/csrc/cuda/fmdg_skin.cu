@@ -722,6 +722,11 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 const float4 tf = g.pkf_F[(size_t)ei * nrint + irho];
                 const float f32 = spl_der(tf, b, (float)g.inv_drho);
                 g.fpb[t] = f32;
+                // lean (one kind: the kind bits are unused): F'(rho) also
+                // rides in the w of the slot's list position, so the force
+                // walk reads it with the neighbour's position (one gather
+                // per pair instead of two); the next step start rewrites w
+                if (LEAN) reinterpret_cast<float *>(g.xl + t)[3] = f32;
                 fp = (double)f32;
                 acc[0] = (double)spl_val(tf, b);
             }
@@ -734,6 +739,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             g.vaream[i] = 0.0;
             g.fpd[t] = 0.0;
             g.fpb[t] = 0.f;
+            if (LEAN) reinterpret_cast<float *>(g.xl + t)[3] = 0.f;
             if (!MIXED) g.fpdf[t] = make_float2(0.f, 0.f);
         }
     }
@@ -767,7 +773,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     if (i >= 0)
     {
         float4 xi = g.xl[t];
-        const int ki = __float_as_int(xi.w);
+        const int ki = LEAN ? 0 : __float_as_int(xi.w);   // (lean EAM: w holds F'(rho))
         const bool active = (group < 0 || g.gslot[t] == group);
         const int nk = g.nkinds;
         double f[3] = {0.0, 0.0, 0.0};
@@ -855,7 +861,10 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             const float4 tph = tpr[2 * ir2], trh = tpr[2 * ir2 + 1];
                             const float phi_d = spl_der(tph, b, inv_h);
                             const float rho_d = spl_der(trh, b, inv_h);
-                            const float fa = -2.f * (fpi * rho_d + g.fpb[js] * rho_d + phi_d);
+                            // F'(rho_j): w of the list position; an overflow
+                            // fallback occurrence (code < 0) carries kind bits
+                            const float fpj = __float_as_int(o.w) >= 0 ? xj.w : g.fpb[js];
+                            const float fa = -2.f * (fpi * rho_d + fpj * rho_d + phi_d);
                             ac.part[0] += fa * rv.x;
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
