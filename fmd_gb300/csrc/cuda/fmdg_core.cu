@@ -426,6 +426,9 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
         if ((rc = dalloc(s, (float4 **)&g.pkf_pr, pr.size()))) return rc;
         FMDG_CK(cudaMemcpy((void *)g.pkf_pr, pr.data(), pr.size() * sizeof(float4), cudaMemcpyHostToDevice));
     }
+    // the 32-byte row tables are read with 256-bit loads (ld_row32)
+    if (((uintptr_t)g.pkf_pr | (uintptr_t)g.pkd_rho | (uintptr_t)g.pkd_phi) % 32)
+        return fmdg_set_error("fmdg_set_eam: row tables not 32-byte aligned");
     invalidate_graph(s);
     return FMDG_OK;
 }

@@ -32,6 +32,16 @@ struct SmemPotT
     float4 offl[DF ? 27 : 1];   // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
 };
 
+// one 32-byte table row (two float4) in a single 256-bit load; p must be
+// 32-byte aligned (the row tables are whole allocations, checked when they
+// are built)
+__device__ __forceinline__ void ld_row32(const float4 *p, float4 &a, float4 &b)
+{
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 // small integer v (|v| < 2^22) as binary32 without a conversion
 // instruction (conversions issue at the binary64 rate on GB300)
 __device__ __forceinline__ float small_int_f(int v) { return __int_as_float(0x4B400000 + v) - 12582912.f; }
@@ -230,19 +240,21 @@ __device__ __forceinline__ void df_pair(const Geo &g, const SmemPotT<DF, ONE> &s
         dfl b;
         const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
         const int ei = pp.iloc, ej = pp.jloc;
-        const float4 *ph = g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2);
-        const float4 *ri = g.pkd_rho + 2 * ((size_t)ei * nint + ir2);
-        const dfl phi_d = df_spl_der(ph[0], ph[1], b, inv_h);
-        const dfl rho_ip = df_spl_der(ri[0], ri[1], b, inv_h);
+        float4 ph0, ph1, ri0, ri1;
+        ld_row32(g.pkd_phi + 2 * (((size_t)ei * ne + ej) * nint + ir2), ph0, ph1);
+        ld_row32(g.pkd_rho + 2 * ((size_t)ei * nint + ir2), ri0, ri1);
+        const dfl phi_d = df_spl_der(ph0, ph1, b, inv_h);
+        const dfl rho_ip = df_spl_der(ri0, ri1, b, inv_h);
         dfl rho_jp = rho_ip;
         if (ei != ej)
         {
-            const float4 *rj = g.pkd_rho + 2 * ((size_t)ej * nint + ir2);
-            rho_jp = df_spl_der(rj[0], rj[1], b, inv_h);
+            float4 rj0, rj1;
+            ld_row32(g.pkd_rho + 2 * ((size_t)ej * nint + ir2), rj0, rj1);
+            rho_jp = df_spl_der(rj0, rj1, b, inv_h);
         }
         const dfl fj = fpj();
         fa = df_neg(df_scale2(df_add(df_add(df_mul(fpi, rho_jp), df_mul(fj, rho_ip)), phi_d), 2.f));
-        eh = df_scale2(df_spl_val(ph[0], ph[1], b), 0.5f);
+        eh = df_scale2(df_spl_val(ph0, ph1, b), 0.5f);
     }
 }
 
@@ -252,8 +264,9 @@ __device__ __forceinline__ dfl df_rho(const Geo &g, const fmdg_pair_t &pp, const
 {
     dfl b;
     const int ir2 = df_table_index(df_mul(p.r2, inv_h), kmax, b);
-    const float4 *row = g.pkd_rho + 2 * ((size_t)pp.jloc * nint + ir2);
-    return df_spl_val(row[0], row[1], b);
+    float4 r0, r1;
+    ld_row32(g.pkd_rho + 2 * ((size_t)pp.jloc * nint + ir2), r0, r1);
+    return df_spl_val(r0, r1, b);
 }
 
 // Sum over the 32 lanes of a warp of v[0..NV), NV <= 8, by a transposing

@@ -858,7 +858,8 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             if (!in) return;
                             float b;
                             const int ir2 = table_index(r2 * inv_h, kmax, b);
-                            const float4 tph = tpr[2 * ir2], trh = tpr[2 * ir2 + 1];
+                            float4 tph, trh;
+                            ld_row32(tpr + 2 * ir2, tph, trh);
                             const float phi_d = spl_der(tph, b, inv_h);
                             const float rho_d = spl_der(trh, b, inv_h);
                             // F'(rho_j): w of the list position; an overflow
