@@ -501,7 +501,8 @@ int fmdg_capacity_estimate(const int *cell_count, int ncell, double cell_volume,
 size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
 {
     const size_t cap = n > 0 ? n : 1;
-    const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8 + 24;
+    const size_t per_atom = 2 * (48 + 16) + 32 + 7 * 4 + 16 + 4 + 4 * (size_t)maxnb + 9 * 8 / 64 + 8 + 24 +
+                            32;   // binary64 position rows (xdf)
     const size_t per_cell = 2 * 4 + 5 * 4 + 32;
     return cap * per_atom + (size_t)ncell * per_cell + 64 * 1024;
 }
@@ -629,7 +630,7 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         c.take(g.bnewidx, cap); c.take(g.dep_count, 4 * (size_t)ncell); c.take(g.arr_base, (size_t)ncell + 1);
         c.take(g.bucket, cap); c.take(g.arr_slot, cap);
         c.take(g.fpf, cap); c.take(g.xf4, cap); c.take(g.nbr, (size_t)cap * maxnb); c.take(g.nbr_count, cap);
-        c.take(g.xlo4, cap); c.take(g.fpdf, cap);
+        c.take(g.xdf, 2 * (size_t)cap); c.take(g.fpdf, cap);
         c.take(g.partials, (size_t)nb * 9 + 8);
         c.take(g.corig, ncell);
         if (g.skin_on)

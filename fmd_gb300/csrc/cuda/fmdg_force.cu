@@ -155,11 +155,16 @@ __global__ void k_prep_local(__grid_constant__ const L loc)
     const double uy = S.x[cap + i] - oc.y;
     const double uz = S.x[2 * (size_t)cap + i] - oc.z;
     const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
-    g.xf4[i] = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
-    // binary64 mode: the remainders, so that xf4 + xlo4 is the double-float
-    // cell-local position
+    const float4 hi = make_float4(lx, ly, lz, __int_as_float((int)S.kind[i]));
+    g.xf4[i] = hi;
+    // binary64 mode: hi and the remainders side by side, the double-float
+    // cell-local position in one 32-byte row
     if (g.prec == FMDG_PREC_FP64)
-        g.xlo4[i] = make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
+    {
+        g.xdf[2 * (size_t)i] = hi;
+        g.xdf[2 * (size_t)i + 1] =
+            make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
+    }
 }
 
 template <class L>
@@ -251,17 +256,19 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density(__gri
             if (!MIXED)
             {
                 // double-float pair arithmetic (fmdg_df.cuh)
-                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                float4 ih, il;
+                ld_row32(g.xdf + 2 * (size_t)i, ih, il);
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
                 const float kmax = (float)(nint - 1);
                 dfl acc_rho = {0.f, 0.f};
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
-                    const float4 jh = g.xf4[j];
+                    float4 jh, jl;
+                    ld_row32(g.xdf + 2 * (size_t)j, jh, jl);
                     const int pidx = ki * nk + __float_as_int(jh.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     if (HYBRID && pp.cat != FMDG_POT_EAM) return;
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
+                    const GeomDF p = geom_df(ih, il, jh, jl, sp.off[code], sp.offl[code]);
                     if (within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][2], pp.p[2]))
                         acc_rho = df_add(acc_rho, df_rho(g, pp, p, inv_h, kmax, nint));
                 });
@@ -373,19 +380,21 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 // in the reference's formulas -- LJ src/lj.h:35-56, Morse
                 // src/morse.h:35-56, EAM src/eam.h:186-226 -- the category
                 // chosen per pair for hybrid tables (src/forces.c:33-290)
-                const float4 ih = g.xf4[i], il = g.xlo4[i];
+                float4 ih, il;
+                ld_row32(g.xdf + 2 * (size_t)i, ih, il);
                 const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[i]) : dfl{0.f, 0.f};
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
                 const float kmax = (float)(nint - 1);
                 dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
-                    const float4 jh = g.xf4[j];
+                    float4 jh, jl;
+                    ld_row32(g.xdf + 2 * (size_t)j, jh, jl);
                     const int pidx = ki * nk + __float_as_int(jh.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
                     const int rci = (cat == FMDG_POT_MORSE) ? 3 : 2;
-                    const GeomDF p = geom_df(ih, il, jh, g.xlo4[j], sp.off[code], sp.offl[code]);
+                    const GeomDF p = geom_df(ih, il, jh, jl, sp.off[code], sp.offl[code]);
                     if (!within_cut_df(g, S, i, ci, j, code, p.r2, sp.pf[pidx][rci], pp.p[rci])) return;
                     dfl fa, eh;     // f_i += fa * rv, energy share eh
                     df_pair(g, sp, pidx, pp, cat, p, fpi, inv_h, kmax, nint, ne, [&]() { return df_of(g.fpdf[j]); },

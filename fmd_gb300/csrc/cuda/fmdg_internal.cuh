@@ -86,9 +86,9 @@ struct Geo   // passed by value to kernels
     const float4 *pkf_pr;       // per element e and interval k: {phi_ee, rho_e} side by side (one 32 B row)
     // binary64 mode, EAM: double-float forms (fmdg_df.cuh) of the tables
     // (per interval {hi coefficients, lo coefficients}), of the cell-local
-    // coordinates (lo parts beside xf4) and of F'(rho)
+    // coordinates and of F'(rho)
     const float4 *pkd_rho, *pkd_phi;
-    float4 *xlo4;
+    float4 *xdf;       // per index {xf4, lo parts}: one 32-byte row (one 256-bit load per neighbour)
     float2 *fpdf;
     float4 *xll;       // skin lists, binary64 mode: lo parts of xl (double-float build-frame positions)
     double inv_dr2, inv_drho;

@@ -150,7 +150,7 @@ __device__ __forceinline__ float spl_der(float4 t, float b, float inv_h)
 struct Geom64 { double rv[3]; double r2; };
 
 // double-float pair geometry (binary64 mode) from cell-local
-// coordinates hi (xf4) + lo (xlo4): rv = x_i - x_j - offset * cellh, the
+// coordinates hi + lo (a row of xdf): rv = x_i - x_j - offset * cellh, the
 // image shift of a periodic neighbour being offset * cellh in the cell
 // frame; r^2 from exact squares of the hi parts.  Agrees with the
 // reference's binary64 geometry to about 1e-14 relative.

@@ -391,7 +391,11 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
     g.xf4[i] = make_float4(lx, ly, lz, kb);
     if (g.prec == FMDG_PREC_FP64)
-        g.xlo4[i] = make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
+    {
+        g.xdf[2 * (size_t)i] = make_float4(lx, ly, lz, kb);
+        g.xdf[2 * (size_t)i + 1] =
+            make_float4((float)(ux - (double)lx), (float)(uy - (double)ly), (float)(uz - (double)lz), 0.f);
+    }
     // (renumbered, or a rebuild already due: the build cell and position of
     // slot t are rewritten by the list build that follows)
     if (!lazy && !dyn->rebuild) slot_rel_build(g, dyn, t, x, kb);
@@ -417,7 +421,7 @@ __device__ __forceinline__ void record_build(const Geo &g, const Side &S, int t,
     g.cb[t] = S.cell_of[i];
     g.xl[t] = xi;
     g.xb[t] = xi;
-    if (g.prec == FMDG_PREC_FP64) g.xll[t] = g.xlo4[i];
+    if (g.prec == FMDG_PREC_FP64) g.xll[t] = g.xdf[2 * (size_t)i + 1];
 }
 
 // the last block of a build to finish clears the system's rebuild flag
