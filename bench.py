@@ -64,7 +64,7 @@ SERVED_FORCE_FLOP = {"lj": 35.5 * 31.0, "morse": 91.0 * 31.0, "eam": 29.5 * 68.0
 # divided by the atoms of the launch): packed Morse on a 149616-atom pack,
 # single-system mixed EAM on the 256000-atom system (both skin lists); the traffic
 # grows with the atoms (the neighbour list dominates it)
-FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 144.87e6 / 149616, "eam_single": 100.40e6 / 256000}
+FORCE_DRAM_BYTES_PER_ATOM = {"morse_pack": 144.87e6 / 149616, "eam_single": 101.07e6 / 256000}
 
 
 class ClockSampler:
