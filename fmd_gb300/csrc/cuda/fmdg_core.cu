@@ -138,6 +138,15 @@ __global__ void k_flush(unsigned *buf, size_t n)
         buf[i] = buf[i] * 1664525u + 1013904223u;
 }
 
+// d2f_rn (integer rounding) beside the conversion instruction
+__global__ void k_d2f_check(const double *x, int n, float *ours, float *ref)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ours[i] = d2f_rn(x[i]);
+    ref[i] = __double2float_rn(x[i]);
+}
+
 // Independent FMA chains: the issue-rate ceiling of the CUDA cores for T.
 template <typename T>
 __global__ void k_fma_peak(T *out, int iters, T a, T b)
@@ -153,6 +162,25 @@ __global__ void k_fma_peak(T *out, int iters, T a, T b)
 }
 
 } // namespace
+
+extern "C" int fmdg_check_d2f(fmdg_sys_t *s, const double *x, int n, float *ours, float *ref)
+{
+    if (n < 0) return fmdg_set_error("fmdg_check_d2f: negative count");
+    if (n == 0) return FMDG_OK;
+    double *dx = nullptr;
+    float *d1 = nullptr, *d2 = nullptr;
+    FMDG_CK(cudaMalloc(&dx, (size_t)n * 8));
+    FMDG_CK(cudaMalloc(&d1, (size_t)n * 4));
+    FMDG_CK(cudaMalloc(&d2, (size_t)n * 4));
+    FMDG_CK(cudaMemcpyAsync(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
+    k_d2f_check<<<fmdg_grid(n, 256), 256, 0, s->stream>>>(dx, n, d1, d2);
+    FMDG_CK(cudaGetLastError());
+    FMDG_CK(cudaMemcpyAsync(ours, d1, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaMemcpyAsync(ref, d2, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    cudaFree(dx); cudaFree(d1); cudaFree(d2);
+    return FMDG_OK;
+}
 
 extern "C" int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops)
 {

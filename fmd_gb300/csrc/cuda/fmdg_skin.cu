@@ -293,13 +293,13 @@ __device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, co
     for (int d = 0; d < 3; d++)
     {
         double u = x[d] - o3[d];
-        float uf = (float)u;
+        float uf = d2f_rn(u);
         // unwrap across a periodic face (binary64 test near half a box)
         if (g.pbc[d] && fabsf(uf) > 0.49f * g.l_f[d])
         {
             if (u > 0.5 * g.l[d]) u -= g.l[d];
             else if (u < -0.5 * g.l[d]) u += g.l[d];
-            uf = (float)u;
+            uf = d2f_rn(u);
         }
         l3[d] = uf;
         u3[d] = u;

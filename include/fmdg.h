@@ -246,6 +246,10 @@ int fmdg_launch_count(fmdg_sys_t *s, long long *count);
 /* issue-rate ceiling of the CUDA cores: independent FMA chains over all
    SMs, 2 flops per FMA (fp64=1: binary64, else binary32) */
 int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops);
+/* self-check of the integer binary64 -> binary32 rounding of the step
+   kernels (d2f_rn): for n inputs, its results and the conversion
+   instruction's */
+int fmdg_check_d2f(fmdg_sys_t *s, const double *x, int n, float *ours, float *ref);
 /* write a buffer larger than L2 so the next kernel starts cold */
 int fmdg_flush_l2(fmdg_sys_t *s);
 
