@@ -164,22 +164,6 @@ __device__ __forceinline__ dfl df_exp(dfl x)
     return {__fmul_rn(p.hi, s), __fmul_rn(p.lo, s)};
 }
 
-// binary64 -> binary32 rounded to nearest even with integer operations
-// (the conversion instruction issues at the binary64 rate on GB300): the
-// 52-bit significand cut to 23 bits, the 29 dropped bits rounding the
-// result (a carry into the exponent is the IEEE result); zero, subnormal
-// and out-of-range inputs take the conversion instruction
-__device__ __forceinline__ float d2f_rn(double x)
-{
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const int e = (int)((hi >> 20) & 0x7ffu);
-    if ((unsigned)(e - 897) > 253u) return __double2float_rn(x);
-    unsigned f = ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned rem = lo & 0x1fffffffu;
-    f += (rem > 0x10000000u) || (rem == 0x10000000u && (f & 1u));
-    return __uint_as_float(f | (hi & 0x80000000u));
-}
-
 // nearest double-float of a binary64 number (hi = x rounded to binary32,
 // lo = the rounded remainder)
 __host__ __device__ __forceinline__ float2 df_split(double x)

@@ -330,11 +330,29 @@ __device__ __forceinline__ double floor_div(double x, double h, double inv_h)
     return f;
 }
 
+// binary64 -> binary32 rounded to nearest even with integer operations
+// (the conversion instruction issues at the binary64 rate on GB300): the
+// 52-bit significand cut to 23 bits, the 29 dropped bits rounding the
+// result (a carry into the exponent is the IEEE result); zero, subnormal
+// and out-of-range inputs take the conversion instruction
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    if ((unsigned)(e - 897) > 253u) return __double2float_rn(x);
+    unsigned f = ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    f += (rem > 0x10000000u) || (rem == 0x10000000u && (f & 1u));
+    return __uint_as_float(f | (hi & 0x80000000u));
+}
+
 // floor_div as an int, through a binary32 estimate when its fraction is
 // clear of an integer by more than its error (then both agree; one binary64
 // instruction instead of a dozen -- binary64 issues at 1/64 of the binary32
 // rate on GB300), else in binary64.  Results below -2 or above 2^30 come
-// back as -2 (callers test against [-1, nc]).
+// back as -2 (callers test against [-1, nc]).  (Conversion-free forms of
+// the binary32 path -- d2f_rn, a magic-number floor -- measured no faster:
+// the binning kernel is memory bound.)
 __device__ __forceinline__ int cell_floor(double x, double h, double inv_h, float inv_hf)
 {
     const float qf = __fmul_rn((float)x, inv_hf);
