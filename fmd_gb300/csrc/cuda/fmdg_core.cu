@@ -169,17 +169,20 @@ extern "C" int fmdg_check_d2f(fmdg_sys_t *s, const double *x, int n, float *ours
     if (n == 0) return FMDG_OK;
     double *dx = nullptr;
     float *d1 = nullptr, *d2 = nullptr;
-    FMDG_CK(cudaMalloc(&dx, (size_t)n * 8));
-    FMDG_CK(cudaMalloc(&d1, (size_t)n * 4));
-    FMDG_CK(cudaMalloc(&d2, (size_t)n * 4));
-    FMDG_CK(cudaMemcpyAsync(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
-    k_d2f_check<<<fmdg_grid(n, 256), 256, 0, s->stream>>>(dx, n, d1, d2);
-    FMDG_CK(cudaGetLastError());
-    FMDG_CK(cudaMemcpyAsync(ours, d1, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
-    FMDG_CK(cudaMemcpyAsync(ref, d2, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream));
-    FMDG_CK(cudaStreamSynchronize(s->stream));
+    cudaError_t e = cudaMalloc(&dx, (size_t)n * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&d1, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&d2, (size_t)n * 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+    {
+        k_d2f_check<<<fmdg_grid(n, 256), 256, 0, s->stream>>>(dx, n, d1, d2);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ours, d1, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ref, d2, (size_t)n * 4, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     cudaFree(dx); cudaFree(d1); cudaFree(d2);
-    return FMDG_OK;
+    return e == cudaSuccess ? FMDG_OK : fmdg_fail("fmdg_check_d2f", e);
 }
 
 extern "C" int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops)
