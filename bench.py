@@ -643,9 +643,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    # Under torchrun (N > 1) rank 0 alone runs and prints; the engine uses
+    # one GPU (multi-GPU serving is not built), and its line says n_gpus 1
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
     if args.impl == "reference":
-        if int(os.environ.get("RANK", "0")) != 0:
-            return
         run_reference(args)
         return
     out = run_served(args) if args.workload == "served" else run_ours(args)
