@@ -1,30 +1,32 @@
 """Benchmark: atom-steps/s of FMD's per-timestep hot path on one GB300.
 
 Workloads
-  served (default)  the served job stream: independent FCC cubes (500 to
-                    200 000 atoms, log-uniform), potential uniform over the
-                    argon LJ / copper Morse / analytic copper EAM, 50-1200 K,
-                    step counts uniform in [1000, 20000], Poisson arrivals at
-                    50 jobs/s (seed 5).  A bounded sample is timed: the first
-                    --jobs jobs with every step count and arrival time
-                    multiplied by --step-scale (the offered load relative to
-                    the device's capacity is unchanged).  Mixed precision
+  served (default)  the served job stream: 2048 independent FCC cubes (500
+                    to 200 000 atoms, log-uniform), potential uniform over
+                    the argon LJ / copper Morse / analytic copper EAM,
+                    50-1200 K, step counts uniform in [1000, 20000], Poisson
+                    arrivals at 50 jobs/s (seed 5).  Mixed precision
                     (binary32 pair arithmetic, binary64 sums), packed per
                     potential, chunks of steps replayed as CUDA graphs.
+                    --jobs / --step-scale shorten it (first jobs; step
+                    counts and arrival times scaled together) for quick runs.
   eam256k           one 256 000-atom EAM system (FCC 40x40x40, a = 3.615 A,
                     300 K, seed 2, dt 1 fs), the single-system drop-in path.
 
     python bench.py [--steps K] [--warmup W] [--workload served|eam256k]
     python bench.py --impl reference     # CPU oracle port on the host cores
 
-served: `value` = every job of the sample resident in HBM, K time steps of
-the whole fleet (all packs, one graph replay per pack per step) between
-CUDA events; the fleet's working set (GBs) is larger than L2.  `e2e` = the
-sample streamed through the request loop (fmdg_srv_* C-ABI) from host
-arrays: arrivals, admission, upload, steps, results, wall clock; p50/p99
-job latency.  `plain` = the same jobs one at a time through the plain
-single-system binary64 path (the path libfmd.so's fmd_dync_integrate
-drives), wall clock including each job's set-up.
+served: `value` = every job of the stream resident in HBM at once, K fleet
+steps (each: FLEET_CHUNK velocity-Verlet steps of every job, all packs'
+graphs replayed concurrently) between CUDA events on a join stream; the
+fleet's working set (tens of GB) is larger than L2.  `e2e` = the stream
+through the request loop (fmdg_srv_* C-ABI) from host arrays: arrivals,
+admission by HBM budget, upload, steps, results; wall clock from the first
+arrival to the last completion; p50/p99 job latency.  `plain_fp64` = jobs
+one at a time through the plain single-system binary64 path (the path
+libfmd.so's fmd_dync_integrate drives): every PLAIN_EVERY-th job timed
+(set-up + first step, then PLAIN_STEPS steps) and extrapolated to its step
+count; `served_over_plain_fp64` = e2e / plain_fp64.
 eam256k: device time with CUDA events per step, L2 flushed (256 MB write)
 before every timed step; `e2e` drives the same steps through the C-ABI
 with pinned host buffers.
@@ -146,8 +148,9 @@ def hbm_side(traffic_bytes, kernel_ms):
 def summarize_clocks(samples):
     if not samples:
         return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-    sm = sorted(float(s[0]) for s in samples if s[0].replace(".", "").isdigit())
-    mx = max(float(s[1]) for s in samples if s[1].replace(".", "").isdigit()) if sm else None
+    sm = sorted(float(s[0]) for s in samples if len(s) > 0 and s[0].replace(".", "").isdigit())
+    mxs = [float(s[1]) for s in samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+    mx = max(mxs) if mxs else None
     names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
     reasons = set()
     for s in samples:
@@ -333,7 +336,8 @@ def run_ours(args):
         "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32-compute/f64-accumulate",
+        "dtype": ("double-float pairs (two binary32, ~48 bits), binary64 integration" if args.precision == "fp64"
+                  else "f32-compute/f64-accumulate"),
         "data": "synthetic",
         "config": {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
                                "300 K, dt 1 fs, NVE", "atoms": natoms, "precision": args.precision,
@@ -364,65 +368,125 @@ def run_ours(args):
 
 
 # ---------------------------------------------------------------- served stream
-SERVED_JOBS = 256
-SERVED_STEP_SCALE = 0.02
+METRIC = "atom-steps/s on 1 GB300, batched-served vs plain at ≤1e-5 force err; p50/p99"
+SERVED_JOBS = 2048
+SERVED_STEP_SCALE = 1.0
+FLEET_CHUNK = 8      # velocity-Verlet steps of every resident job per timed fleet step
+PLAIN_EVERY = 16     # plain arm: every 16th job of the stream
+PLAIN_STEPS = 200    # plain arm: steps timed per sampled job after its first
+REF_EVERY = 16       # reference arm and cpu_baseline: every 16th job of the stream
 
 
 def served_config(args):
-    return {"workload": "served job stream (2048-job stream, seed 5: FCC cubes 500-200000 atoms log-uniform, "
-                        "LJ argon / Morse copper / analytic-EAM copper, 50-1200 K, Poisson arrivals at 50/s); "
-                        f"sample: first {args.jobs} jobs, step counts and arrival times x {args.step_scale}",
+    scale = "" if args.step_scale == 1.0 else f"; step counts and arrival times x {args.step_scale}"
+    return {"workload": f"served job stream, {args.jobs} jobs (seed 5): FCC cubes 500-200000 atoms log-uniform, "
+                        "LJ argon / Morse copper / analytic-EAM copper, 50-1200 K, 1000-20000 steps, "
+                        "Poisson arrivals at 50/s" + scale,
             "jobs": args.jobs, "step_scale": args.step_scale, "precision": "mixed",
-            "step": "one velocity-Verlet step of every resident job (value); one job (e2e, plain)",
-            "l2": "fleet working set larger than L2 (no flush needed)"}
+            "step": f"value: {FLEET_CHUNK} velocity-Verlet steps of every job of the stream, all resident "
+                    "(no job reaches its last step, so the timed steps form no thermo record); "
+                    "e2e: the whole stream",
+            "l2": "fleet working set (tens of GB) larger than L2, no flush needed"}
 
 
-def served_jobs(args):
+def served_jobs(args, atoms=True, every=1):
+    """The stream's job descriptions (every `every`-th job), with their
+    atoms unless atoms=False."""
     from fmd_gb300 import serve
-    jobs = serve.served_stream(args.jobs, seed=5, step_scale=args.step_scale)
-    for j in jobs:
-        j["x"], j["v"], j["l"] = serve.job_atoms(j)
+    jobs = serve.served_stream(args.jobs, seed=5, step_scale=args.step_scale)[::every]
+    if atoms:
+        for j in jobs:
+            j["x"], j["v"], j["l"] = serve.job_atoms(j)
     return jobs
 
 
-def cpu_port_jobs(jobs, threads, budget_s=12.0, max_steps=10):
+def cpu_port_job(j, threads, setfl, max_atom_steps=4.0e6, max_steps=10):
     """The CPU oracle port (restated reference algorithm, OpenMP, per-thread
-    buffers) on the first jobs of the sample, one at a time; returns
-    (atom-steps/s, description of the sample)."""
+    buffers) on one job of the stream: set-up and initial forces untimed,
+    then k velocity-Verlet steps timed (k bounded by max_atom_steps);
+    returns (atom-steps, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from fmd_gb300 import serve, workloads
-    done_as, spent, used = 0.0, 0.0, []
+    from fmd_gb300 import serve
+    if "x" not in j:
+        j["x"], j["v"], j["l"] = serve.job_atoms(j)
+    P = serve.POTENTIALS[j["pot"]]
+    nc, cellh, order, counts = serve.host_binning(j["x"], j["l"], P["rc"])
+    if j["pot"] == "lj":
+        pots = [("lj", 0, 0, 3.405, 0.0104, 8.5125)]
+    elif j["pot"] == "morse":
+        pots = [("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)]
+    else:
+        pots = [("eam", 0, 0)]
+    o = pyoracle.Oracle(threads=threads)
+    o.setup([j["l"]] * 3, [1, 1, 1], [nc] * 3, [cellh] * 3, [("Cu", P["mass"])], pots,
+            setfl if j["pot"] == "eam" else None)
+    n = len(order)
+    cell = np.repeat(np.arange(nc ** 3, dtype=np.int32), counts)
+    o.upload(cell, j["x"][order], j["v"][order], np.zeros(n, np.uint32), np.zeros(n, np.int32),
+             order.astype(np.uint32), nc ** 3)
+    o.forces(-1)
+    k = int(max(1, min(max_steps, j["steps"], max_atom_steps // n)))
+    t0 = time.perf_counter()
+    o.vv(k, P["dt"])
+    dt = time.perf_counter() - t0
+    o.close()
+    return float(n * k), dt
+
+
+def cpu_port_jobs(jobs, threads, budget_s=12.0):
+    """cpu_port_job over the given jobs, one at a time, until budget_s of
+    timed CPU work; returns (atom-steps/s, one-line description)."""
+    from fmd_gb300 import workloads
+    done_as, spent, used = 0.0, 0.0, {}
     with tempfile.TemporaryDirectory() as work:
         setfl = workloads.write_analytic_eam(os.path.join(work, "analytic.eam.alloy"))
         for j in jobs:
             if spent >= budget_s:
                 break
-            P = serve.POTENTIALS[j["pot"]]
-            nc, cellh, order, counts = serve.host_binning(j["x"], j["l"], P["rc"])
-            if j["pot"] == "lj":
-                pots = [("lj", 0, 0, 3.405, 0.0104, 8.5125)]
-            elif j["pot"] == "morse":
-                pots = [("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)]
-            else:
-                pots = [("eam", 0, 0)]
-            o = pyoracle.Oracle(threads=threads)
-            o.setup([j["l"]] * 3, [1, 1, 1], [nc] * 3, [cellh] * 3, [("Cu", P["mass"])], pots,
-                    setfl if j["pot"] == "eam" else None)
-            n = len(order)
-            cell = np.repeat(np.arange(nc ** 3, dtype=np.int32), counts)
-            o.upload(cell, j["x"][order], j["v"][order], np.zeros(n, np.uint32), np.zeros(n, np.int32),
-                     order.astype(np.uint32), nc ** 3)
-            o.forces(-1)
-            k = max(1, min(max_steps, j["steps"]))
-            t0 = time.perf_counter()
-            o.vv(k, P["dt"])
-            dt = time.perf_counter() - t0
-            o.close()
-            done_as += n * k
-            spent += dt
-            used.append(f"{j['pot']} {n} atoms x {k} steps")
-    return done_as / spent, f"{len(used)} jobs of the sample, one at a time: " + "; ".join(used)
+            a, t = cpu_port_job(j, threads, setfl)
+            done_as += a
+            spent += t
+            used[j["pot"]] = used.get(j["pot"], 0) + 1
+    desc = (f"{sum(used.values())} jobs of the stream (every {REF_EVERY}th; "
+            + ", ".join(f"{v} {k}" for k, v in sorted(used.items()))
+            + f"), one at a time, up to 10 steps or 4e6 atom-steps each, {threads} threads")
+    return done_as / spent, desc
+
+
+def plain_sample(L, eam, jobs, every=PLAIN_EVERY, nsteps=PLAIN_STEPS):
+    """The plain arm: jobs of the stream one at a time through the plain
+    single-system binary64 path (the path libfmd.so's fmd_dync_integrate
+    drives).  Every `every`-th job: set-up plus its first step timed as a
+    fixed cost, then up to `nsteps` steps timed; the job's time is the fixed
+    cost plus the per-step time times its remaining steps (the plain path
+    rebuilds its exact neighbour list every step, so a step costs the same
+    all along).  Returns (atom-steps/s, details)."""
+    from fmd_gb300 import serve
+    t_total, as_total, timed_s = 0.0, 0.0, 0.0
+    drifts = []
+    for j in jobs[::every]:
+        t0 = time.perf_counter()
+        one = serve.Single(L, j["pot"], j["x"], j["v"], j["l"], precision=serve.PREC_FP64, eam=eam)
+        one.steps(1)
+        one.thermo()                        # synchronises
+        t1 = time.perf_counter()
+        k = min(nsteps, j["steps"] - 1)
+        if k > 0:
+            one.steps(k)
+            t = one.thermo()
+        else:
+            t = one.thermo()
+        t2 = time.perf_counter()
+        e0 = one.th0.kinetic + one.th0.potential
+        drifts.append(abs(t.kinetic + t.potential - e0) / abs(e0))
+        one.close()
+        t_total += (t1 - t0) + ((t2 - t1) * (j["steps"] - 1) / k if k > 0 else 0.0)
+        as_total += float(len(j["x"])) * j["steps"]
+        timed_s += t2 - t0
+    return as_total / t_total, {"jobs": len(jobs[::every]), "every": every, "steps_timed_per_job": nsteps,
+                                "seconds_timed": timed_s, "seconds_extrapolated": t_total,
+                                "median_rel_energy_drift": float(np.median(drifts))}
 
 
 def run_served(args):
@@ -432,15 +496,17 @@ def run_served(args):
     eam = serve.eam_tables(L)
     jobs = served_jobs(args)
     n_atoms = sum(len(j["x"]) for j in jobs)
-    K, W = args.steps, max(args.warmup, 8)
+    K, W = args.steps, args.warmup
 
-    # --- value: the whole sample resident in HBM, K fleet steps ----------
-    fleet = serve.Server(L, budget_bytes=200 << 30, max_jobs=len(jobs) + 1, chunk_steps=1, eam=eam)
+    # --- value: the whole stream resident in HBM, K fleet steps of
+    # FLEET_CHUNK velocity-Verlet steps of every job --------------------
+    fleet = serve.Server(L, budget_bytes=240 << 30, max_jobs=len(jobs) + 1, chunk_steps=FLEET_CHUNK, eam=eam)
     for j in jobs:
-        fleet.submit(j["pot"], j["x"], j["v"], j["l"], W + K + 8, precision=serve.PREC_MIXED)
+        fleet.submit(j["pot"], j["x"], j["v"], j["l"], (W + K + 2) * FLEET_CHUNK, precision=serve.PREC_MIXED)
     fleet.admit()
     st = fleet.stats()
-    assert st.running == len(jobs), "the sample does not fit the fleet budget"
+    assert st.running == len(jobs), "the stream does not fit the fleet budget"
+    fleet_bytes = st.bytes_in_use
     for _ in range(W):              # warm-up; the autotuner picks block sizes here
         fleet.run_resident(1)
     sampler = ClockSampler()
@@ -456,26 +522,27 @@ def run_served(args):
         phases[p] = {"bin_ms": pm[0], "nlist_ms": pm[1], "density_ms": pm[2], "force_ms": pm[3],
                      "atoms": atoms, "jobs": members, "threads_per_block": tuned[p]}
     fleet.close()
-    value = n_atoms * K / (ms * 1e-3)
+    value = n_atoms * K * FLEET_CHUNK / (ms * 1e-3)
     if args.only == "fleet":
-        return {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1, "steps": K,
+        return {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": 1, "steps": K,
                 "warmup": W, "ms_per_step": ms / K, "config": served_config(args), "gpu_launches": int(k1 - k0),
                 "phases": phases, "clocks": clocks, "note": "resident fleet only (--only fleet)"}
     # peak of the binary32 FMA pipe (measured microkernel)
     h = C.c_void_p()
     serve.check(L, L.fmdg_create(C.byref(h), 0), "create")
-    peak32, peak64 = C.c_double(), C.c_double()
+    peak32 = C.c_double()
     serve.check(L, L.fmdg_measure_fma_peak(h, 0, C.byref(peak32)), "peak")
-    serve.check(L, L.fmdg_measure_fma_peak(h, 1, C.byref(peak64)), "peak")
     L.fmdg_destroy(h)
     dom = max(serve.POT_NAMES, key=lambda p: phases[p]["force_ms"])
     fl = SERVED_FORCE_FLOP[dom] * phases[dom]["atoms"]
     achieved = fl / (phases[dom]["force_ms"] * 1e-3) / 1e12
 
-    # --- e2e: the sample streamed through the request loop ---------------
+    # --- e2e: the stream through the request loop ------------------------
     srv = serve.Server(L, budget_bytes=64 << 30, max_jobs=1024, chunk_steps=32, eam=eam)
     ids = [None] * len(jobs)
     nxt = 0
+    sampler_e2e = ClockSampler()
+    sampler_e2e.start()
     t0 = srv.now()
     active = 0
     while nxt < len(jobs) or active > 0:
@@ -489,6 +556,7 @@ def run_served(args):
             if wait_s > 0:
                 time.sleep(min(wait_s, 0.01))
         active = srv.progress(wait=(nxt >= len(jobs)))
+    clocks_e2e = sampler_e2e.stop()
     res = [srv.result(i) for i in ids]
     sst = srv.stats()
     srv.close()
@@ -511,21 +579,8 @@ def run_served(args):
 
     served_drift = float(np.median([drift(r) for r in res]))
 
-    # --- plain: the same jobs one at a time, binary64 single-system path -----
-    plain = {}
-    for name, prec in (("fp64", serve.PREC_FP64),):
-        t_start = time.perf_counter()
-        drifts = []
-        for j in jobs:
-            one = serve.Single(L, j["pot"], j["x"], j["v"], j["l"], precision=prec, eam=eam)
-            one.steps(j["steps"])
-            t = one.thermo()
-            e0 = one.th0.kinetic + one.th0.potential
-            drifts.append(abs(t.kinetic + t.potential - e0) / abs(e0))
-            one.close()
-        t_plain = time.perf_counter() - t_start
-        plain[name] = {"value": job_as.sum() / t_plain, "unit": "atom-steps/s", "seconds": t_plain,
-                       "median_rel_energy_drift": float(np.median(drifts))}
+    # --- plain: jobs one at a time, binary64 single-system path ------------
+    plain_value, plain = plain_sample(L, eam, jobs)
 
     # --- force error of the mixed path against binary64 at identical
     # positions (a thermalised state: 20 binary64 steps), one job per potential
@@ -546,41 +601,38 @@ def run_served(args):
     if args.skip_cpu:
         cpu_value, cpu_sample = None, "skipped"
     else:
-        cpu_value, cpu_sample = cpu_port_jobs(jobs, cores)
+        cpu_value, cpu_sample = cpu_port_jobs(jobs[::REF_EVERY], cores)
     out = {
-        "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 1,
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": 1,
         "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32-compute/f64-accumulate", "data": "synthetic",
+        "served_over_plain_fp64": e2e_value / plain_value,
+        "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+        "max_rel_force_err_mixed_vs_fp64": max(ferr.values()),
+        "median_rel_energy_drift": served_drift,
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s",
+                "h2d_bytes_per_step": h2d / total_steps, "d2h_bytes_per_step": d2h / total_steps,
+                "how": "fmdg_srv_* request loop, jobs submitted from host arrays at their arrival times; "
+                       "wall clock first arrival to last completion; bytes per job-step"},
+        "plain_fp64": {"value": plain_value, "unit": "atom-steps/s", **plain},
         "config": served_config(args),
         "gpu_launches": int(k1 - k0),
-        "served": {"jobs": len(jobs), "atoms_resident": n_atoms,
-                   "throughput_e2e": e2e_value, "plain_fp64_e2e": plain["fp64"]["value"],
-                   "served_over_plain_fp64": e2e_value / plain["fp64"]["value"],
-                   "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
-                   "makespan_s": float(span), "median_rel_energy_drift": served_drift,
-                   "plain": plain, "max_rel_force_err_mixed_vs_fp64": ferr,
-                   "device_error_bits": errbits, "bytes_peak": sst.bytes_peak,
-                   "graph_rebuilds": int(sum(sst.pack_rebuilds[c][m] for c in range(4) for m in range(2))),
-                   "threads_per_block": tuned},
-        "phases": phases,
-        "roofline": {"bound": "fp32-issue", "kernel": f"k_force<LocPack> ({dom} pack: pair forces + finish step)",
+        "roofline": {"bound": "fp32-issue", "kernel": f"k_force_skin<LocPack> ({dom} packs: pair forces + finish step)",
                      "achieved": achieved, "peak": peak32.value, "unit": "TFLOP/s",
                      "frac": achieved / peak32.value,
                      "peak_source": "measured FMA-chain microkernel (MEASURED_PEAKS.json has no CUDA-core peak)",
                      "traffic": (FORCE_DRAM_BYTES_PER_ATOM["morse_pack"] * phases[dom]["atoms"] if dom == "morse"
                                  else None),
-                     "traffic_note": "DRAM bytes of the force phase of this category per step (all its packs), "
-                                     "scaled by atoms from an ncu capture of a 149616-atom Morse pack",
                      **hbm_side(FORCE_DRAM_BYTES_PER_ATOM["morse_pack"] * phases[dom]["atoms"] if dom == "morse"
                                 else None, phases[dom]["force_ms"])},
-        "clocks": clocks,
-        "e2e": {"value": e2e_value, "unit": "atom-steps/s",
-                "h2d_bytes_per_step": h2d / total_steps, "d2h_bytes_per_step": d2h / total_steps,
-                "how": "fmdg_srv_* request loop: jobs submitted from host arrays at their arrival times, "
-                       "admitted by HBM budget, uploaded, stepped in packs, results read back; wall clock "
-                       "from the first arrival to the last completion; bytes per job-step"},
         "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
                          "sample": cpu_sample},
+        "clocks": clocks,
+        "served": {"jobs": len(jobs), "atoms": n_atoms, "fleet_bytes": fleet_bytes,
+                   "makespan_s": float(span), "force_err": ferr, "device_error_bits": errbits,
+                   "e2e_bytes_peak": sst.bytes_peak, "threads_per_block": tuned, "clocks_e2e": clocks_e2e,
+                   "graph_rebuilds": int(sum(sst.pack_rebuilds[c][m] for c in range(4) for m in range(2)))},
+        "phases": phases,
     }
     return out
 
@@ -588,40 +640,54 @@ def run_served(args):
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: the
     oracle port (the reference's own sources are not present on the GPU
-    host), all threads, same workload, metric and unit."""
+    host), all threads, same workload, metric and unit.  Each step is a
+    bounded sample: one job of the stream (every REF_EVERY-th, in turn) for
+    up to 10 velocity-Verlet steps (served), or up to 10 steps of the
+    256 000-atom EAM system (eam256k)."""
     cores = os.cpu_count() or 1
     if args.workload == "served":
-        jobs = served_jobs(args)
-        vals, sample = [], ""
-        for _ in range(args.warmup):            # untimed, short
-            cpu_port_jobs(jobs, cores, budget_s=1.0)
-        for _ in range(max(1, min(args.steps, 3))):
-            v, sample = cpu_port_jobs(jobs, cores, budget_s=8.0)
-            vals.append(v)
-        value = float(np.median(vals))
-        out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s",
-               "n_gpus": 0, "steps": len(vals), "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        from fmd_gb300 import workloads
+        jobs = served_jobs(args, atoms=False, every=REF_EVERY)
+        done_as, spent = 0.0, 0.0
+        with tempfile.TemporaryDirectory() as work:
+            setfl = workloads.write_analytic_eam(os.path.join(work, "analytic.eam.alloy"))
+            for s in range(args.warmup + args.steps):
+                j = jobs[s % len(jobs)]
+                a, t = cpu_port_job(j, cores, setfl)
+                if s >= args.warmup:
+                    done_as += a
+                    spent += t
+                j.pop("x", None)
+                j.pop("v", None)
+        value = done_as / spent
+        out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom-steps/s",
+               "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": spent / args.steps * 1e3,
+               "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": served_config(args),
                "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                                "sample": f"median of {len(vals)} samples; each: {sample}"},
+                                "sample": f"each step one job of the stream (every {REF_EVERY}th, in turn), "
+                                          "up to 10 steps or 4e6 atom-steps"},
                "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
-    vals = []
     for _ in range(args.warmup):                # untimed, short
         cpu_port_run(cores, target_s=1.0, max_steps=1)
-    for _ in range(max(1, min(args.steps, 3))):
-        v, k = cpu_port_run(cores, target_s=8.0, max_steps=10)
-        vals.append(v)
-    value = float(np.median(vals))
+    done_as, spent = 0.0, 0.0
     w = WORKLOAD
+    natoms = int(np.prod(w["cells"])) * 4
+    for _ in range(args.steps):
+        v, k = cpu_port_run(cores, target_s=8.0, max_steps=10)
+        done_as += natoms * k
+        spent += natoms * k / v
+    value = done_as / spent
     out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 0,
-           "steps": len(vals), "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": spent / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic",
            "config": {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
-                                  "300 K, dt 1 fs, NVE", "atoms": int(np.prod(w["cells"])) * 4},
+                                  "300 K, dt 1 fs, NVE", "atoms": natoms},
            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                            "sample": f"median of {len(vals)} timed samples of up to 10 steps each"},
+                            "sample": "each step up to 10 velocity-Verlet steps of the system"},
            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -629,7 +695,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
@@ -637,7 +703,7 @@ def main():
     ap.add_argument("--workload", default="served", choices=["served", "eam256k"])
     ap.add_argument("--only", default="all", choices=["all", "fleet"],
                     help="served: 'fleet' times the resident fleet only (profiling runs)")
-    ap.add_argument("--jobs", type=int, default=SERVED_JOBS, help="served: jobs of the stream sample")
+    ap.add_argument("--jobs", type=int, default=SERVED_JOBS, help="served: jobs of the stream (its first jobs)")
     ap.add_argument("--step-scale", type=float, default=SERVED_STEP_SCALE,
                     help="served: factor on step counts and arrival times")
     args = ap.parse_args()

@@ -1,13 +1,12 @@
 """Build the GB300 engine in-tree (no cmake, no pip install).
 
-    python -m fmd_gb300.build          # libfmd.so + the oracle port
+    python -m fmd_gb300.build          # libfmd.so
 
-Outputs (git-ignored):
+Output (git-ignored):
   fmd_gb300/lib/libfmd.so   host C (fmd.h API) + sm_103a CUDA engine (fmdg.h)
-  oracle/liboracle.so       CPU restatement of the reference's hot path
-                            (test infrastructure; never linked into libfmd.so)
-  oracle/_ref/libfmdref.so  the reference compiled from its own sources, only
-                            when they are present (this container)
+
+The test infrastructure (the CPU oracle) has its own recipe,
+oracle/build.py.
 """
 from __future__ import annotations
 
@@ -24,8 +23,6 @@ INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIBFMD = os.path.join(LIBDIR, "libfmd.so")
-ORACLE_LIB = os.path.join(ROOT, "oracle", "liboracle.so")
-REF_SRC = "/root/reference"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -80,30 +77,8 @@ def build_libfmd(verbose=False):
     return LIBFMD
 
 
-def build_oracle():
-    src = os.path.join(ROOT, "oracle", "fmd_oracle.c")
-    if not os.path.exists(src):
-        return None
-    deps = [src] + glob.glob(os.path.join(ROOT, "oracle", "*.h"))
-    if _stale(ORACLE_LIB, deps):
-        _run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
-              "-I" + os.path.join(ROOT, "oracle"), src, "-o", ORACLE_LIB, "-lm"])
-    return ORACLE_LIB
-
-
-def build_reference():
-    """Compile the reference from its own sources (only where present)."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src")):
-        return None
-    _run(["make", "-s", "-C", ROOT, "-f", "oracle/Makefile.ref", "REF=" + REF_SRC, "-j8"])
-    return os.path.join(ROOT, "oracle", "_ref", "libfmdref.so")
-
-
 def build(verbose=False):
-    lib = build_libfmd(verbose)
-    build_oracle()
-    build_reference()
-    return lib
+    return build_libfmd(verbose)
 
 
 if __name__ == "__main__":

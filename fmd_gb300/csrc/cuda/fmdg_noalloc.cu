@@ -19,6 +19,14 @@
 // overwrites it completely, so calls that overlap on the GPU (different
 // streams, no ordering between them) race and must be serialised by the
 // caller.
+//
+// The first look-up is made under a lock, so first calls from several host
+// threads are safe.  A cudaDeviceReset of a device invalidates the address
+// kept for it: this entry point must not be called on that device again in
+// the same process.  Atom kinds must lie in [0, nkinds): an atom whose kind,
+// or a neighbour's kind, lies outside gets NaN forces (and the energy is
+// NaN), the pair table is never read out of range.
+#include <mutex>
 #include <stdio.h>
 #include <string.h>
 #include "fmdg_internal.cuh"
@@ -65,7 +73,8 @@ __global__ void __launch_bounds__(128) k_pair_noalloc(NoallocArgs a, const doubl
         const int c = cell_of[i];
         const int cx = c / (a.nc[1] * a.nc[2]), cy = (c / a.nc[2]) % a.nc[1], cz = c % a.nc[2];
         const double xi[3] = {x[i], x[n + i], x[2 * (size_t)n + i]};
-        const int ki = kind[i];
+        const unsigned ki = kind[i];
+        bool bad = ki >= (unsigned)a.nkinds;
         double f[3] = {0.0, 0.0, 0.0};
         for (int code = 0; code < 27; code++)
         {
@@ -78,7 +87,13 @@ __global__ void __launch_bounds__(128) k_pair_noalloc(NoallocArgs a, const doubl
             for (int j = cell_start[nb]; j < cell_start[nb + 1]; j++)
             {
                 if (code == 13 && j == i) continue;
-                const fmdg_pair_t &pp = a.pairs[ki * a.nkinds + kind[j]];
+                const unsigned kj = kind[j];
+                if (bad || kj >= (unsigned)a.nkinds)
+                {
+                    bad = true;     // kinds outside the pair table: no table read
+                    continue;
+                }
+                const fmdg_pair_t &pp = a.pairs[ki * a.nkinds + kj];
                 double rv[3];
                 for (int d = 0; d < 3; d++)
                 {
@@ -112,6 +127,11 @@ __global__ void __launch_bounds__(128) k_pair_noalloc(NoallocArgs a, const doubl
                 }
             }
         }
+        if (bad)
+        {
+            for (int d = 0; d < 3; d++) f[d] = __longlong_as_double(0x7ff8000000000000ll);
+            pe = f[0];
+        }
         for (int d = 0; d < 3; d++) F[(size_t)d * n + i] = f[d];
     }
     // deterministic block sum -> this block's slot of the static partials
@@ -138,6 +158,7 @@ __global__ void k_pair_noalloc_final(const double *partials, int nblocks, double
 }
 
 double *g_partials_addr[FMDG_NOALLOC_MAX_DEVICES];
+std::mutex g_partials_lock;   // guards the first look-up on each device
 
 } // namespace
 
@@ -175,16 +196,21 @@ extern "C" int fmdg_pair_forces_noalloc(int n, const int nc[3], const int pbc[3]
     int dev = 0;
     FMDG_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= FMDG_NOALLOC_MAX_DEVICES) return fmdg_set_error("fmdg_pair_forces_noalloc: device id");
-    if (g_partials_addr[dev] == nullptr)
+    double *partials = nullptr;
     {
-        void *p = nullptr;
-        FMDG_CK(cudaGetSymbolAddress(&p, g_noalloc_partials));
-        g_partials_addr[dev] = (double *)p;
+        std::lock_guard<std::mutex> lk(g_partials_lock);
+        if (g_partials_addr[dev] == nullptr)
+        {
+            void *p = nullptr;
+            FMDG_CK(cudaGetSymbolAddress(&p, g_noalloc_partials));
+            g_partials_addr[dev] = (double *)p;
+        }
+        partials = g_partials_addr[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
     const int nb = n > 0 ? (n + 127) / 128 : 1;
-    k_pair_noalloc<<<nb, 128, 0, st>>>(a, x, kind, cell_start, cell_of, F, g_partials_addr[dev]);
-    k_pair_noalloc_final<<<1, 256, 0, st>>>(g_partials_addr[dev], nb, pe);
+    k_pair_noalloc<<<nb, 128, 0, st>>>(a, x, kind, cell_start, cell_of, F, partials);
+    k_pair_noalloc_final<<<1, 256, 0, st>>>(partials, nb, pe);
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
 }

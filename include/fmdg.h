@@ -219,11 +219,15 @@ int fmdg_run_host(fmdg_sys_t *s, int nsteps, double dt, int group, const double 
    cell_start[ncell+1] and cell_of[n] of atoms sorted by cell (flat cell
    index z + nz*(y + ny*x)); F (3 rows of n) and *pe (one double) receive the
    result.  pairs: host table of nkinds*nkinds entries (LJ or Morse only,
-   nkinds <= 4).  stream: a cudaStream_t or NULL.  Scratch is a fixed
+   nkinds <= 4); kind[i] must lie in [0, nkinds): an atom whose kind, or a
+   neighbour's, lies outside gets NaN forces and *pe is NaN (the table is
+   never read out of range).  stream: a cudaStream_t or NULL.  Scratch is a fixed
    512 KiB file-scope device array: at most 1048576 atoms per call (larger
    n returns FMDG_E_ARG with a message); the first call on a device looks up
-   that array's address and should come before any stream capture; calls
-   that overlap on the GPU share the array and race. */
+   that array's address (under a lock: first calls from several host
+   threads are safe) and should come before any stream capture; after a
+   cudaDeviceReset of a device do not call it on that device again in the
+   same process; calls that overlap on the GPU share the array and race. */
 int fmdg_pair_forces_noalloc(int n, const int nc[3], const int pbc[3], const double l[3], int nkinds,
                              const fmdg_pair_t *pairs, const double *x, const unsigned *kind,
                              const int *cell_start, const int *cell_of, double *F, double *pe, void *stream);

@@ -1,6 +1,6 @@
 """ctypes wrapper of the CPU oracle (oracle/fmd_oracle.c) -- test
 infrastructure: used by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline only.  The oracle is built by `fmd_gb300.build.build_oracle()`.
+baseline only.  The oracle is built by `oracle/build.py` (build_oracle).
 """
 from __future__ import annotations
 
@@ -31,8 +31,11 @@ def _ptr(a):
 
 def _lib():
     if not os.path.exists(LIB):
-        from fmd_gb300.build import build_oracle
-        build_oracle()
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(HERE, "build.py"))
+        ob = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(ob)
+        ob.build_oracle()
     L = C.CDLL(LIB)
     L.oracle_create.restype = P
     for name, args in [("oracle_destroy", [P]), ("oracle_set_threads", [P, C.c_int]),

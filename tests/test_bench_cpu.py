@@ -55,6 +55,12 @@ def test_clock_sampler_without_nvidia_smi(monkeypatch, tmp_path):
     assert out["sm_mhz"] is None and out["reasons"] == ["nvidia-smi unavailable"]
 
 
+def test_clock_summary_without_max_clock():
+    # readings whose max-clock field is not a number (or that are short)
+    out = bench.summarize_clocks([["1980", "[N/A]", "0x0"], ["1990"]])
+    assert out["sm_mhz"] == 1990.0 and out["sm_max_mhz"] is None and out["samples"] == 2
+
+
 def test_hbm_side():
     out = bench.hbm_side(1.0e9, 1.0)       # 1 GB in 1 ms
     assert abs(out["dram_gbs"] - 1000.0) < 1e-9
@@ -70,7 +76,8 @@ def test_reference_arm_line():
     lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
-    assert d["impl"] == "reference" and d["metric"] == "atom-steps/s" and d["value"] > 0
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["value"] > 0
+    assert d["unit"] == "atom-steps/s" and d["config"]["jobs"] == 2048 and d["config"]["step_scale"] == 1.0
     assert d["warmup"] == 3 and d["steps"] == 1 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
