@@ -148,6 +148,7 @@ _DUMP_PROTOS = {
     "refresh": (None, [P]),
     "update_forces": (None, [P]),
     "potential_energy": (D, [P]),
+    "virial": (D, [P]),
     "grid": (None, [P, P, P, P, P]),
     "ttm_1d": (C.c_int, [P, P, P, P, P, P]),
 }
@@ -199,6 +200,8 @@ class Lib:
                             _ptr(out["F"]), _ptr(out["vaream"]))
         assert k == n, (k, n)
         out["pe"] = self.wb("potential_energy")(md)
+        if self.has(self.prefix + "virial"):
+            out["virial"] = self.wb("virial")(md)
         return out
 
     def set_state(self, md, x=None, v=None):

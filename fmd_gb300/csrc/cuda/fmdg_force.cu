@@ -360,14 +360,14 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
     const Side S = g.side[dyn->cur];
     const int cap = g.cap;
     const int i = bx * blockDim.x + threadIdx.x;
-    // pe, m v^2, m v (3), count
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    // pe, m v^2, m v (3), count, pair virial
+    double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     if (i < n)
     {
         const int ki = S.kind[i];
         const bool active = (group < 0 || S.group[i] == group);
         double f[3] = {0.0, 0.0, 0.0};
-        double pe = 0.0;
+        double pe = 0.0, vir = 0.0;
         if (active)
         {
             const CellXYZ ci = cell_xyz(g, S.cell_of[i]);
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[i]) : dfl{0.f, 0.f};
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
                 const float kmax = (float)(nint - 1);
-                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f}, virs = {0.f, 0.f};
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     float4 jh, jl;
@@ -401,9 +401,11 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             fa, eh);
                     for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(fa, p.rv[d]));
                     pes = df_add(pes, eh);
+                    virs = df_add(virs, df_mul(fa, p.r2));     // rv . (fa rv), both sides of the pair
                 });
                 for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
                 pe = df_to_double(pes);
+                vir = 0.5 * df_to_double(virs);
             }
             else
             {
@@ -411,7 +413,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpf[i] : 0.f;
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
-                Acc32<4> ac;
+                Acc32<5> ac;
                 for_each_pair(g, S, i, ci, [&](int j, int code) {
                     if (group >= 0 && S.group[j] != group) return;
                     const float4 xj = g.xf4[j];
@@ -435,6 +437,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] += rv.y * factor;
                             ac.part[2] += rv.z * factor;
                             ac.part[3] += 0.5f * (eps4 * (inv_rs12 - inv_rs6));
+                            ac.part[4] += factor * r2;
                         }
                     }
                     else if (cat == FMDG_POT_MORSE)
@@ -451,6 +454,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] += factor * rv.y;
                             ac.part[2] += factor * rv.z;
                             ac.part[3] += 0.5f * (D0 * (e2 - 2.f * e1));
+                            ac.part[4] += factor * r2;
                         }
                     }
                     else if (cat == FMDG_POT_EAM)
@@ -470,6 +474,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                             ac.part[1] -= mag * rv.y;
                             ac.part[2] -= mag * rv.z;
                             ac.part[3] += 0.5f * spl_val(tph, b);
+                            ac.part[4] -= mag * r2;
                         }
                     }
                     ac.tick();
@@ -477,6 +482,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
                 ac.flush();
                 for (int d = 0; d < 3; d++) f[d] = ac.total(d);
                 pe = ac.total(3);
+                vir = 0.5 * ac.total(4);
             }
         }
         if (active && g.ttm_on)
@@ -501,6 +507,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
         }
         for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
         acc[0] = pe;
+        acc[6] = vir;
         if (active)
         {
             const double m = sp.mass[ki];
@@ -521,12 +528,12 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_force(__grid_
             acc[5] = 1.0;
         }
     }
-    __shared__ double blk[6];
+    __shared__ double blk[7];
     __shared__ unsigned ticket;
-    block_reduce_store<6>(acc, blk);
+    block_reduce_store<7>(acc, blk);
     if (threadIdx.x == 0)
     {
-        for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
+        for (int k = 0; k < 7; k++) g.partials[(size_t)k * nb + bx] = blk[k];
         __threadfence();
         ticket = atomicAdd(&g.dyn->blocks_done, 1u);
     }

@@ -382,27 +382,31 @@ struct Acc32
 // thermo record (src/integrators.c:78-92) and, when a Berendsen thermostat
 // is active, the velocity scale of the next start step
 // (src/integrators.c:44-50): lambda = sqrt(1 + dt/tau * (T0/T - 1)).
+// Partial rows per block: 0 pair energy, 1 m v^2, 2-4 m v, 5 count,
+// 6 pair virial, 8 embedding energy.  keep_pe: the energy and virial of the
+// last force evaluation stay (thermo-only reductions).
 // Run by one whole block of at most 256 threads.
 __device__ __forceinline__ void final_reduce(const Geo &g, int nblocks, int keep_pe, int with_emb, int thermostat,
                              double dt, double tau, double T0)
 {
-    __shared__ double red[8][7];
+    __shared__ double red[8][8];
     const int t = threadIdx.x;
-    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = t; b < nblocks; b += blockDim.x)
     {
         for (int k = 0; k < 6; k++) s[k] += __ldcg(&g.partials[(size_t)k * nblocks + b]);
         if (with_emb) s[6] += __ldcg(&g.partials[(size_t)nblocks * 8 + b]);
+        if (!keep_pe) s[7] += __ldcg(&g.partials[(size_t)nblocks * 6 + b]);
     }
-    for (int k = 0; k < 7; k++)
+    for (int k = 0; k < 8; k++)
         for (int off = 16; off > 0; off >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], off);
     if ((t & 31) == 0)
-        for (int k = 0; k < 7; k++) red[t >> 5][k] = s[k];
+        for (int k = 0; k < 8; k++) red[t >> 5][k] = s[k];
     __syncthreads();
     if (t == 0)
     {
         for (int w = 1; w < (int)(blockDim.x >> 5); w++)
-            for (int k = 0; k < 7; k++) red[0][k] += red[w][k];
+            for (int k = 0; k < 8; k++) red[0][k] += red[w][k];
         fmdg_thermo_t *th = g.thermo;
         const double mv2 = red[0][1];
         const double N = red[0][5];
@@ -412,7 +416,11 @@ __device__ __forceinline__ void final_reduce(const Geo &g, int nblocks, int keep
         th->momentum[1] = red[0][3];
         th->momentum[2] = red[0][4];
         th->count = N;
-        if (!keep_pe) th->potential = red[0][0] + red[0][6];
+        if (!keep_pe)
+        {
+            th->potential = red[0][0] + red[0][6];
+            th->virial = red[0][7];
+        }
         if (thermostat)
             g.dyn->lambda = sqrt(1 + dt / tau * (T0 / th->temperature - 1));
     }

@@ -772,7 +772,8 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     const int cap = g.cap;
     const int t = bx * blockDim.x + threadIdx.x;
     const bool thermo = loc_thermo(loc, g);
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    // pe, m v^2, m v (3), count, pair virial
+    double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     const int i = (t < cap) ? g.pos[t] : -1;
     if (i >= 0)
     {
@@ -781,7 +782,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
         const bool active = (group < 0 || g.gslot[t] == group);
         const int nk = g.nkinds;
         double f[3] = {0.0, 0.0, 0.0};
-        double pe = 0.0;
+        double pe = 0.0, vir = 0.0;
         if (active)
         {
             const int nint = g.Nr2 - 1;
@@ -793,7 +794,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 const dfl fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? df_of(g.fpdf[t]) : dfl{0.f, 0.f};
                 const dfl inv_h = df_of(df_split(g.inv_dr2));
                 const float kmax = (float)(nint - 1);
-                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f};
+                dfl fs[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, pes = {0.f, 0.f}, virs = {0.f, 0.f};
                 for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xjf, float4 o) {
                     if (group >= 0 && g.gslot[js] != group) return;
                     const int pidx = ki * nk + __float_as_int(xjf.w);
@@ -807,9 +808,11 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             fa, eh);
                     for (int d = 0; d < 3; d++) fs[d] = df_add(fs[d], df_mul(fa, p.rv[d]));
                     pes = df_add(pes, eh);
+                    virs = df_add(virs, df_mul(fa, p.r2));     // rv . (fa rv), both sides of the pair
                 });
                 for (int d = 0; d < 3; d++) f[d] = df_to_double(fs[d]);
                 pe = df_to_double(pes);
+                vir = 0.5 * df_to_double(virs);
             }
             else if constexpr (LEAN)
             {
@@ -846,11 +849,14 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         e = 0.5f * (pq.x * (e2 - 2.f * e1));
                     }
                 };
-                // E: this step forms the energy (thermo record); otherwise the
-                // energy terms are dropped from the walk
-                auto walk = [&](auto with_e) {
+                // E: the walk sums the energy, V: the pair virial (rv . F =
+                // fa r^2); both on steps that form the thermo record only
+                // (the EAM walk keeps its energy term on every step)
+                auto walk = [&](auto with_e, auto with_v) {
                     constexpr bool E = decltype(with_e)::value;
-                    Acc32<E ? 4 : 3> ac;
+                    constexpr bool V = decltype(with_v)::value;
+                    constexpr int NA = V ? 5 : (E ? 4 : 3);
+                    Acc32<NA> ac;
                     if constexpr (CAT == CAT_EAM)
                     {
                         const float band = 1e-4f * rc2f;
@@ -874,6 +880,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
                             if constexpr (E) ac.part[3] += 0.5f * spl_val(tph, b);
+                            if constexpr (V) ac.part[NA - 1] += fa * r2;
                         }, [&](int k) { ac.entries(k); });
                         ac.flush();
                     }
@@ -905,6 +912,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
                             if constexpr (E) ac.part[3] += e;
+                            if constexpr (V) ac.part[NA - 1] += fa * r2;
                         }, [&](int k) { ac.entries(k); });
                         ac.flush();
                         if (npend == 1)
@@ -918,6 +926,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                                 ac.part[1] += fa * prv.y;
                                 ac.part[2] += fa * prv.z;
                                 if constexpr (E) ac.part[3] += e;
+                                if constexpr (V) ac.part[NA - 1] += fa * r2;
                                 ac.flush();
                             }
                         }
@@ -934,28 +943,30 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                                 ac.part[1] += fa * rv.y;
                                 ac.part[2] += fa * rv.z;
                                 if constexpr (E) ac.part[3] += e;
+                                if constexpr (V) ac.part[NA - 1] += fa * r2;
                             }, [&](int k) { ac.entries(k); });
                             ac.flush();
                         }
                     }
                     for (int d = 0; d < 3; d++) f[d] = ac.total(d);
                     if constexpr (E) pe = ac.total(3);
+                    if constexpr (V) vir = 0.5 * ac.total(NA - 1);
                 };
                 // (the EAM walk keeps its energy term: dropping it measured
                 // slower for that kernel)
-                if constexpr (CAT == CAT_EAM)
-                    walk(std::true_type{});
-                else if (thermo)
-                    walk(std::true_type{});
+                if (thermo)
+                    walk(std::true_type{}, std::true_type{});
+                else if constexpr (CAT == CAT_EAM)
+                    walk(std::true_type{}, std::false_type{});
                 else
-                    walk(std::false_type{});
+                    walk(std::false_type{}, std::false_type{});
             }
             else
             {
                 const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpb[t] : 0.f;
                 const float inv_h = (float)g.inv_dr2;
                 const float kmax = (float)(nint - 1);
-                Acc32<4> ac;
+                Acc32<5> ac;
                 for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                     if (group >= 0 && g.gslot[js] != group) return;
                     const int pidx = ki * nk + __float_as_int(xj.w);
@@ -973,6 +984,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             ac.part[1] += rv.y * fa;
                             ac.part[2] += rv.z * fa;
                             ac.part[3] += e;
+                            ac.part[4] += fa * r2;
                         }
                     }
                     else if (cat == FMDG_POT_MORSE)
@@ -985,6 +997,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
                             ac.part[3] += e;
+                            ac.part[4] += fa * r2;
                         }
                     }
                     else if (cat == FMDG_POT_EAM)
@@ -1004,6 +1017,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                             ac.part[1] -= mag * rv.y;
                             ac.part[2] -= mag * rv.z;
                             ac.part[3] += 0.5f * spl_val(tph, b);
+                            ac.part[4] -= mag * r2;
                         }
                     }
                     ac.tick();
@@ -1011,6 +1025,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 ac.flush();
                 for (int d = 0; d < 3; d++) f[d] = ac.total(d);
                 pe = ac.total(3);
+                vir = 0.5 * ac.total(4);
             }
         }
         if (active && g.ttm_on)
@@ -1032,6 +1047,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
         }
         for (int d = 0; d < 3; d++) g.F[(size_t)d * cap + i] = f[d];
         acc[0] = pe;
+        acc[6] = vir;
         if (active)
         {
             const double m = sp.mass[ki];
@@ -1055,13 +1071,13 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
             }
         }
     }
-    __shared__ double blk[6];
+    __shared__ double blk[7];
     __shared__ unsigned ticket;
-    if (thermo) block_reduce_store<6>(acc, blk);
+    if (thermo) block_reduce_store<7>(acc, blk);
     if (threadIdx.x == 0)
     {
         if (thermo)
-            for (int k = 0; k < 6; k++) g.partials[(size_t)k * nb + bx] = blk[k];
+            for (int k = 0; k < 7; k++) g.partials[(size_t)k * nb + bx] = blk[k];
         __threadfence();
         ticket = atomicAdd(&dyn->blocks_done, 1u);
     }

@@ -10,12 +10,16 @@
 //   TTM type 2 solve    src/ttm.c:154-192, 314-383 (tabulated C, G; Zhigilei K)
 //   xi                  src/ttm.c:305-311, 376-382
 //   friction term       src/forces.c:292-330 (added in k_force)
-// Per-cell sums over atoms use warp-aggregated binary64 atomics (lanes with
-// the same cell are combined by shuffles, one atomic per group); the order
-// of the global additions is not fixed, so these fields can differ from run
-// to run in the last bits.  The solver runs in one thread block: the grid
-// has tens to hundreds of cells and the substeps are sequential; every
-// quantity is binary64.
+// Per-cell sums over atoms are deterministic: lanes of a warp with the same
+// cell are combined by shuffles in lane order (binary64), and each group's
+// sum is added to the cell as a 64-bit fixed-point integer (integer atomics
+// give the same total whatever order the additions arrive in).  Scales:
+// mass 2^44, momentum 2^40, thermal kinetic term 2^36 (internal units;
+// resolution 6e-14, 9e-13 and 1.5e-11 per group, far below the binary64
+// rounding of the reference's own sums relative to the cell totals); a term
+// beyond the fixed-point range sets FMDG_ERRBIT_INTERNAL and is skipped.
+// The solver runs in one thread block: the grid has tens to hundreds of
+// cells and the substeps are sequential; every quantity is binary64.
 #include "fmdg_internal.cuh"
 #include "fmdg_turi.cuh"
 
@@ -72,12 +76,29 @@ __device__ __forceinline__ bool group_sum(int key, double (&v)[NV])
     return lane == leader;
 }
 
+// fixed-point scales of the per-cell sums (powers of two: v * scale is exact)
+constexpr double FX_MASS = 17592186044416.0;   // 2^44
+constexpr double FX_MOM = 1099511627776.0;     // 2^40
+constexpr double FX_KIN = 68719476736.0;       // 2^36
+constexpr double FX_LIMIT = 4.0e18;            // |v * scale| below 2^62: room for the sums
+
+__device__ __forceinline__ void add_fixed(Dyn *dyn, long long *dst, double v, double scale)
+{
+    const double q = v * scale;
+    if (!(fabs(q) < FX_LIMIT))
+    {
+        atomic_or_err(dyn, FMDG_ERRBIT_INTERNAL);
+        return;
+    }
+    atomicAdd(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__double2ll_rn(q));
+}
+
 __global__ void k_turi_clear(DTuri t)
 {
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < t.ncells; c += gridDim.x * blockDim.x)
     {
-        for (int k = 0; k < 5; k++) t.acc[5 * c + k] = 0.0;
-        t.tacc[c] = 0.0;
+        for (int k = 0; k < 5; k++) t.acc[5 * c + k] = 0;
+        t.tacc[c] = 0;
     }
 }
 
@@ -104,7 +125,11 @@ __global__ void k_turi_pass_a(Geo g, DTuri t, double dt)
     }
     if (bad) atomic_or_err(dyn, FMDG_ERRBIT_TTM);
     if (group_sum<5>(key, v) && key >= 0)
-        for (int k = 0; k < 5; k++) atomicAdd(&t.acc[5 * key + k], v[k]);
+    {
+        add_fixed(dyn, &t.acc[5 * key], v[0], FX_MASS);
+        for (int d = 0; d < 3; d++) add_fixed(dyn, &t.acc[5 * key + 1 + d], v[1 + d], FX_MOM);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&t.acc[5 * key + 4]), (unsigned long long)v[4]);
+    }
 }
 
 // vcm, mass, number (src/turi.c:1163-1171 for the interior cells)
@@ -113,9 +138,9 @@ __global__ void k_turi_finish_a(Geo g, DTuri t, double dt)
     if (!turi_window(t, g.dyn->time, dt)) return;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < t.ncells; c += gridDim.x * blockDim.x)
     {
-        const double m = t.acc[5 * c];
+        const double m = (double)t.acc[5 * c] / FX_MASS;
         t.mass[c] = m;
-        for (int d = 0; d < 3; d++) t.vcm[3 * c + d] = t.acc[5 * c + 1 + d] / m;
+        for (int d = 0; d < 3; d++) t.vcm[3 * c + d] = ((double)t.acc[5 * c + 1 + d] / FX_MOM) / m;
         t.num[c] = (unsigned)t.acc[5 * c + 4];
     }
 }
@@ -141,14 +166,14 @@ __global__ void k_turi_pass_b(Geo g, DTuri t, double dt)
         for (int d = 0; d < 3; d++) vt[d] = S.v[(size_t)d * cap + i] - t.vcm[3 * key + d];
         v[0] = m * (vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]);
     }
-    if (group_sum<1>(key, v) && key >= 0) atomicAdd(&t.tacc[key], v[0]);
+    if (group_sum<1>(key, v) && key >= 0) add_fixed(dyn, &t.tacc[key], v[0], FX_KIN);
 }
 
 __global__ void k_turi_finish_b(Geo g, DTuri t, double dt)
 {
     if (!turi_window(t, g.dyn->time, dt)) return;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < t.ncells; c += gridDim.x * blockDim.x)
-        t.Ti[c] = t.tacc[c] / (3.0 * K_BOLTZMANN_D * t.num[c]);
+        t.Ti[c] = ((double)t.tacc[c] / FX_KIN) / (3.0 * K_BOLTZMANN_D * t.num[c]);
 }
 
 // natural spline on arbitrary knots with the reference's bisection

@@ -25,8 +25,8 @@ struct DTuri
     int ttm;              // 1 when a TTM solver is attached
     double tcellh[3], inv_tcellh[3], tcell_volume;
     double starttime, stoptime;
-    double *acc;          // 5 per cell: sum m, sum m v (3), count
-    double *tacc;         // sum m |v - vcm|^2
+    long long *acc;       // 5 per cell, 64-bit fixed point: sum m, sum m v (3); count (integer)
+    long long *tacc;      // sum m |v - vcm|^2, 64-bit fixed point
     double *mass, *vcm, *Ti;
     unsigned *num;
     double *Te, *Te2, *xi, *Ke, *Ce, *Gc, *srcz;

@@ -569,6 +569,7 @@ void _fmdh_thermo_from_device(fmd_t *md)
     for (int d = 0; d < 3; d++) md->GroupMomentum[d] = th.momentum[d];
     md->GroupParticlesNum = (unsigned)th.count;
     md->GroupPotentialEnergy = th.potential;
+    md->GroupVirial = th.virial;
     md->thermo_pending = false;
 }
 

@@ -123,6 +123,7 @@ struct _fmd
     double DesiredTemperature, BerendsenThermostatParam;
     bool KineticEnergyUpdated;
     double GroupTemperature, GroupKineticEnergy, GroupPotentialEnergy;
+    double GroupVirial;    /* pair virial of the last force evaluation (no reference counterpart) */
     double GroupMomentum[3];
     unsigned GroupParticlesNum;
     bool thermo_pending;      /* device thermo record newer than the cache */

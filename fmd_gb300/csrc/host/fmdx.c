@@ -64,6 +64,14 @@ double fmdx_potential_energy(fmd_t *md)
     return md->GroupPotentialEnergy;
 }
 
+/* pair virial sum r_ij . F_ij of the last force evaluation (eV; no
+   counterpart in the reference) */
+double fmdx_virial(fmd_t *md)
+{
+    if (md->thermo_pending) _fmdh_thermo_from_device(md);
+    return md->GroupVirial;
+}
+
 int fmdx_time_iteration(fmd_t *md) { return md->time_iteration; }
 
 fmdg_sys_t *fmdx_device(fmd_t *md) { return md->dev; }

@@ -32,7 +32,7 @@ class Pair(C.Structure):
 
 class Thermo(C.Structure):
     _fields_ = [("kinetic", C.c_double), ("temperature", C.c_double), ("momentum", C.c_double * 3),
-                ("potential", C.c_double), ("count", C.c_double), ("pad", C.c_double)]
+                ("potential", C.c_double), ("count", C.c_double), ("virial", C.c_double)]
 
 
 class JobDesc(C.Structure):

@@ -65,7 +65,12 @@ typedef struct
 } fmdg_pair_t;
 
 /* Thermodynamic reductions of the active group (src/integrators.c:78-92,
-   src/matter.c:31-68) plus the last potential energy (src/lj.c:89). */
+   src/matter.c:31-68) plus the last potential energy (src/lj.c:89) and
+   pair virial.  The virial has no live counterpart in the reference (its
+   only one, src/misc.c:66-82, is unused and sums x . F, wrong under
+   periodic images): here it is the pair form over the same pairs and pair
+   forces as the energy, sum over pairs of r_ij . F_ij (eV), so that
+   P V = N k_B T + virial / 3. */
 typedef struct
 {
     double kinetic;        /* 0.5 * sum m v^2                        */
@@ -73,7 +78,7 @@ typedef struct
     double momentum[3];    /* sum m v (internal units)               */
     double potential;      /* pair + embedding energy                */
     double count;          /* atoms in the active group              */
-    double pad;
+    double virial;         /* sum over pairs r_ij . F_ij (last force evaluation) */
 } fmdg_thermo_t;
 
 /* --- lifetime -------------------------------------------------------- */

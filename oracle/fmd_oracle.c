@@ -519,6 +519,7 @@ typedef struct
     double *F;      /* 3 per atom, flat index */
     double *va;
     double pe;
+    double vir;     /* pair virial sum r_ij . F_ij (no reference counterpart on the hot path) */
 } acc_t;
 
 static void flat_starts(oracle_sys_t *o)
@@ -634,6 +635,12 @@ static void pair_update(oracle_sys_t *o, acc_t *a, int pass, ocell_t *c1, int i1
         a->F[3 * g1 + d] += mag3[d];
         a->F[3 * g2 + d] -= mag3[d];
     }
+    /* pair virial r_12 . F_12, F_12 = mag3 the force on atom 1 (the
+       reference's only virial, src/misc.c:66-82, is unused and sums x . F,
+       which is wrong under periodic images; this is the pair form over the
+       same pairs and forces as src/lj.h:26-58, src/morse.h:26-58,
+       src/eam.h:177-228) */
+    a->vir += rv[0] * mag3[0] + rv[1] * mag3[1] + rv[2] * mag3[2];
 }
 
 /* half-shell sweep (src/lj.c:36-87): cell c, atoms i1, the 13 upper
@@ -668,20 +675,23 @@ static void sweep_cell(oracle_sys_t *o, acc_t *a, int pass, int c, int group)
     }
 }
 
-static double run_pass(oracle_sys_t *o, int pass, int group, double *F, double *va)
+static double run_pass(oracle_sys_t *o, int pass, int group, double *F, double *va, double *vir)
 {
     const int n = o->start[o->ncell];
     const int nt = o->nthreads;
     double pe = 0.0;
+    *vir = 0.0;
     if (nt <= 1)
     {
-        acc_t a = {F, va, 0.0};
+        acc_t a = {F, va, 0.0, 0.0};
         for (int c = 0; c < o->ncell; c++) sweep_cell(o, &a, pass, c, group);
+        *vir = a.vir;
         return a.pe;
     }
     double *bufF = (double *)calloc((size_t)nt * 3 * n + 1, sizeof(double));
     double *bufV = (double *)calloc((size_t)nt * n + 1, sizeof(double));
     double *pes = (double *)calloc(nt, sizeof(double));
+    double *virs = (double *)calloc(nt, sizeof(double));
 #pragma omp parallel num_threads(nt)
     {
 #ifdef _OPENMP
@@ -689,10 +699,11 @@ static double run_pass(oracle_sys_t *o, int pass, int group, double *F, double *
 #else
         const int t = 0;
 #endif
-        acc_t a = {bufF + (size_t)t * 3 * n, bufV + (size_t)t * n, 0.0};
+        acc_t a = {bufF + (size_t)t * 3 * n, bufV + (size_t)t * n, 0.0, 0.0};
 #pragma omp for schedule(dynamic, 16)
         for (int c = 0; c < o->ncell; c++) sweep_cell(o, &a, pass, c, group);
         pes[t] = a.pe;
+        virs[t] = a.vir;
 #pragma omp for schedule(static)
         for (int g = 0; g < n; g++)
         {
@@ -703,8 +714,12 @@ static double run_pass(oracle_sys_t *o, int pass, int group, double *F, double *
             }
         }
     }
-    for (int q = 0; q < nt; q++) pe += pes[q];
-    free(bufF); free(bufV); free(pes);
+    for (int q = 0; q < nt; q++)
+    {
+        pe += pes[q];
+        *vir += virs[q];
+    }
+    free(bufF); free(bufV); free(pes); free(virs);
     return pe;
 }
 
@@ -720,7 +735,8 @@ int oracle_compute_forces(oracle_sys_t *o, int group)
     {
         /* pass 1: host densities, then F'(rho) and the embedding energy
            (src/eam.c:160-223) */
-        run_pass(o, 1, group, F, va);
+        double unused;
+        run_pass(o, 1, group, F, va, &unused);
         for (int c = 0; c < o->ncell; c++)
         {
             ocell_t *cl = icell(o, c);
@@ -744,7 +760,8 @@ int oracle_compute_forces(oracle_sys_t *o, int group)
             }
         }
     }
-    const double pe = run_pass(o, 0, group, F, va);
+    double vir = 0.0;
+    const double pe = run_pass(o, 0, group, F, va, &vir);
     for (int c = 0; c < o->ncell; c++)
     {
         ocell_t *cl = icell(o, c);
@@ -752,6 +769,7 @@ int oracle_compute_forces(oracle_sys_t *o, int group)
             memcpy(cl->F + 3 * i, F + 3 * (o->start[c] + i), 3 * sizeof(double));
     }
     o->th.potential = pe + emb;
+    o->th.virial = vir;
     free(F);
     free(va);
     return 0;

@@ -36,7 +36,9 @@ typedef struct
 
 typedef struct
 {
-    double kinetic, temperature, momentum[3], potential, count, pad;
+    /* virial: pair virial sum over pairs r_ij . F_ij of the last force
+       evaluation (pressure P V = N k T + virial / 3) */
+    double kinetic, temperature, momentum[3], potential, count, virial;
 } oracle_thermo_t;
 
 oracle_sys_t *oracle_create(void);

@@ -22,7 +22,7 @@ class PairT(C.Structure):
 
 class ThermoT(C.Structure):
     _fields_ = [("kinetic", C.c_double), ("temperature", C.c_double), ("momentum", C.c_double * 3),
-                ("potential", C.c_double), ("count", C.c_double), ("pad", C.c_double)]
+                ("potential", C.c_double), ("count", C.c_double), ("virial", C.c_double)]
 
 
 def _ptr(a):
@@ -138,6 +138,7 @@ class Oracle:
         th = ThermoT()
         self.L.oracle_get_thermo(self.o, C.byref(th))
         out["pe"] = th.potential
+        out["virial"] = th.virial
         return out
 
     def set_state(self, x=None, v=None):

@@ -71,6 +71,20 @@ def _ttm_state():
     return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def _cu01_state():
+    x, v = workloads.fcc_state(8, 8, 8, 3.615, 300.0, MASS["Cu"], seed=51, disp=0.04)
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
+LP_CU01 = 3.6316    # lattice parameter of the reference's type-2 TTM example (examples/04_ttm2.c:92)
+
+
+def _ttm_cu_state():
+    x, v = workloads.fcc_state(5, 5, 30, LP_CU01, 303.0, MASS["Cu"], seed=52, origin=(0.0, 0.0, 5 * LP_CU01),
+                               disp=0.03)
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def _custom_state():
     x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
     v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
@@ -122,6 +136,21 @@ CASES = {
                         run=("integrate", -1, 0.002), steps=20, every=10,
                         turi=dict(cat=0, dims=(2, 2, 3),
                                   fields=["TEMPERATURE", "NUMBER_DENSITY", "VCM", "MASS"])),
+    # the reference's own data files (examples/data): the Mishin copper setfl
+    # (as examples/02_collision.c:78 loads it) and the type-2 TTM tables of
+    # examples/04_ttm2.c:116-160 (Ce_Cu.dat, G_Cu.dat, its Zhigilei K,
+    # timestep ratio, activation fraction and laser; a shorter slab and an
+    # earlier pulse so a short run crosses it)
+    "eam_cu01": dict(box=(28.92, 28.92, 28.92), pbc=(1, 1, 1), names=["Cu"],
+                     pots=[("eam_file", 0, 0, "Cu01.eam.alloy")], state=_cu01_state,
+                     run=("integrate", -1, 0.001), steps=60, every=10, data=("Cu01.eam.alloy",)),
+    "ttm2_cu": dict(box=(5 * LP_CU01, 5 * LP_CU01, 40 * LP_CU01), pbc=(1, 1, 0), names=["Cu"],
+                    pots=[("eam_file", 0, 0, "Cu01.eam.alloy")], state=_ttm_cu_state,
+                    run=("integrate", -1, 0.002), steps=30, every=10,
+                    data=("Cu01.eam.alloy", "Ce_Cu.dat", "G_Cu.dat"),
+                    turi=dict(cat=2, dims=(1, 1, 20), zhigilei=(1.57e6, 2.66e6, 2.41e11), Te=303.0, ratio=200,
+                              frac=0.1, tables=("Ce_Cu.dat", "G_Cu.dat"),
+                              laser=(2e4, 0.85, 0.02e-12, 100e-15, 14e-9))),
     "hybrid": dict(box=(40.0, 30.0, 30.0), pbc=(1, 1, 1), names=["Cu", "Ar"],
                    pots=[("eam_analytic", 0, 0), ("lj", 1, 1, 3.4, 0.0104, 8.5),
                          ("lj", 0, 1, 2.87, 0.0652, 7.175)], state=_hybrid_state,
@@ -129,12 +158,30 @@ CASES = {
 }
 
 
-def setup(lib: api.Lib, name: str, workdir: str, state: dict | None = None):
+def write_data(workdir: str, data: dict):
+    """Write data files (name -> bytes) into the work folder."""
+    for fname, raw in data.items():
+        with open(os.path.join(workdir, fname), "wb") as f:
+            f.write(bytes(raw))
+
+
+def golden_data(g: dict) -> dict:
+    """The data files a golden .npz recorded (keys data:<file name>)."""
+    return {k[5:]: np.asarray(v, np.uint8).tobytes() for k, v in g.items() if k.startswith("data:")}
+
+
+def setup(lib: api.Lib, name: str, workdir: str, state: dict | None = None, data: dict | None = None):
     """Create an FMD instance for case `name` through the fmd.h API and load
-    its seeded state.  Returns (md, state)."""
+    its seeded state.  `data`: the case's data files (name -> bytes), written
+    into workdir first.  Returns (md, state)."""
     case = CASES[name]
     if state is None:
         state = case["state"]()
+    if data:
+        write_data(workdir, data)
+    for fname in case.get("data", ()):
+        if not os.path.exists(os.path.join(workdir, fname)):
+            raise FileNotFoundError(f"case {name} needs the data file {fname}")
     md = C.c_void_p(lib.fmd_create())
     lib.fmd_io_setShowErrorMessages(md, False)
     lib.fmd_box_setSubdomains(md, 1, 1, 1)
@@ -151,6 +198,9 @@ def setup(lib: api.Lib, name: str, workdir: str, state: dict | None = None):
             if not os.path.exists(path):
                 workloads.write_analytic_eam(path)
             pot = lib.fmd_pot_eam_alloy_load(md, path.encode())
+            lib.fmd_pot_apply(md, p[1], p[2], pot)
+        elif p[0] == "eam_file":
+            pot = lib.fmd_pot_eam_alloy_load(md, os.path.join(workdir, p[3]).encode())
             lib.fmd_pot_apply(md, p[1], p[2], pot)
     spath = os.path.join(workdir, name + ".stt")
     api.write_state(spath, 0.0, case["box"], case["pbc"], state["names"], state["kind"],
@@ -179,7 +229,10 @@ def setup_turi(lib, md, tu, workdir):
         lib._fmd_ttm_setHeatConductivity_constant1(md, h, tu["K"])
         lib._fmd_ttm_setCouplingFactor_constant1(md, h, tu["G"])
     else:
-        pc, pg = write_ttm_tables(workdir)
+        if "tables" in tu:
+            pc, pg = (os.path.join(workdir, f) for f in tu["tables"])
+        else:
+            pc, pg = write_ttm_tables(workdir)
         lib._fmd_ttm_setHeatCapacity_file(md, h, pc.encode())
         v, A, B = tu["zhigilei"]
         lib._fmd_ttm_setHeatConductivity_zhigilei(md, h, api.HeatConductivityZhigilei(v, A, B))

@@ -8,7 +8,10 @@ Run from the repository root in a container that has the reference sources:
 The reference is compiled unmodified as a single-rank CPU library
 (oracle/_ref/libfmdref.so) and driven through its own fmd.h API with the
 cases of tests/cases.py; white-box dumps come from oracle/ref_probe.c.
-Outputs: tests/golden/<case>.npz and tests/golden/bin_<case>.npz.
+Outputs: tests/golden/<case>.npz and tests/golden/bin_<case>.npz.  Cases
+that load the reference's example data files (examples/data: the Mishin
+copper setfl, the type-2 TTM tables) record those files' bytes in their .npz
+(keys data:<file name>), so the tests run without a reference checkout.
 """
 from __future__ import annotations
 
@@ -28,11 +31,14 @@ from fmd_gb300 import api  # noqa: E402
 import cases  # noqa: E402
 
 REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libfmdref.so")
+# the reference's example data files (examples/data), read from its checkout
+REF_DATA = os.path.join(os.environ.get("FMD_REFERENCE", "/root/reference"), "examples", "data")
 
 
 def golden_case(lib, name, work):
     case = cases.CASES[name]
-    md, st = cases.setup(lib, name, work)
+    data = {f: open(os.path.join(REF_DATA, f), "rb").read() for f in case.get("data", ())}
+    md, st = cases.setup(lib, name, work, data=data)
     grp, dt = case["run"][1], case["run"][2]
     rec = cases.Recorder(lib)
     if "turi" in case:
@@ -51,6 +57,8 @@ def golden_case(lib, name, work):
                s1_pe=np.array(d1["pe"]), thermo=np.array(rec.rows),
                errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2),
                time_iteration=np.array(lib.wb("time_iteration")(md) if lib.has("oref_time_iteration") else -1))
+    for f, raw in data.items():       # recorded so the tests need no reference checkout
+        out["data:" + f] = np.frombuffer(raw, dtype=np.uint8)
     if "turi" in case:
         ev = [(t, tu, f) for (t, tu, f, _) in rec.fields]
         out["field_events"] = np.array(ev, dtype=np.float64).reshape(-1, 3)
@@ -134,19 +142,59 @@ def golden_io(lib, name, work):
     print("io", name, {k: len(v) for k, v in files.items()})
 
 
+ARGON_C = os.path.join(os.path.dirname(HERE), "c", "argon_relink.c")
+ARGON_C_DURATION = 0.4
+
+
+def argon_c_state(path):
+    """The seeded initial state of the C relink program (FCC argon 10^3
+    cells, 100 K)."""
+    from fmd_gb300 import workloads
+    x, v = workloads.fcc_state(10, 10, 10, 5.26, 100.0, 39.948, seed=61, disp=0.05)
+    n = len(x)
+    api.write_state(path, 0.0, (52.6,) * 3, (1, 1, 1), ["Ar"], np.zeros(n, np.uint32), np.zeros(n, np.int32), x, v)
+
+
+def golden_argon_c(work):
+    """tests/c/argon_relink.c compiled unchanged against the reference's own
+    fmd.h and linked with the reference library: its printed series and the
+    files it writes."""
+    import subprocess
+    ref_inc = os.path.join(os.environ.get("FMD_REFERENCE", "/root/reference"), "src")
+    exe = os.path.join(work, "argon_ref.x")
+    subprocess.run(["gcc", "-std=c11", "-O2", "-Werror=implicit-function-declaration", ARGON_C, "-I" + ref_inc,
+                    REF_LIB, "-Wl,-rpath," + os.path.dirname(REF_LIB), "-o", exe], check=True)
+    st = os.path.join(work, "state0.stt")
+    argon_c_state(st)
+    out = os.path.join(work, "out") + "/"
+    os.makedirs(out)
+    r = subprocess.run([exe, st, out, repr(ARGON_C_DURATION)], check=True, capture_output=True, text=True)
+    files = {f: open(os.path.join(out, f), "rb").read() for f in sorted(os.listdir(out))}
+    rec = {"stdout": np.frombuffer(r.stdout.encode(), np.uint8),
+           "state0": np.frombuffer(open(st, "rb").read(), np.uint8),
+           "files": np.array(sorted(files))}
+    for f, raw in files.items():
+        rec["file:" + f] = np.frombuffer(raw, np.uint8)
+    np.savez_compressed(os.path.join(HERE, "argon_c.npz"), **rec)
+    print("argon_c", r.stdout.count("tick"), "ticks", sorted(files))
+
+
 def main():
     names = sys.argv[1:] or list(cases.CASES)
     if len(names) > 1 or not sys.argv[1:]:
         # one process per case: the reference's fmd_free reads the instance
         # after freeing it (src/misc.c:650-660), so instances are not reused
         import subprocess
-        for name in names + ([] if sys.argv[1:] else ["bin_lj", "bin_morse_open", "io_lj_small", "io_hybrid"]):
+        for name in names + ([] if sys.argv[1:] else ["bin_lj", "bin_morse_open", "io_lj_small", "io_hybrid",
+                                                        "argon_c"]):
             subprocess.run([sys.executable, os.path.abspath(__file__), name], check=True)
         return
     lib = api.Lib(REF_LIB, prefix="oref_")
     with tempfile.TemporaryDirectory() as work:
         for name in names:
-            if name.startswith("bin_"):
+            if name == "argon_c":
+                golden_argon_c(work)
+            elif name.startswith("bin_"):
                 golden_binning(lib, name[4:], work)
             elif name.startswith("io_"):
                 golden_io(lib, name[3:], work)

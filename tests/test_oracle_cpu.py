@@ -24,11 +24,15 @@ def oracle_for_case(name, g, work, threads=1):
     kinds = [(n, cases.MASS[n]) for n in case["names"]]
     pots = []
     setfl = None
+    cases.write_data(work, cases.golden_data(g))
     for p in case["pots"]:
         if p[0] == "eam_analytic":
             setfl = os.path.join(work, "analytic.eam.alloy")
             if not os.path.exists(setfl):
                 workloads.write_analytic_eam(setfl)
+            pots.append(("eam", p[1], p[2]))
+        elif p[0] == "eam_file":
+            setfl = os.path.join(work, p[3])
             pots.append(("eam", p[1], p[2]))
         else:
             pots.append(p)
@@ -72,7 +76,7 @@ def test_oracle_matches_reference(name):
     fmax = np.abs(g["s0_F"]).max()
     assert np.abs(d0["F"] - g["s0_F"]).max() <= 1e-12 * fmax
     assert abs(d0["pe"] - float(g["s0_pe"])) <= 1e-12 * abs(float(g["s0_pe"]))
-    if name in ("eam", "hybrid"):
+    if name in ("eam", "hybrid", "eam_cu01"):
         assert np.abs(d0["vaream"] - g["s0_vaream"]).max() <= 1e-12 * np.abs(g["s0_vaream"]).max()
     gt = g["thermo"]
     assert rows.shape[0] == gt.shape[0]

@@ -40,7 +40,7 @@ def run_case(lib, name):
     case = cases.CASES[name]
     st = dict(names=case["names"], kind=g["state_kind"], group=g["state_group"], x=g["state_x"], v=g["state_v"])
     with tempfile.TemporaryDirectory() as work:
-        md, _ = cases.setup(lib, name, work, state=st)
+        md, _ = cases.setup(lib, name, work, state=st, data=cases.golden_data(g))
         grp, dt = case["run"][1], case["run"][2]
         rec = cases.Recorder(lib)
         if "turi" in case:
@@ -66,7 +66,7 @@ def test_case_parity(gpu_lib, name):
     err = np.abs(d0["F"] - g["s0_F"]).max() / fmax
     assert err <= FORCE_TOL, f"step-0 force error {err:.3e}"
     assert abs(d0["pe"] - float(g["s0_pe"])) <= FORCE_TOL * max(1.0, abs(float(g["s0_pe"]))), (d0["pe"], g["s0_pe"])
-    if name in ("eam", "hybrid"):
+    if name in ("eam", "hybrid", "eam_cu01", "ttm2_cu"):
         vmax = np.abs(g["s0_vaream"]).max()
         assert np.abs(d0["vaream"] - g["s0_vaream"]).max() <= FORCE_TOL * vmax
     # trajectory
@@ -130,7 +130,7 @@ MIXED_FORCE_TOL = 1e-5   # mixed mode: max |dF| / max |F| against the binary64 r
 MIXED_PE_TOL = 1e-6      # relative potential energy
 
 
-@pytest.mark.parametrize("name", ["lj", "lj_small", "morse_open", "eam", "hybrid"])
+@pytest.mark.parametrize("name", ["lj", "lj_small", "morse_open", "eam", "hybrid", "eam_cu01"])
 def test_mixed_precision_forces(gpu_lib, name):
     """binary32 pair arithmetic with binary64 sums stays within the stated
     bound of the reference's binary64 forces and energy at step 0."""
@@ -140,7 +140,7 @@ def test_mixed_precision_forces(gpu_lib, name):
     st = dict(names=case["names"], kind=g["state_kind"], group=g["state_group"], x=g["state_x"], v=g["state_v"])
     gpu_lib.L.fmdx_set_precision.argtypes = [C.c_void_p, C.c_int]
     with tempfile.TemporaryDirectory() as work:
-        md, _ = cases.setup(gpu_lib, name, work, state=st)
+        md, _ = cases.setup(gpu_lib, name, work, state=st, data=cases.golden_data(g))
         gpu_lib.L.fmdx_set_precision(md, 1)
         gpu_lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
         d0 = gpu_lib.dump(md)

@@ -3,8 +3,10 @@ reference's golden vectors by tests/test_oracle_cpu.py) at sizes beyond the
 golden fixtures, and size-independent checks at the full benchmark size.
 
 binary64 tolerances: forces <= 1e-10 of max |F|, energies <= 1e-10
-relative, positions after 30 steps <= 1e-9 A, cell order exact.
-mixed mode: forces <= 1e-5 of max |F|, energy <= 1e-6 relative.
+relative, pair virial <= 1e-10 of max(|W|, |PE|), positions after 30
+steps <= 1e-9 A, cell order exact.
+mixed mode: forces <= 1e-5 of max |F|, energy <= 1e-6 relative, pair
+virial <= 1e-6 of max(|W|, |PE|).
 """
 import ctypes as C
 import os
@@ -125,6 +127,9 @@ def test_gpu_vs_oracle_fp64(gpu_lib, name):
         fmax = np.abs(r0["F"]).max()
         assert np.abs(g0["F"] - r0["F"]).max() <= 1e-10 * fmax
         assert abs(g0["pe"] - r0["pe"]) <= 1e-10 * abs(r0["pe"])
+        # pair virial (relative to the larger of |W| and |PE|: W of a
+        # near-equilibrium crystal can be small)
+        assert abs(g0["virial"] - r0["virial"]) <= 1e-10 * max(abs(r0["virial"]), abs(r0["pe"]))
         nsteps = 30
         gpu_lib.fmd_dync_integrate(md, -1, (nsteps - 0.5) * dt, dt)
         g1 = gpu_lib.dump(md)
@@ -151,6 +156,7 @@ def test_gpu_vs_oracle_mixed(gpu_lib, name):
         err = np.abs(g0["F"] - r0["F"]).max() / np.abs(r0["F"]).max()
         assert err <= 1e-5, err
         assert abs(g0["pe"] - r0["pe"]) <= 1e-6 * abs(r0["pe"])
+        assert abs(g0["virial"] - r0["virial"]) <= 1e-6 * max(abs(r0["virial"]), abs(r0["pe"]))
         gpu_lib.fmd_free(md)
         o.close()
 

@@ -7,7 +7,8 @@
 * pack vs the single-system path (different list, different summation
   order): binary64 positions within 1e-9 A and forces within 1e-9 of max |F|
   after 25 steps; mixed within 1e-6 A and 5e-5;
-* pack vs the binary64 oracle at the pack's own final positions: forces
+* pack vs the binary64 oracle at the pack's own final positions: forces,
+  and the last thermo record's energy and pair virial
   within 1e-10 (binary64) and 1e-5 (mixed) of max |F|.
 
 Hybrid jobs ("cuar": EAM copper beside Lennard-Jones argon, copper-argon
@@ -112,7 +113,8 @@ def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
     srv.set_skin(0.3)
     jid = srv.submit(pot, x, v, l, 40, precision=precision, keep_state=True, kind=kind)
     srv.drain()
-    assert srv.result(jid).state == 2
+    r = srv.result(jid)
+    assert r.state == 2
     xp, vp, Fp, ids = srv.state(jid, len(x))
     srv.close()
     nc, cellh, order, counts = serve.host_binning3(xp, l, serve.job_rc(pot))
@@ -136,6 +138,12 @@ def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
     tol = 1e-10 if precision == serve.PREC_FP64 else 1e-5
     err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
     assert err <= tol, err
+    # the job's last thermo record (formed by the packed force kernel on its
+    # last step, at these positions): energy and pair virial
+    tol_e = 1e-10 if precision == serve.PREC_FP64 else 1e-6
+    assert abs(r.last.potential - d["pe"]) <= tol_e * abs(d["pe"]), (r.last.potential, d["pe"])
+    scale = max(abs(d["virial"]), abs(d["pe"]))
+    assert abs(r.last.virial - d["virial"]) <= tol_e * scale, (r.last.virial, d["virial"])
 
 
 def test_alone_vs_mix(L, eam):
