@@ -12,8 +12,11 @@ Workloads
                     counts and arrival times scaled together) for quick runs.
   eam256k           one 256 000-atom EAM system (FCC 40x40x40, a = 3.615 A,
                     300 K, seed 2, dt 1 fs), the single-system drop-in path.
+  ttm               the laser-heated EAM slab with the 1-D two-temperature
+                    model (800 000 atoms, 50 electron cells), the fmd.h path;
+                    roofline of the HBM-bound turi field passes.
 
-    python bench.py [--steps K] [--warmup W] [--workload served|eam256k]
+    python bench.py [--steps K] [--warmup W] [--workload served|eam256k|ttm]
     python bench.py --impl reference     # CPU oracle port on the host cores
 
 served: `value` = every job of the stream resident in HBM at once, K fleet
@@ -367,6 +370,177 @@ def run_ours(args):
     return out
 
 
+# ---------------------------------------------------------------- TTM slab
+TTM = dict(cells=(40, 50, 100), a=3.615, T=300.0, seed=4, mass=63.546, dt=0.001, vacuum=20.0,
+           dims=(1, 1, 50), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100, frac=0.1,
+           laser=(500.0, 0.0, 1e-12, 100e-15, 15e-9), t_start=0.95)
+# algorithmic HBM bytes per atom-step of the memory-bound TTM kernels
+# (binary64 state): the two turi field passes each read x, v (48 B) and the
+# kind (4 B) of every atom (src/turi.c:959-1335); the kick-drift reads x, v,
+# F and the kind, writes x, v (124 B, src/integrators.c:129-179)
+TTM_FIELD_BYTES = 2 * (48 + 4)
+SE_KICK_BYTES = 72 + 4 + 48
+
+
+def ttm_config():
+    w = TTM
+    return {"workload": "laser-heated EAM copper slab with a 1-D two-temperature model: FCC %dx%dx%d cells "
+                        "(%d atoms; a = 3.615 A, 300 K seed 4), periodic x, y, %.0f A vacuum on both free z "
+                        "faces, analytic EAM; electron grid of %d cells along z, gamma 96.6 J/m^3K^2, K 400 W/mK, "
+                        "G 1e17 W/m^3K, 100 explicit substeps of 0.01 fs per 1 fs step; 500 J/m^2 Gaussian pulse "
+                        "(FWHM 100 fs at 1 ps, 15 nm depth); timed steps start at %.2f ps (through the pulse)"
+                        % (*w["cells"], 4 * int(np.prod(w["cells"])), w["vacuum"], w["dims"][2], w["t_start"]),
+            "atoms": 4 * int(np.prod(w["cells"])), "precision": "mixed forces, binary64 electron temperatures",
+            "step": "one symplectic-Euler step: kick-drift, cell refresh, turi field passes, TTM solver, "
+                    "neighbour list, EAM density, pair forces + friction term",
+            "l2": "working set (~0.5 GB) larger than L2, no flush needed"}
+
+
+def make_ttm_system(lib, api, work):
+    from fmd_gb300 import workloads
+    w = TTM
+    nx, ny, nz = w["cells"]
+    a = w["a"]
+    box = (nx * a, ny * a, nz * a + 2 * w["vacuum"])
+    x, v = workloads.fcc_state(nx, ny, nz, a, w["T"], w["mass"], seed=w["seed"], origin=(0.0, 0.0, w["vacuum"]))
+    n = len(x)
+    md = C.c_void_p(lib.fmd_create())
+    lib.fmd_io_setShowErrorMessages(md, True)
+    lib.fmd_box_setSubdomains(md, 1, 1, 1)
+    lib.fmd_box_setSize(md, *box)
+    lib.fmd_box_setPBC(md, True, True, False)
+    api.set_atom_kinds(lib, md, ["Cu"], [w["mass"]])
+    path = workloads.write_analytic_eam(os.path.join(work, "analytic.eam.alloy"))
+    pot = lib.fmd_pot_eam_alloy_load(md, path.encode())
+    lib.fmd_pot_apply(md, 0, 0, pot)
+    spath = os.path.join(work, "slab.stt")
+    api.write_state(spath, 0.0, box, (1, 1, 0), ["Cu"], np.zeros(n, np.uint32), np.zeros(n, np.int32), x, v)
+    lib.fmd_io_loadState(md, spath.encode(), False)
+    lib.L.fmdx_set_precision.argtypes = [C.c_void_p, C.c_int]
+    lib.L.fmdx_set_precision(md, 1)
+    lib.fmd_matt_getTemperature(md)          # the TTM set-up reads the group's atom count
+    h = lib.fmd_turi_add(md, 1, *w["dims"], 0.0, -1.0)
+    lib._fmd_ttm_setHeatCapacity_linear(md, h, api.HeatCapacityLinear(w["gamma"]))
+    lib._fmd_ttm_setHeatConductivity_constant1(md, h, w["K"])
+    lib._fmd_ttm_setCouplingFactor_constant1(md, h, w["G"])
+    lib.fmd_ttm_setElectronTemperature(md, h, w["Te"])
+    lib.fmd_ttm_setTimestepRatio(md, h, w["ratio"])
+    lib.fmd_ttm_setCellActivationFraction(md, h, w["frac"])
+    lib._fmd_ttm_setLaserSource_gaussian(md, h, api.LaserGaussian(*w["laser"]))
+    return md, h, n
+
+
+def run_ttm(args):
+    import fmd_gb300
+    from fmd_gb300 import api
+    lib = fmd_gb300.load()
+    L = lib.L
+    L.fmdx_device.restype = C.c_void_p
+    L.fmdx_device.argtypes = [C.c_void_p]
+    for name, at in [("fmdg_se_steps", [C.c_void_p, C.c_int, C.c_double, C.c_int]),
+                     ("fmdg_timer_start", [C.c_void_p]), ("fmdg_timer_stop", [C.c_void_p, C.POINTER(C.c_float)]),
+                     ("fmdg_sync", [C.c_void_p]), ("fmdg_set_profiling", [C.c_void_p, C.c_int]),
+                     ("fmdg_get_profile", [C.c_void_p, C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+                     ("fmdg_measure_fma_peak", [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
+                     ("fmdg_launch_count", [C.c_void_p, C.POINTER(C.c_longlong)]),
+                     ("fmdg_get_errors", [C.c_void_p, C.POINTER(C.c_uint), C.c_int])]:
+        getattr(L, name).argtypes = at
+        getattr(L, name).restype = C.c_int
+    w = TTM
+    dt = w["dt"]
+
+    def ck(rc, what):
+        if rc != 0:
+            L.fmdg_last_error.restype = C.c_char_p
+            raise RuntimeError(f"{what}: {L.fmdg_last_error().decode()}")
+
+    with tempfile.TemporaryDirectory() as work:
+        md, h, natoms = make_ttm_system(lib, api, work)
+        # to the window before the pulse (warm-up included)
+        n_pre = max(1, int(round(args.ttm_start / dt)) - args.steps)
+        lib.fmd_dync_integrate(md, -1, (n_pre - 0.5) * dt, dt)
+        field_te = lib.fmd_field_find(md, h, api.FMD_FIELD_TTM_TE)
+        dev = C.c_void_p(L.fmdx_device(md))
+        # e2e: the fmd.h call one step at a time, the electron temperature
+        # field read back after every step
+        arr = C.c_void_p()
+        dims = (C.c_uint * 3)()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            lib.fmd_dync_integrate(md, -1, 0.5 * dt, dt)
+            a3s = lib.fmd_field_getArray(md, h, field_te, C.byref(arr), dims)
+            lib.fmd_array3s_free(a3s)
+        t1 = time.perf_counter()
+        e2e_value = natoms * args.steps / (t1 - t0)
+        te_bytes = 8 * dims[0] * dims[1] * dims[2]
+        # device time: K steps replayed from the captured step graph
+        ck(L.fmdg_se_steps(dev, args.warmup, dt, -1), "warm-up")
+        ck(L.fmdg_sync(dev), "sync")
+        sampler = ClockSampler()
+        sampler.start()
+        lc0, lc1 = C.c_longlong(0), C.c_longlong(0)
+        L.fmdg_launch_count(dev, C.byref(lc0))
+        ms = C.c_float(0.0)
+        ck(L.fmdg_timer_start(dev), "timer")
+        ck(L.fmdg_se_steps(dev, args.steps, dt, -1), "steps")
+        ck(L.fmdg_timer_stop(dev, C.byref(ms)), "timer")
+        L.fmdg_launch_count(dev, C.byref(lc1))
+        clocks = sampler.stop()
+        ck(L.fmdg_set_profiling(dev, 1), "prof")
+        nprof = max(3, min(10, args.steps))
+        ck(L.fmdg_se_steps(dev, nprof, dt, -1), "profile")
+        phases = {}
+        for ph in ("bin", "turi", "ttm", "force"):
+            pms, pn = C.c_float(0.0), C.c_int(0)
+            L.fmdg_get_profile(dev, ph.encode(), C.byref(pms), C.byref(pn))
+            phases[ph] = pms.value / max(pn.value, 1)
+        ck(L.fmdg_set_profiling(dev, 0), "prof")
+        peak32 = C.c_double(0)
+        ck(L.fmdg_measure_fma_peak(dev, 0, C.byref(peak32)), "peak")
+        errs = C.c_uint(0)
+        L.fmdg_get_errors(dev, C.byref(errs), 0)
+        ttm = lib.ttm_1d(md)
+        lib.fmd_free(md)
+    te = np.asarray(ttm["Te"])
+    peak, src = hbm_peak_gbs()
+    ms_per_step = ms.value / args.steps
+    field_gbs = TTM_FIELD_BYTES * natoms / (phases["turi"] * 1e-3) / 1e9
+    kick_gbs = SE_KICK_BYTES * natoms / (phases["bin"] * 1e-3) / 1e9
+    force_tf = natoms * (FLOP_DENSITY + FLOP_FORCE) / (phases["force"] * 1e-3) / 1e12
+    cores = os.cpu_count() or 1
+    if args.skip_cpu:
+        cpu_value, cpu_steps = None, 0
+    else:
+        cpu_value, cpu_steps = cpu_port_run(cores)
+    return {
+        "metric": "atom-steps/s", "value": natoms / (ms_per_step * 1e-3), "unit": "atom-steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-compute/f64-accumulate (Te f64)", "data": "synthetic",
+        "config": dict(ttm_config(), t_start_ps=args.ttm_start), "gpu_launches": int(lc1.value - lc0.value),
+        "phases_ms": phases,
+        "roofline": {"bound": "hbm", "kernel": "k_turi_pass_a + k_turi_pass_b (turi field passes; with the "
+                                              "cell clears and finishes of the phase)",
+                     "achieved": field_gbs, "peak": peak, "unit": "GB/s", "frac": field_gbs / peak,
+                     "peak_source": src, "algorithmic_bytes_per_atom": TTM_FIELD_BYTES, "traffic": None},
+        "hbm_kernels": {"kick_drift_refresh": {"achieved_gbs": kick_gbs, "frac": kick_gbs / peak,
+                                               "algorithmic_bytes_per_atom": SE_KICK_BYTES,
+                                               "note": "k_bin_classify (kick-drift) + the reference-order "
+                                                       "refresh kernels; bytes of the kick-drift only"},
+                        "ttm_solver_ms": phases["ttm"]},
+        "roofline_force": {"bound": "fp32-issue", "kernel": "neighbour list + EAM density + pair forces",
+                           "achieved": force_tf, "peak": peak32.value, "unit": "TFLOP/s",
+                           "frac": force_tf / peak32.value},
+        "clocks": clocks, "device_errors": errs.value,
+        "te_max_k": float(te[te >= 0].max()) if (te >= 0).any() else None,
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": te_bytes,
+                "how": "fmd_dync_integrate one step at a time through the fmd.h API (the state stays resident), "
+                       "the electron-temperature field array read back after every step; wall clock"},
+        "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cpu_steps} velocity-Verlet steps of the 256000-atom EAM system (the "
+                                   "oracle port has no TTM solver: the EAM part of the step)"},
+    }
+
+
 # ---------------------------------------------------------------- served stream
 METRIC = "atom-steps/s on 1 GB300, batched-served vs plain at ≤1e-5 force err; p50/p99"
 SERVED_JOBS = 2048
@@ -684,10 +858,13 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": spent / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
-                                  "300 K, dt 1 fs, NVE", "atoms": natoms},
+           "config": (ttm_config() if args.workload == "ttm" else
+                      {"workload": "EAM FCC 40x40x40 (256000 atoms), analytic EAM on 10000-point splines, "
+                                   "300 K, dt 1 fs, NVE", "atoms": natoms}),
            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": cores, "kind": "port",
-                            "sample": "each step up to 10 velocity-Verlet steps of the system"},
+                            "sample": "each step up to 10 velocity-Verlet steps of the 256000-atom EAM system"
+                                      + (" (the oracle port has no TTM solver: the EAM part of the step)"
+                                         if args.workload == "ttm" else "")},
            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -700,7 +877,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline (profiling runs)")
-    ap.add_argument("--workload", default="served", choices=["served", "eam256k"])
+    ap.add_argument("--workload", default="served", choices=["served", "eam256k", "ttm"])
+    ap.add_argument("--ttm-start", type=float, default=TTM["t_start"],
+                    help="ttm: simulation time (ps) at which the timed steps start")
     ap.add_argument("--only", default="all", choices=["all", "fleet"],
                     help="served: 'fleet' times the resident fleet only (profiling runs)")
     ap.add_argument("--jobs", type=int, default=SERVED_JOBS, help="served: jobs of the stream (its first jobs)")
@@ -716,7 +895,12 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    out = run_served(args) if args.workload == "served" else run_ours(args)
+    if args.workload == "served":
+        out = run_served(args)
+    elif args.workload == "ttm":
+        out = run_ttm(args)
+    else:
+        out = run_ours(args)
     print(json.dumps(out))
 
 

@@ -715,13 +715,16 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         FMDG_CK(cudaMemcpyAsync(S.cell_of, cell_of.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
     }
     FMDG_CK(cudaMemcpyAsync(S.cell_start, start.data(), ((size_t)ncell + 1) * 4, cudaMemcpyHostToDevice, st));
-    // cell origins (c * cellh per axis, the binary64 products the kernels
-    // would form)
+    // frame origins of the cell-local binary32 coordinates: the cell centres
+    // ((c + 1/2) * cellh per axis, binary64).  Centred frames keep the
+    // coordinates within half a cell (plus the skin drift) of zero, so their
+    // binary32 rounding is half that of corner-relative ones; pair geometry
+    // only uses differences, so the choice of frame changes nothing else
     std::vector<double4_32a> corig(ncell);
     for (int c = 0; c < ncell; c++)
     {
         const int cx = c / (g.nc[1] * g.nc[2]), cy = (c / g.nc[2]) % g.nc[1], cz = c % g.nc[2];
-        corig[c] = make_double4_32a(cx * g.cellh[0], cy * g.cellh[1], cz * g.cellh[2], 0.0);
+        corig[c] = make_double4_32a((cx + 0.5) * g.cellh[0], (cy + 0.5) * g.cellh[1], (cz + 0.5) * g.cellh[2], 0.0);
     }
     FMDG_CK(cudaMemcpyAsync((void *)g.corig, corig.data(), (size_t)ncell * sizeof(double4_32a),
                             cudaMemcpyHostToDevice, st));
@@ -935,10 +938,33 @@ extern "C" int fmdg_se_steps(fmdg_sys_t *s, int nsteps, double dt, int active_gr
     if (nsteps <= 0) return FMDG_OK;
     if (s->profiling)
     {
+        // phases timed separately with events: 0 kick-drift + refresh,
+        // 4 turi field passes, 5 TTM solver, 3 neighbour list + density +
+        // pair forces (+ friction term); the launches of se_step_launches
+        // in the same order
         for (int k = 0; k < nsteps; k++)
         {
-            int rc = se_step_launches(s, dt, active_group);
+            FMDG_CK(cudaEventRecord(s->pev[0], s->stream));
+            int rc = fmdg_launch_refresh(s, FMDG_REFRESH_SE, dt, active_group, 0);
             if (rc) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[1], s->stream));
+            for (int q = 0; q < s->nturi; q++)
+                if ((rc = fmdg_launch_turi_fields(s, q, dt))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[2], s->stream));
+            for (int q = 0; q < s->nturi; q++)
+                if ((rc = fmdg_launch_ttm_solve(s, q, dt))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[3], s->stream));
+            if ((rc = fmdg_launch_forces(s, active_group, 0, dt, 0, 1.0, 0.0))) return rc;
+            FMDG_CK(cudaEventRecord(s->pev[4], s->stream));
+            FMDG_CK(cudaEventSynchronize(s->pev[4]));
+            const int phase[4] = {0, 4, 5, 3};
+            for (int q = 0; q < 4; q++)
+            {
+                float ms = 0.0f;
+                FMDG_CK(cudaEventElapsedTime(&ms, s->pev[q], s->pev[q + 1]));
+                s->prof_ms[phase[q]] += ms;
+                s->prof_n[phase[q]] += 1;
+            }
         }
         return FMDG_OK;
     }
@@ -1243,8 +1269,8 @@ extern "C" int fmdg_set_profiling(fmdg_sys_t *s, int on)
 
 extern "C" int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches)
 {
-    static const char *names[5] = {"bin", "nlist", "density", "force", "turi"};
-    for (int k = 0; k < 5; k++)
+    static const char *names[6] = {"bin", "nlist", "density", "force", "turi", "ttm"};
+    for (int k = 0; k < 6; k++)
         if (strcmp(name, names[k]) == 0)
         {
             *ms = s->prof_ms[k];

@@ -110,8 +110,11 @@ __device__ __forceinline__ Geom64 geom64(const Geo &g, const Side &S, const doub
 template <bool DF>
 __device__ __forceinline__ float3 geom32(const SmemPotT<DF> &sp, float4 xi, float4 xj, int code)
 {
-    const float4 o = sp.off[code];
-    return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
+    // the offset's binary32 part, then its remainder (the binary32 rounding
+    // of (ox, oy, oz) * cellh would shift every pair across a cell face by
+    // up to half an ulp of the cell width)
+    const float4 o = sp.off[code], ol = sp.offl[code];
+    return make_float3(xi.x - xj.x - o.x - ol.x, xi.y - xj.y - o.y - ol.y, xi.z - xj.z - o.z - ol.z);
 }
 
 // is r2 (binary32) within rc2?  Near the cutoff the decision is taken in

@@ -68,7 +68,7 @@ struct Geo   // passed by value to kernels
     int pbc[3];
     double l[3], cellh[3], inv_cellh[3];
     float l_f[3], inv_cellh_f[3];   // binary32 copies (fast paths with binary64 fallbacks)
-    const double4_32a *corig;       // per cell: origin (cx, cy, cz) * cellh in binary64
+    const double4_32a *corig;       // per cell: frame origin, the centre (cx + 1/2, cy + 1/2, cz + 1/2) * cellh, binary64
     Side side[2];
     double *F, *vaream;
     float *fpf;        // binary32 copy of F'(rho) (mixed-precision EAM force pass)
@@ -161,8 +161,8 @@ struct fmdg_sys
     cudaEvent_t ev0, ev1;
     cudaEvent_t pev[6];
     bool profiling;
-    float prof_ms[5];
-    int prof_n[5];
+    float prof_ms[6];
+    int prof_n[6];
     long long launches;
     // captured multi-step graph
     cudaGraphExec_t graph;
@@ -293,6 +293,9 @@ int fmdg_set_error(const char *msg);
 // kernel launch wrappers (defined in their translation units)
 int fmdg_launch_refresh(fmdg_sys_t *s, int mode, double dt, int group, int thermostat);
 int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt);
+// the two halves of fmdg_launch_turi: the field passes, then the TTM solver
+int fmdg_launch_turi_fields(fmdg_sys_t *s, int k, double dt);
+int fmdg_launch_ttm_solve(fmdg_sys_t *s, int k, double dt);
 int fmdg_launch_forces(fmdg_sys_t *s, int group, int finish, double dt, int thermostat, double tau, double T0);
 int fmdg_launch_density(fmdg_sys_t *s, int group);
 int fmdg_launch_nlist(fmdg_sys_t *s);

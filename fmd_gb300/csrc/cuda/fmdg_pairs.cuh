@@ -29,7 +29,7 @@ struct SmemPotT
     double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
     float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
-    float4 offl[DF ? 27 : 1];   // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl in double-float
+    float4 offl[27];    // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl = the binary64 offset
 };
 
 // one 32-byte table row (two float4) in a single 256-bit load; p must be
@@ -72,7 +72,7 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
     {
         const float ox = small_int_f(c / 9 - 1), oy = small_int_f((c / 3) % 3 - 1), oz = small_int_f(c % 3 - 1);
         sp.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], 0.f);
-        if (DF) sp.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
+        sp.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
     }
     __syncthreads();
 }

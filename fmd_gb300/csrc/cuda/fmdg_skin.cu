@@ -51,11 +51,15 @@ namespace {
 constexpr int SLOT_BITS = 25;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
-template <bool DF>   // DF: binary64 mode (the remainders); else a placeholder
+// Image offsets of the stencil codes in shared memory.  off = (ox, oy, oz)
+// * binary32 cellh is exact in binary32 (|o| <= 2); the remainder offl =
+// (ox, oy, oz) * (cellh - binary32 cellh) completes it to the binary64
+// offset (double-float in binary64 mode, one more subtraction in binary32).
+template <bool DF>   // DF: binary64 mode (layout kept apart so binary32 kernels stay lean)
 struct SkinOffT
 {
     float4 off[125];    // image offset of each stencil code, binary32; .w: the code's bits
-    float4 offl[DF ? 125 : 1];   // the remainders (binary64 offset - off): off + offl in double-float
+    float4 offl[125];   // the remainders (binary64 offset - off)
 };
 
 template <bool DF>
@@ -66,14 +70,29 @@ __device__ __forceinline__ void load_offsets(const Geo &g, SkinOffT<DF> &so)
     {
         const float ox = small_int_f(c / (W * W) - R), oy = small_int_f((c / W) % W - R), oz = small_int_f(c % W - R);
         so.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], __int_as_float(c));
-        if (DF) so.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
+        so.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
     }
     __syncthreads();
 }
 
+// binary32 pair vector x_i - x_j - offset without the offset's remainder
+// (list-radius prefilters)
 __device__ __forceinline__ float3 rv_of(float4 xi, float4 xj, float4 o)
 {
     return make_float3(xi.x - xj.x - o.x, xi.y - xj.y - o.y, xi.z - xj.z - o.z);
+}
+
+// binary32 pair vector of a list entry with the offset's remainder: the
+// binary32 rounding of (ox, oy, oz) * cellh would otherwise shift every
+// pair across a cell face by up to half an ulp of the cell width
+// (5e-7 A), as much as the rounding of the coordinates themselves.  o.w
+// holds the stencil code (an overflow-fallback occurrence: -1 - code).
+template <bool DF>
+__device__ __forceinline__ float3 rv_lo(const SkinOffT<DF> &so, float4 xi, float4 xj, float4 o)
+{
+    const int code = __float_as_int(o.w);
+    const float4 ol = so.offl[code ^ (code >> 31)];
+    return make_float3(xi.x - xj.x - o.x - ol.x, xi.y - xj.y - o.y - ol.y, xi.z - xj.z - o.z - ol.z);
 }
 
 // binary64 minimum-image geometry rv = x_a - (x_b + shift)
@@ -105,8 +124,8 @@ __device__ __forceinline__ bool within_cut_skin(const Geo &g, int ta, int tb, fl
     return geom64_mi(g, g.xd[ta], g.xd[tb]).r2 < rc2;
 }
 
-// Gap along one axis between a point at u inside its cell [0, h) and the
-// cell at offset o (0 for the cell itself).
+// Gap along one axis between a point at u inside its cell box [0, h) and
+// the cell at offset o (0 for the cell itself).
 __device__ __forceinline__ float axis_gap(int o, float u, float h)
 {
     return o > 0 ? fmaxf(0.f, (float)o * h - u) : (o < 0 ? fmaxf(0.f, u + (float)(-o - 1) * h) : 0.f);
@@ -137,16 +156,18 @@ __device__ __forceinline__ bool within_cut_df_mi(const Geo &g, int t, int js, df
 // code, in a fixed order: f(code, c).  On a periodic axis shorter than the
 // stencil a cell recurs with another image (at most one image of a pair
 // lies within the list radius).  xi: the atom's binary32 position relative
-// to cell ci; a cell whose box lies farther than the list radius from xi
-// (plus 1e-4 relative) holds no candidate and is skipped.
+// to the centre of cell ci; a cell whose box lies farther than the list
+// radius from xi (plus 1e-4 relative) holds no candidate and is skipped.
 template <typename F>
 __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, float4 xi, F &&f)
 {
     const int R = g.srad, W = 2 * R + 1;
     const float lim2 = g.rskin2 * 1.0001f;
+    // position inside the cell box [0, h) (up to the drift since the build)
+    const float ux = xi.x + 0.5f * g.cellh_f[0], uy = xi.y + 0.5f * g.cellh_f[1], uz = xi.z + 0.5f * g.cellh_f[2];
     for (int ox = -R; ox <= R; ox++)
     {
-        const float gx = axis_gap(ox, xi.x, g.cellh_f[0]);
+        const float gx = axis_gap(ox, ux, g.cellh_f[0]);
         if (gx * gx > lim2) continue;
         int cx = ci.x + ox;
         if (cx < 0 || cx >= g.nc[0])
@@ -156,7 +177,7 @@ __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, 
         }
         for (int oy = -R; oy <= R; oy++)
         {
-            const float gy = axis_gap(oy, xi.y, g.cellh_f[1]);
+            const float gy = axis_gap(oy, uy, g.cellh_f[1]);
             if (gx * gx + gy * gy > lim2) continue;
             int cy = ci.y + oy;
             if (cy < 0 || cy >= g.nc[1])
@@ -166,7 +187,7 @@ __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, 
             }
             for (int oz = -R; oz <= R; oz++)
             {
-                const float gz = axis_gap(oz, xi.z, g.cellh_f[2]);
+                const float gz = axis_gap(oz, uz, g.cellh_f[2]);
                 if (gx * gx + gy * gy + gz * gz > lim2) continue;
                 int cz = ci.z + oz;
                 if (cz < 0 || cz >= g.nc[2])
@@ -643,7 +664,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 int npend = 0, pend = 0;
                 float pr2 = 0.f;
                 for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                    const float3 rv = rv_of(xi, xj, o);
+                    const float3 rv = rv_lo(so, xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     const bool near = fabsf(r2 - rc2f) <= band;
                     const bool in = (r2 < rc2f) && !near;
@@ -669,7 +690,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 else if (npend > 1)
                 {
                     for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                        const float3 rv = rv_of(xi, xj, o);
+                        const float3 rv = rv_lo(so, xi, xj, o);
                         const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                         if (!(fabsf(r2 - rc2f) <= band)) return;
                         if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
@@ -690,7 +711,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                     if (group >= 0 && g.gslot[js] != group) return;
                     const int pidx = ki * nk + __float_as_int(xj.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
-                    const float3 rv = rv_of(xi, xj, o);
+                    const float3 rv = rv_lo(so, xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     if ((!HYBRID || pp.cat == FMDG_POT_EAM) &&
                         within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
@@ -861,7 +882,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                     {
                         const float band = 1e-4f * rc2f;
                         for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                            const float3 rv = rv_of(xi, xj, o);
+                            const float3 rv = rv_lo(so, xi, xj, o);
                             const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                             bool in = r2 < rc2f;
                             if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
@@ -897,7 +918,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         int npend = 0, pend = 0;
                         float3 prv = make_float3(0.f, 0.f, 0.f);
                         for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                            const float3 rv = rv_of(xi, xj, o);
+                            const float3 rv = rv_lo(so, xi, xj, o);
                             const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                             const bool near = fabsf(r2 - rc2f) <= band;
                             const bool in = (r2 < rc2f) && !near;
@@ -933,7 +954,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         else if (npend > 1)
                         {
                             for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                                const float3 rv = rv_of(xi, xj, o);
+                                const float3 rv = rv_lo(so, xi, xj, o);
                                 const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                                 if (!(fabsf(r2 - rc2f) <= band)) return;
                                 if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
@@ -972,7 +993,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                     const int pidx = ki * nk + __float_as_int(xj.w);
                     const fmdg_pair_t &pp = sp.pairs[pidx];
                     const int cat = (CAT == CAT_HYBRID) ? pp.cat : CAT;
-                    const float3 rv = rv_of(xi, xj, o);
+                    const float3 rv = rv_lo(so, xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     if (cat == FMDG_POT_LJ)
                     {

@@ -309,7 +309,7 @@ __global__ void k_ttm_solve(Geo g, DTuri t, double dt)
 
 } // namespace
 
-int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt)
+int fmdg_launch_turi_fields(fmdg_sys_t *s, int k, double dt)
 {
     DTuri &t = s->turi[k];
     cudaStream_t st = s->stream;
@@ -321,11 +321,22 @@ int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt)
     k_turi_pass_b<<<nba, 256, 0, st>>>(s->g, t, dt);
     k_turi_finish_b<<<nbc, 256, 0, st>>>(s->g, t, dt);
     s->launches += 5;
-    if (t.ttm)
-    {
-        k_ttm_solve<<<1, 128, 0, st>>>(s->g, t, dt);
-        s->launches++;
-    }
     FMDG_CK(cudaGetLastError());
     return FMDG_OK;
+}
+
+int fmdg_launch_ttm_solve(fmdg_sys_t *s, int k, double dt)
+{
+    DTuri &t = s->turi[k];
+    if (!t.ttm) return FMDG_OK;
+    k_ttm_solve<<<1, 128, 0, s->stream>>>(s->g, t, dt);
+    s->launches++;
+    FMDG_CK(cudaGetLastError());
+    return FMDG_OK;
+}
+
+int fmdg_launch_turi(fmdg_sys_t *s, int k, double dt)
+{
+    int rc = fmdg_launch_turi_fields(s, k, dt);
+    return rc ? rc : fmdg_launch_ttm_solve(s, k, dt);
 }

@@ -28,7 +28,12 @@ EAM_RC = 5.5
 EAM_TAPER_START = 5.0     # cubic switching function on [5.0, 5.5] A for phi and f
 EAM_NR = 10000
 EAM_NRHO = 10000
-EAM_DRHO = 0.004          # rho grid 0 .. 39.996 (lattice value ~16)
+# rho grid 0 .. 119.988.  The lattice value at a = 3.615 A is ~16, but this
+# potential has no equilibrium near 3.615 A: its energy per atom falls
+# monotonically as the lattice contracts, down to a ~ 2.7 A (rho ~ 49), so a
+# periodic crystal at 3.615 A is under ~ -74 GPa and collapses locally after
+# ~10^3 steps, densities reaching 45-50; the table covers them with margin
+EAM_DRHO = 0.012
 
 
 def _taper(r):
@@ -56,7 +61,7 @@ def write_analytic_eam(path, element="Cu", mass=63.546, lattice=3.615):
 
     r grid: Nr = 10000 points, dr = 5.5/9999 (the loader pads Nr by 2 and
     needs (Nr+1)*dr > cutoff, src/eam.c:412-415); rho grid: Nrho = 10000,
-    drho = 0.004.  The pair block stores r*phi(r) as the format requires.
+    drho = 0.012.  The pair block stores r*phi(r) as the format requires.
     """
     f, phi, F = analytic_eam_functions()
     dr = EAM_RC / (EAM_NR - 1)

@@ -245,10 +245,13 @@ int fmdg_change_group(fmdg_sys_t *s, int old_group, int new_group);
 int fmdg_sync(fmdg_sys_t *s);
 int fmdg_timer_start(fmdg_sys_t *s);
 int fmdg_timer_stop(fmdg_sys_t *s, float *ms);
-/* with profiling on, fmdg_vv_steps launches each phase between CUDA events
-   (no graph) and accumulates its device time: phases "bin" (start step +
-   refresh), "density" (EAM pass 1 + embedding), "force" (pair forces +
-   finish step), "turi" (field updates); ms summed over steps */
+/* with profiling on, fmdg_vv_steps and fmdg_se_steps launch each phase
+   between CUDA events (no graph) and accumulate its device time: phases
+   "bin" (start step / kick-drift + refresh), "nlist", "density" (EAM pass 1
+   + embedding), "force" (pair forces + finish step; fmdg_se_steps: list,
+   density and forces together), "turi" (field passes), "ttm" (fmdg_se_steps:
+   the TTM electron solver; fmdg_vv_steps counts it under "turi"); ms summed
+   over steps */
 int fmdg_set_profiling(fmdg_sys_t *s, int on);
 int fmdg_get_profile(fmdg_sys_t *s, const char *name, float *ms, int *launches);
 int fmdg_launch_count(fmdg_sys_t *s, long long *count);

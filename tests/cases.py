@@ -85,6 +85,11 @@ def _ttm_cu_state():
     return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def _ttm_slab_state():
+    x, v = workloads.fcc_state(4, 4, 100, 3.615, 300.0, MASS["Cu"], seed=4, origin=(0.0, 0.0, 20.0))
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def _custom_state():
     x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
     v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
@@ -151,6 +156,17 @@ CASES = {
                     turi=dict(cat=2, dims=(1, 1, 20), zhigilei=(1.57e6, 2.66e6, 2.41e11), Te=303.0, ratio=200,
                               frac=0.1, tables=("Ce_Cu.dat", "G_Cu.dat"),
                               laser=(2e4, 0.85, 0.02e-12, 100e-15, 14e-9))),
+    # the laser-heated EAM slab of the TTM configuration (100 FCC cells along
+    # z with 20 A of vacuum on either side, free z faces, a 50-cell 1-D
+    # electron grid, gamma 96.6, K 400, G 1e17, 100 substeps of 0.01 fs,
+    # 500 J/m^2 Gaussian pulse of 100 fs, 15 nm depth) on a 4 x 4 cell
+    # cross-section instead of 20 x 20 (6400 atoms); the pulse at 0.06 ps,
+    # crossed by the 200-step run
+    "ttm_slab": dict(box=(4 * 3.615, 4 * 3.615, 100 * 3.615 + 40.0), pbc=(1, 1, 0), names=["Cu"],
+                     pots=[("eam_analytic", 0, 0)], state=_ttm_slab_state, run=("integrate", -1, 0.001),
+                     steps=200, every=40,
+                     turi=dict(cat=1, dims=(1, 1, 50), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100,
+                               frac=0.1, laser=(500.0, 0.0, 0.06e-12, 100e-15, 15e-9))),
     "hybrid": dict(box=(40.0, 30.0, 30.0), pbc=(1, 1, 1), names=["Cu", "Ar"],
                    pots=[("eam_analytic", 0, 0), ("lj", 1, 1, 3.4, 0.0104, 8.5),
                          ("lj", 0, 1, 2.87, 0.0652, 7.175)], state=_hybrid_state,

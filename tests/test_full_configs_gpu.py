@@ -5,6 +5,8 @@ API on the GPU.
   then 10 000 NVE steps at 2 fs; trajectories diverge chaotically, so the
   NVE energy drift (max |E(t) - E(0)| / |E(0)| over 20 samples) is compared:
   binary64 and mixed precision within 2x the oracle's drift (+1e-7).
+* EAM copper, 256 000 atoms: step-0 forces of both precisions against the
+  oracle, and the 5000-step NVE drift of each within 2x the oracle's.
 * Morse collision, 512 000-atom slab + a 20 A projectile sphere at 2 km/s,
   periodic x, y, 100 A vacuum in z: step-0 forces against the oracle
   (binary64 1e-10, mixed 1e-5 of max |F|), then 200 steps: no atom lost
@@ -79,6 +81,59 @@ def test_lj_argon_nve_drift(gpu_lib):
     bound = 2.0 * drifts["oracle"] + 1e-7
     assert drifts[0] <= bound, drifts
     assert drifts[1] <= bound, drifts
+
+
+def _eam256k():
+    x, v = workloads.fcc_state(40, 40, 40, 3.615, 300.0, 63.546, seed=2)
+    return dict(box=(40 * 3.615,) * 3, pbc=(1, 1, 1), kinds=[("Cu", 63.546)], pots=[("eam", 0, 0)], x=x, v=v,
+                kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), dt=0.001)
+
+
+def test_eam256k_full_size(gpu_lib):
+    """The 256 000-atom EAM configuration (FCC 40^3, 300 K seed 2, dt 1 fs):
+    step-0 forces of both precisions at identical positions against the
+    binary64 oracle (binary64 1e-10, mixed 1e-5 of max |F|; the mixed-vs-
+    binary64 error printed), then 5000 NVE steps in each precision: the
+    energy drift (max |E(t) - E(0)| / |E(0)| over samples every 250 steps)
+    within 2x the oracle's drift on the same protocol (+1e-7).  The
+    oracle's 5000-step run takes minutes of host time, so its drift is
+    recorded in tests/golden/cfg1_drift.json (make_cfg1_drift.py)."""
+    import json
+    lib = gpu_lib
+    spec = _eam256k()
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cfg1_drift.json")
+    if not os.path.exists(path):
+        pytest.skip("the oracle's drift record (make_cfg1_drift.py) is absent")
+    ref = json.load(open(path))
+    forces, drifts, errs = {}, {}, {}
+    with tempfile.TemporaryDirectory() as work:
+        for prec in (0, 1):
+            md, o = build_both(lib, spec, work, precision=prec)
+            lib.fmd_dync_integrate(md, -1, 0.0, 0.001)
+            forces[prec] = lib.dump(md)
+            if prec == 0:
+                o.set_threads(os.cpu_count() or 1)
+                o.forces(-1)
+                r0 = o.dump()
+                e0_oracle = r0["pe"] + o.thermo(-1).kinetic
+            o.close()
+            es = [_energy(lib, md)]
+            for _ in range(ref["steps"] // ref["every"]):
+                lib.fmd_dync_integrate(md, -1, (ref["every"] - 0.5) * 0.001, 0.001)
+                es.append(_energy(lib, md))
+            drifts[prec] = _drift(es)
+            lib.fmd_free(md)
+    fmax = np.abs(r0["F"]).max()
+    for prec in (0, 1):
+        np.testing.assert_array_equal(forces[prec]["id"], r0["id"])
+        errs[prec] = float(np.abs(forces[prec]["F"] - r0["F"]).max() / fmax)
+    errs["mixed_vs_binary64"] = float(np.abs(forces[1]["F"] - forces[0]["F"]).max() / np.abs(forces[0]["F"]).max())
+    print("EAM 256k: force errors", errs, "drifts", drifts, "oracle drift", ref["drift"])
+    assert errs[0] <= 1e-10 and errs[1] <= 1e-5 and errs["mixed_vs_binary64"] <= 1e-5, errs
+    # the same initial total energy as the oracle's recorded run
+    assert abs(ref["energies"][0] - e0_oracle) <= 1e-10 * abs(e0_oracle)
+    bound = 2.0 * ref["drift"] + 1e-7
+    assert drifts[0] <= bound and drifts[1] <= bound, (drifts, ref["drift"])
 
 
 def _collision(seed=3):

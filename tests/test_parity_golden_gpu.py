@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import cases
+from fmd_gb300 import api
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
@@ -82,26 +83,50 @@ def test_case_parity(gpu_lib, name):
     assert np.abs(d1["x"] - g["s1_x"]).max() <= POS_TOL
 
 
+TTM_TOL = 1e-10         # electron temperatures (every event) and every field at the first update
+FIELD_TOL = 1e-10       # atomic fields after the first update (measured <= 1.5e-11 over 30-200 steps)
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    ok = np.isfinite(b)
+    assert np.array_equal(ok, np.isfinite(a))
+    if not ok.any():
+        return 0.0
+    return float(np.abs(a[ok] - b[ok]).max() / max(np.abs(b[ok]).max(), 1e-300))
+
+
 @pytest.mark.parametrize("name", [n for n in cases.CASES if "turi" in cases.CASES[n]])
 def test_turi_fields(gpu_lib, name):
     """Field-update events (order, turi, field, time) and every field array
-    seen by the handler match the reference; the final TTM state (Te, xi, Ti,
-    number of atoms per cell) matches on the interior cells."""
+    seen by the handler match the reference to 1e-10 relative (measured:
+    Te ~1e-16, atomic fields <= 1.5e-11 over 30-200 steps); the final TTM
+    state: number of atoms per cell exact, Te, xi and Ti to 1e-10."""
     g, d0, d1, rec = run_case(gpu_lib, name)
     ev = np.array([(t, tu, f) for (t, tu, f, _) in rec.fields]).reshape(-1, 3)
     np.testing.assert_array_equal(ev[:, 1:], g["field_events"][:, 1:])
     np.testing.assert_allclose(ev[:, 0], g["field_events"][:, 0], rtol=0, atol=1e-12)
-    for k, (_, _, _, vals) in enumerate(rec.fields):
+    t_first = ev[0, 0]
+    worst = {}
+    for k, (t, _, f, vals) in enumerate(rec.fields):
         key = "field_%03d" % k
-        if key in g:
-            np.testing.assert_allclose(vals, g[key], rtol=1e-9, atol=1e-9, equal_nan=True, err_msg=key)
+        if key not in g:
+            continue
+        cat = rec.field_cats.get(int(f))
+        e = _rel(vals, g[key])
+        tag = ("first" if t == t_first else "later", cat)
+        worst[tag] = max(worst.get(tag, 0.0), e)
+        tol = TTM_TOL if (t == t_first or cat == api.FMD_FIELD_TTM_TE) else FIELD_TOL
+        assert e <= tol, (key, t, cat, e)
+    print(name, "max relative field errors (event, category):", worst)
     if "ttm_Te" in g:
         lo, hi = 1, len(g["ttm_Te"]) - 1
         t = rec.ttm
         np.testing.assert_array_equal(t["num"][lo:hi], g["ttm_num"][lo:hi])
-        for q in ("Te", "xi", "Ti"):
-            np.testing.assert_allclose(t[q][lo:hi], g["ttm_" + q][lo:hi], rtol=1e-9, atol=1e-9, equal_nan=True,
-                                       err_msg=q)
+        errs = {q: _rel(t[q][lo:hi], g["ttm_" + q][lo:hi]) for q in ("Te", "xi", "Ti")}
+        print(name, "final TTM state relative errors:", errs)
+        assert errs["Te"] <= TTM_TOL, errs
+        assert errs["xi"] <= FIELD_TOL and errs["Ti"] <= FIELD_TOL, errs
 
 
 @pytest.mark.parametrize("name", ["lj", "morse_open"])
@@ -150,3 +175,39 @@ def test_mixed_precision_forces(gpu_lib, name):
     assert err <= MIXED_FORCE_TOL, f"mixed force error {err:.3e}"
     pe_err = abs(d0["pe"] - float(g["s0_pe"])) / abs(float(g["s0_pe"]))
     assert pe_err <= MIXED_PE_TOL, f"mixed PE error {pe_err:.3e}"
+
+
+MIXED_TE_TOL = 1e-9     # mixed mode: electron temperatures against the binary64 reference (measured 2e-11)
+
+
+def test_ttm_mixed_te_error(gpu_lib):
+    """The laser-heated slab (200 steps through the pulse) in mixed
+    precision: binary32 pair arithmetic moves the atoms slightly differently
+    from the reference, the lattice temperature that couples to the
+    electrons follows, and the electron temperatures stay within 1e-6 of
+    the reference's binary64 values at every event and at the end."""
+    import ctypes as C
+    name = "ttm_slab"
+    g = load_golden(name)
+    case = cases.CASES[name]
+    st = dict(names=case["names"], kind=g["state_kind"], group=g["state_group"], x=g["state_x"], v=g["state_v"])
+    gpu_lib.L.fmdx_set_precision.argtypes = [C.c_void_p, C.c_int]
+    with tempfile.TemporaryDirectory() as work:
+        md, _ = cases.setup(gpu_lib, name, work, state=st)
+        gpu_lib.L.fmdx_set_precision(md, 1)
+        rec = cases.Recorder(gpu_lib)
+        rec.record_fields(md, case["turi"]["_handle"])
+        gpu_lib.fmd_setEventHandler(md, None, rec.cb)
+        gpu_lib.fmd_dync_integrate(md, -1, 0.0, case["run"][2])
+        cases.run(gpu_lib, name, md, rec)
+        ttm = gpu_lib.ttm_1d(md)
+        gpu_lib.fmd_free(md)
+    worst = 0.0
+    for k, (t, _, f, vals) in enumerate(rec.fields):
+        key = "field_%03d" % k
+        if key in g and rec.field_cats.get(int(f)) == api.FMD_FIELD_TTM_TE:
+            worst = max(worst, _rel(vals, g[key]))
+    lo, hi = 1, len(g["ttm_Te"]) - 1
+    final = _rel(ttm["Te"][lo:hi], g["ttm_Te"][lo:hi])
+    print("mixed-mode electron temperature error: events %.3e, final %.3e" % (worst, final))
+    assert worst <= MIXED_TE_TOL and final <= MIXED_TE_TOL, (worst, final)

@@ -6,7 +6,7 @@ binary64 tolerances: forces <= 1e-10 of max |F|, energies <= 1e-10
 relative, pair virial <= 1e-10 of max(|W|, |PE|), positions after 30
 steps <= 1e-9 A, cell order exact.
 mixed mode: forces <= 1e-5 of max |F|, energy <= 1e-6 relative, pair
-virial <= 1e-6 of max(|W|, |PE|).
+virial <= 1e-5 of max(|W|, |PE|).
 """
 import ctypes as C
 import os
@@ -156,7 +156,9 @@ def test_gpu_vs_oracle_mixed(gpu_lib, name):
         err = np.abs(g0["F"] - r0["F"]).max() / np.abs(r0["F"]).max()
         assert err <= 1e-5, err
         assert abs(g0["pe"] - r0["pe"]) <= 1e-6 * abs(r0["pe"])
-        assert abs(g0["virial"] - r0["virial"]) <= 1e-6 * max(abs(r0["virial"]), abs(r0["pe"]))
+        # the virial sums pair terms f r^2 that cancel like the forces do:
+        # the force bound, relative to max(|W|, |PE|)
+        assert abs(g0["virial"] - r0["virial"]) <= 1e-5 * max(abs(r0["virial"]), abs(r0["pe"]))
         gpu_lib.fmd_free(md)
         o.close()
 

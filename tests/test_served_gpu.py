@@ -139,11 +139,14 @@ def test_pack_forces_vs_oracle(L, eam, pot, ncell, precision):
     err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
     assert err <= tol, err
     # the job's last thermo record (formed by the packed force kernel on its
-    # last step, at these positions): energy and pair virial
-    tol_e = 1e-10 if precision == serve.PREC_FP64 else 1e-6
-    assert abs(r.last.potential - d["pe"]) <= tol_e * abs(d["pe"]), (r.last.potential, d["pe"])
+    # last step, at these positions): energy and pair virial, relative to
+    # max(|W|, |PE|) (a hot LJ gas has a small net energy: its pair terms
+    # cancel); binary64 1e-10, mixed 1e-6 (energy) and 1e-5 (virial, whose
+    # terms f r^2 cancel like the forces)
     scale = max(abs(d["virial"]), abs(d["pe"]))
-    assert abs(r.last.virial - d["virial"]) <= tol_e * scale, (r.last.virial, d["virial"])
+    tol_pe, tol_w = (1e-10, 1e-10) if precision == serve.PREC_FP64 else (1e-6, 1e-5)
+    assert abs(r.last.potential - d["pe"]) <= tol_pe * scale, (r.last.potential, d["pe"])
+    assert abs(r.last.virial - d["virial"]) <= tol_w * scale, (r.last.virial, d["virial"])
 
 
 def test_alone_vs_mix(L, eam):
