@@ -663,6 +663,38 @@ def plain_sample(L, eam, jobs, every=PLAIN_EVERY, nsteps=PLAIN_STEPS):
                                 "median_rel_energy_drift": float(np.median(drifts))}
 
 
+def served_force_errors(L, eam, jobs, per_pot=3, max_atoms=40000):
+    """Max relative force error of the served (packed, mixed-precision)
+    kernels against the binary64 path at identical positions: per
+    potential the coldest jobs of the stream up to max_atoms atoms (cold
+    crystals have the smallest net forces, the largest relative errors)
+    and the first job; each runs 24 packed steps, then the binary64
+    single-system path evaluates the forces at the job's final positions.
+    Returns {potential: max error}."""
+    from fmd_gb300 import serve
+    out = {}
+    for p in serve.POT_NAMES:
+        mine = [j for j in jobs if j["pot"] == p and len(j["x"]) <= max_atoms]
+        pick = sorted(mine, key=lambda j: j["T"])[:per_pot] + [next(j for j in jobs if j["pot"] == p)]
+        worst = 0.0
+        for j in pick:
+            srv = serve.Server(L, chunk_steps=8, eam=eam)
+            jid = srv.submit(p, j["x"], j["v"], j["l"], 24, precision=serve.PREC_MIXED, keep_state=True)
+            srv.drain()
+            xp, vp, Fp, _ = srv.state(jid, len(j["x"]))
+            srv.close()
+            # the binary64 forces at the same positions: Single numbers the
+            # atoms by their row in xp
+            one = serve.Single(L, p, xp, vp, j["l"], precision=serve.PREC_FP64, eam=eam)
+            _, _, F64, rows = one.state()
+            one.close()
+            Fb = np.zeros_like(F64)
+            Fb[rows] = F64
+            worst = max(worst, float(np.abs(Fp - Fb).max() / np.abs(Fb).max()))
+        out[p] = worst
+    return out
+
+
 def run_served(args):
     import fmd_gb300
     from fmd_gb300 import serve
@@ -756,20 +788,7 @@ def run_served(args):
     # --- plain: jobs one at a time, binary64 single-system path ------------
     plain_value, plain = plain_sample(L, eam, jobs)
 
-    # --- force error of the mixed path against binary64 at identical
-    # positions (a thermalised state: 20 binary64 steps), one job per potential
-    ferr = {}
-    for p in serve.POT_NAMES:
-        j = next(j for j in jobs if j["pot"] == p)
-        one = serve.Single(L, p, j["x"], j["v"], j["l"], precision=serve.PREC_FP64, eam=eam)
-        one.steps(20)
-        serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
-        F64 = one.state()[2]
-        serve.check(L, L.fmdg_set_precision(one.h, serve.PREC_MIXED), "precision")
-        serve.check(L, L.fmdg_compute_forces(one.h, -1), "forces")
-        F32 = one.state()[2]
-        one.close()
-        ferr[p] = float(np.abs(F32 - F64).max() / np.abs(F64).max())
+    ferr = served_force_errors(L, eam, jobs)
 
     cores = os.cpu_count() or 1
     if args.skip_cpu:

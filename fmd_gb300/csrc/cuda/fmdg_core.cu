@@ -252,8 +252,9 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     s->fblk = 128;
     // Verlet skin of the neighbour list (A) of mixed-precision systems;
     // FMD_SKIN=0 keeps the exact per-step stencil list
-    s->g.skin = 0.5;
-    if (const char *e = getenv("FMD_SKIN")) s->g.skin = atof(e);
+    s->skin = 0.5;
+    if (const char *e = getenv("FMD_SKIN")) s->skin = atof(e);
+    s->g.xs = s->g.inv_xs = 1.0;
     *out = s;
     return FMDG_OK;
 }
@@ -330,7 +331,8 @@ extern "C" int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, con
         if (rc) return rc;
         rc = dalloc(s, (fmdg_pair_t **)&s->g.pairs, FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
-        rc = dalloc(s, (float4 **)&s->g.pairf, FMDG_MAXK * FMDG_MAXK);
+        // the binary32 table, then the skin kernels' scaled copy (skin_params)
+        rc = dalloc(s, (float4 **)&s->g.pairf, 2 * FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
         rc = dalloc(s, (float2 **)&s->g.paird, 4 * FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
@@ -368,6 +370,54 @@ extern "C" int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table)
     FMDG_CK(cudaMemcpy((void *)s->g.pairf, pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice));
     FMDG_CK(cudaMemcpy((void *)s->g.paird, pd, sizeof(float2) * 4 * nk2, cudaMemcpyHostToDevice));
     s->g.has_eam = (s->cats >> FMDG_POT_EAM) & 1;
+    invalidate_graph(s);
+    return fmdg_skin_scale(s);
+}
+
+// The scaled frame of the skin-list binary32 coordinates (see Geo::xs):
+// xs, the scaled cell widths, the scaled skin radii and the pair
+// parameters in scaled units, each formed in binary64 and rounded once.
+// Per category (the layout of fmdg_pair_t.p): LJ {eps4, sig^2 xs^2,
+// rc^2 xs^2}, Morse {D0, alpha / xs, r0 xs, rc^2 xs^2}, EAM {rc^2 xs^2 in
+// p[2]}.
+int fmdg_skin_scale(fmdg_sys_t *s)
+{
+    Geo &g = s->g;
+    if (!s->box_set) return FMDG_OK;
+    const double xs = (g.prec == FMDG_PREC_MIXED) ? (double)(float)g.cellh[0] / g.cellh[0] : 1.0;
+    g.xs = xs;
+    g.inv_xs = 1.0 / xs;
+    for (int d = 0; d < 3; d++) g.cellh_s[d] = (float)(g.cellh[d] * xs);
+    if (s->rsk > 0.0)
+    {
+        g.rskin2 = (float)(s->rsk * xs * s->rsk * xs);
+        g.half_skin2 = (float)(0.25 * s->skin * s->skin * xs * xs);
+    }
+    const int nk2 = s->nkinds * s->nkinds;
+    if (nk2 > 0 && g.pairf)
+    {
+        float4 pf[FMDG_MAXK * FMDG_MAXK];
+        for (int k = 0; k < nk2; k++)
+        {
+            const double *p = s->h_pairs[k].p;
+            double q[4] = {p[0], p[1], p[2], p[3]};
+            if (s->h_pairs[k].cat == FMDG_POT_LJ)
+            {
+                q[1] = p[1] * xs * xs;
+                q[2] = p[2] * xs * xs;
+            }
+            else if (s->h_pairs[k].cat == FMDG_POT_MORSE)
+            {
+                q[1] = p[1] / xs;
+                q[2] = p[2] * xs;
+                q[3] = p[3] * xs * xs;
+            }
+            else
+                q[2] = p[2] * xs * xs;
+            pf[k] = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
+        }
+        FMDG_CK(cudaMemcpy((void *)skin_params(g), pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice));
+    }
     invalidate_graph(s);
     return FMDG_OK;
 }
@@ -461,7 +511,7 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
     if (((uintptr_t)g.pkf_pr | (uintptr_t)g.pkd_rho | (uintptr_t)g.pkd_phi) % 32)
         return fmdg_set_error("fmdg_set_eam: row tables not 32-byte aligned");
     invalidate_graph(s);
-    return FMDG_OK;
+    return fmdg_skin_scale(s);
 }
 
 extern "C" int fmdg_set_precision(fmdg_sys_t *s, int mode)
@@ -469,7 +519,7 @@ extern "C" int fmdg_set_precision(fmdg_sys_t *s, int mode)
     if (mode != FMDG_PREC_FP64 && mode != FMDG_PREC_MIXED) return fmdg_set_error("fmdg_set_precision: bad mode");
     s->g.prec = mode;
     invalidate_graph(s);
-    return FMDG_OK;
+    return fmdg_skin_scale(s);
 }
 
 // Neighbour-list entries per atom: 1.3x the pairs an atom of the densest
@@ -489,7 +539,7 @@ int fmdg_list_capacity(const fmdg_sys_t *s, const int *cell_count, int ncell)
         const double hmin = fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
         rc2max = hmin * hmin;
     }
-    const double rlist = sqrt(rc2max) + (s->g.skin > 0.0 ? s->g.skin : 1e-2);
+    const double rlist = sqrt(rc2max) + (s->skin > 0.0 ? s->skin : 1e-2);
     if (s->list_capacity > 0) return s->list_capacity;
     return fmdg_capacity_estimate(cell_count, ncell, g.cellh[0] * g.cellh[1] * g.cellh[2], rlist);
 }
@@ -549,7 +599,7 @@ int fmdg_set_steps_left(fmdg_sys_t *s, int steps)
 extern "C" int fmdg_set_skin(fmdg_sys_t *s, double skin)
 {
     if (!(skin >= 0.0)) return fmdg_set_error("fmdg_set_skin: negative skin");
-    s->g.skin = skin;
+    s->skin = skin;
     s->skin_set = true;
     return FMDG_OK;
 }
@@ -578,7 +628,7 @@ extern "C" int fmdg_share_eam(fmdg_sys_t *s, const fmdg_sys_t *owner)
     g.inv_dr2 = o.inv_dr2; g.inv_drho = o.inv_drho;
     s->eam_borrowed = true;
     invalidate_graph(s);
-    return FMDG_OK;
+    return fmdg_skin_scale(s);
 }
 
 extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const double *x, const double *v,
@@ -628,7 +678,6 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     for (int d3 = 0; d3 < 3; d3++)
     {
         g.cellh_f[d3] = (float)g.cellh[d3];
-        g.cellh_l[d3] = (float)(g.cellh[d3] - (double)g.cellh_f[d3]);
     }
     // a skin list needs the list radius below half of every periodic box
     // length (one image inside it) and within two cells; otherwise the
@@ -637,9 +686,9 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     // pair arithmetic costs more on the longer list than the rebuilds save:
     // EAM 256k 3.0e8 vs 3.5e8 atom-steps/s; LJ and Morse gain 7-8%)
     g.skin_on = 0;
-    if (g.skin > 0.0 && cap < (1 << 25) && (s->skin_set || g.prec == FMDG_PREC_MIXED))
+    if (s->skin > 0.0 && cap < (1 << 25) && (s->skin_set || g.prec == FMDG_PREC_MIXED))
     {
-        const double rsk = sqrt(rc2max) + g.skin;
+        const double rsk = sqrt(rc2max) + s->skin;
         bool ok = rsk <= 2.0 * fmin(g.cellh[0], fmin(g.cellh[1], g.cellh[2]));
         for (int d3 = 0; d3 < 3; d3++)
             if (g.pbc[d3] && !(g.l[d3] > 2.0 * rsk)) ok = false;
@@ -689,13 +738,13 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
         FMDG_CK(cudaMemcpyAsync(g.pos, iota.data(), (size_t)cap * 4, cudaMemcpyHostToDevice, st));
         // build cells: valid cell indexes before the first build writes them
         FMDG_CK(cudaMemsetAsync(g.cb, 0, (size_t)cap * 4, st));
-        const double rsk = sqrt(rc2max) + g.skin;
-        g.rskin2 = (float)(rsk * rsk);
-        g.half_skin2 = (float)(0.25 * g.skin * g.skin);
+        const double rsk = sqrt(rc2max) + s->skin;
+        s->rsk = rsk;
         g.srad = 1;
         for (int d3 = 0; d3 < 3; d3++)
             if (rsk > g.cellh[d3]) g.srad = 2;
     }
+    if ((rc = fmdg_skin_scale(s))) return rc;
     // host SoA staging
     std::vector<double> hx(3 * (size_t)cap, 0.0), hv(3 * (size_t)cap, 0.0);
     for (int i = 0; i < n; i++)

@@ -78,8 +78,7 @@ struct Geo   // passed by value to kernels
     int *nbr_count;    // true count (entries beyond maxnb are not stored)
     int maxnb;
     float rlist2;      // binary32 prefilter radius^2 (largest cutoff + margin)
-    float cellh_f[3];
-    float cellh_l[3];  // binary32 remainders cellh - cellh_f (cellh_f + cellh_l in double-float)
+    float cellh_f[3];  // binary32 cell widths (remainders cellh - cellh_f formed per block)
     // packed spline tables: per interval k {y_k, y_k+1, y''_k, y''_k+1}
     const double4_32a *pk_rho, *pk_phi, *pk_F;     // binary64
     const float4 *pkf_rho, *pkf_phi, *pkf_F;   // binary32 copies (mixed mode)
@@ -141,9 +140,21 @@ struct Geo   // passed by value to kernels
     float *fpb;            // by slot: F'(rho) binary32
     double *fpd;           // by slot: F'(rho) binary64
     int srad;              // stencil radius in cells of the list build
-    float rskin2;          // (largest cutoff + skin)^2
-    float half_skin2;      // (skin/2)^2: displacement that triggers a rebuild
-    double skin;
+    float rskin2;          // (largest cutoff + skin)^2, scaled units (xs)
+    float half_skin2;      // (skin/2)^2, scaled units: displacement that triggers a rebuild
+    // Scaled frame of the skin-list binary32 coordinates (xl, xb, xf4 of a
+    // skin system): x' = xs x with xs = binary32(cellh[0]) / cellh[0] in
+    // mixed precision (1 in binary64 mode).  The scaled cell width along x
+    // is then a binary32 number, so the stencil offsets o * cellh_s are
+    // exact (on every axis of a cubic grid) and a pair vector is off only
+    // by the rounding of the two coordinates.  The binary32 pair kernels
+    // work in scaled units with parameters scaled on the host
+    // (skin_params), form the real force factor, and scale each atom's
+    // force by 1/xs and its virial by 1/xs^2 in binary64; energies need no
+    // scaling.  (Binary32 xs^2 and the EAM index factor inv_dr2 / xs^2 of a
+    // scaled r^2 are formed per thread from xs.)
+    double xs, inv_xs;
+    float cellh_s[3];      // scaled cell widths, binary32 (remainders cellh xs - cellh_s formed per block)
 };
 
 struct fmdg_sys
@@ -182,7 +193,18 @@ struct fmdg_sys
     bool skin_set;                // skin chosen by the caller (any precision)
     int list_capacity;            // neighbour-list entries per atom; 0: estimated at upload
     int build_lanes;              // threads per atom of a skin-list build; 0: by size
+    double rsk;                   // skin-list radius (largest cutoff + skin), real units
+    double skin;                  // Verlet skin of the neighbour list (A), 0: exact per-step list
 };
+
+// the skin kernels' binary32 pair parameters in the scaled frame: the
+// second half of the binary32 parameter table
+__host__ __device__ inline const float4 *skin_params(const Geo &g) { return g.pairf + FMDG_MAXK * FMDG_MAXK; }
+
+// scale of the skin-path binary32 frame and the constants that follow from
+// it (Geo::xs ...); called whenever the cell grid, the precision, the pair
+// table or the EAM tables change
+int fmdg_skin_scale(fmdg_sys_t *s);
 
 // time step of the next launches and the half-kick coefficients
 // dt * 0.5 / m of every kind, in binary64 as the reference forms them

@@ -28,8 +28,9 @@ struct SmemPotT
     double mass[FMDG_MAXK];
     double hk[FMDG_MAXK];   // half kick dt * 0.5 / m of each kind (one division per kind)
     int elem[FMDG_MAXK];
-    float4 off[27];     // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
-    float4 offl[27];    // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl = the binary64 offset
+    // per-step kernels only (ONE: the skin kernels' one-kind layout has its own offsets)
+    float4 off[ONE ? 1 : 27];    // image offset of stencil code c: (ox, oy, oz) * cellh (binary32)
+    float4 offl[ONE ? 1 : 27];   // the remainders (ox, oy, oz) * (cellh - binary32 cellh): off + offl = the binary64 offset
 };
 
 // one 32-byte table row (two float4) in a single 256-bit load; p must be
@@ -51,13 +52,16 @@ __device__ __forceinline__ float small_int_f(int v) { return __int_as_float(0x4B
 // offset remainders (binary64 mode).  Everything was formed on the host
 // (no binary64 or conversion work here).
 template <bool DF, bool ONE>
-__device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
+__device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp, const float4 *pf = nullptr)
 {
+    // pf: the binary32 parameter table (default g.pairf; the skin kernels
+    // pass skin_params(g), their scaled frame)
+    if (!pf) pf = g.pairf;
     const int nk2 = ONE ? 1 : g.nkinds * g.nkinds;
     for (int k = threadIdx.x; k < nk2; k += blockDim.x)
     {
         sp.pairs[k] = g.pairs[k];
-        const float4 f = g.pairf[k];
+        const float4 f = pf[k];
         sp.pf[k][0] = f.x; sp.pf[k][1] = f.y; sp.pf[k][2] = f.z; sp.pf[k][3] = f.w;
         if (DF)
             for (int q = 0; q < 4; q++) sp.pd[k][q] = g.paird[4 * k + q];
@@ -68,11 +72,14 @@ __device__ __forceinline__ void load_pot(const Geo &g, SmemPotT<DF, ONE> &sp)
         sp.hk[k] = g.st.hk[k];
         sp.elem[k] = g.eam_elem[k];
     }
-    for (int c = threadIdx.x; c < 27; c += blockDim.x)
+    // remainders cellh - binary32 cellh (3 binary64 operations per block)
+    const float lx = (float)(g.cellh[0] - (double)g.cellh_f[0]), ly = (float)(g.cellh[1] - (double)g.cellh_f[1]),
+                lz = (float)(g.cellh[2] - (double)g.cellh_f[2]);
+    for (int c = threadIdx.x; c < (ONE ? 0 : 27); c += blockDim.x)
     {
         const float ox = small_int_f(c / 9 - 1), oy = small_int_f((c / 3) % 3 - 1), oz = small_int_f(c % 3 - 1);
         sp.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], 0.f);
-        sp.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
+        sp.offl[c] = make_float4(ox * lx, oy * ly, oz * lz, 0.f);
     }
     __syncthreads();
 }

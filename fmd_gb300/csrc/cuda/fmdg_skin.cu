@@ -51,29 +51,39 @@ namespace {
 constexpr int SLOT_BITS = 25;
 constexpr int SLOT_MASK = (1 << SLOT_BITS) - 1;
 
-// Image offsets of the stencil codes in shared memory.  off = (ox, oy, oz)
-// * binary32 cellh is exact in binary32 (|o| <= 2); the remainder offl =
-// (ox, oy, oz) * (cellh - binary32 cellh) completes it to the binary64
-// offset (double-float in binary64 mode, one more subtraction in binary32).
-template <bool DF>   // DF: binary64 mode (layout kept apart so binary32 kernels stay lean)
+// Image offsets of the stencil codes in shared memory, in the scaled frame
+// (Geo::xs): off = (ox, oy, oz) * cellh_s is exact in binary32 (|o| <= 2);
+// the remainder offl = (ox, oy, oz) * (cellh xs - cellh_s) completes it to
+// the binary64 offset (double-float in binary64 mode; in binary32 one more
+// subtraction in the general kernels, zero on a cubic grid).
+template <bool LO>   // LO: with the remainders (binary64 mode, general binary32 kernels); lean layouts go without
 struct SkinOffT
 {
     float4 off[125];    // image offset of each stencil code, binary32; .w: the code's bits
-    float4 offl[125];   // the remainders (binary64 offset - off)
+    float4 offl[LO ? 125 : 1];   // the remainders (binary64 offset - off)
 };
 
-template <bool DF>
-__device__ __forceinline__ void load_offsets(const Geo &g, SkinOffT<DF> &so)
+template <bool LO>
+__device__ __forceinline__ void load_offsets(const Geo &g, SkinOffT<LO> &so)
 {
     const int R = g.srad, W = 2 * R + 1;
+    // remainders cellh xs - cellh_s (3 binary64 operations per block)
+    const float lx = (float)(g.cellh[0] * g.xs - (double)g.cellh_s[0]),
+                ly = (float)(g.cellh[1] * g.xs - (double)g.cellh_s[1]),
+                lz = (float)(g.cellh[2] * g.xs - (double)g.cellh_s[2]);
     for (int c = threadIdx.x; c < W * W * W; c += blockDim.x)
     {
         const float ox = small_int_f(c / (W * W) - R), oy = small_int_f((c / W) % W - R), oz = small_int_f(c % W - R);
-        so.off[c] = make_float4(ox * g.cellh_f[0], oy * g.cellh_f[1], oz * g.cellh_f[2], __int_as_float(c));
-        so.offl[c] = make_float4(ox * g.cellh_l[0], oy * g.cellh_l[1], oz * g.cellh_l[2], 0.f);
+        so.off[c] = make_float4(ox * g.cellh_s[0], oy * g.cellh_s[1], oz * g.cellh_s[2], __int_as_float(c));
+        if (LO) so.offl[c] = make_float4(ox * lx, oy * ly, oz * lz, 0.f);
     }
     __syncthreads();
 }
+
+// the scaled frame (Geo::xs): binary32 xs^2 (force constants) and the EAM
+// r^2-grid index factor of a scaled r^2
+__device__ __forceinline__ float scaled_xs2(const Geo &g) { return (float)(g.xs * g.xs); }
+__device__ __forceinline__ float scaled_index_factor(const Geo &g) { return (float)(g.inv_dr2 * (g.inv_xs * g.inv_xs)); }
 
 // binary32 pair vector x_i - x_j - offset without the offset's remainder
 // (list-radius prefilters)
@@ -164,10 +174,10 @@ __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, 
     const int R = g.srad, W = 2 * R + 1;
     const float lim2 = g.rskin2 * 1.0001f;
     // position inside the cell box [0, h) (up to the drift since the build)
-    const float ux = xi.x + 0.5f * g.cellh_f[0], uy = xi.y + 0.5f * g.cellh_f[1], uz = xi.z + 0.5f * g.cellh_f[2];
+    const float ux = xi.x + 0.5f * g.cellh_s[0], uy = xi.y + 0.5f * g.cellh_s[1], uz = xi.z + 0.5f * g.cellh_s[2];
     for (int ox = -R; ox <= R; ox++)
     {
-        const float gx = axis_gap(ox, ux, g.cellh_f[0]);
+        const float gx = axis_gap(ox, ux, g.cellh_s[0]);
         if (gx * gx > lim2) continue;
         int cx = ci.x + ox;
         if (cx < 0 || cx >= g.nc[0])
@@ -177,7 +187,7 @@ __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, 
         }
         for (int oy = -R; oy <= R; oy++)
         {
-            const float gy = axis_gap(oy, uy, g.cellh_f[1]);
+            const float gy = axis_gap(oy, uy, g.cellh_s[1]);
             if (gx * gx + gy * gy > lim2) continue;
             int cy = ci.y + oy;
             if (cy < 0 || cy >= g.nc[1])
@@ -187,7 +197,7 @@ __device__ __forceinline__ void for_each_stencil_cell(const Geo &g, CellXYZ ci, 
             }
             for (int oz = -R; oz <= R; oz++)
             {
-                const float gz = axis_gap(oz, uz, g.cellh_f[2]);
+                const float gz = axis_gap(oz, uz, g.cellh_s[2]);
                 if (gx * gx + gy * gy + gz * gz > lim2) continue;
                 int cz = ci.z + oz;
                 if (cz < 0 || cz >= g.nc[2])
@@ -276,13 +286,15 @@ __device__ __forceinline__ void for_each_slot_pair(const Geo &g, const Side &S, 
     else
     {
         const double4_32a xdi = g.xd[t], oi = g.corig[S.cell_of[i]];
-        xi = make_float4((float)(xdi.x - oi.x), (float)(xdi.y - oi.y), (float)(xdi.z - oi.z), xi.w);
+        const double xs = g.xs;
+        xi = make_float4((float)((xdi.x - oi.x) * xs), (float)((xdi.y - oi.y) * xs), (float)((xdi.z - oi.z) * xs),
+                         xi.w);
         const float lim2 = g.rskin2 * 1.0001f;
         for_each_candidate(g, S, i, xi, [&](int j, int code) {
             const int js = S.slot[j];
             const double4_32a xdj = g.xd[js], oj = g.corig[S.cell_of[j]];
-            const float4 xj = make_float4((float)(xdj.x - oj.x), (float)(xdj.y - oj.y), (float)(xdj.z - oj.z),
-                                          g.xf4[j].w);
+            const float4 xj = make_float4((float)((xdj.x - oj.x) * xs), (float)((xdj.y - oj.y) * xs),
+                                          (float)((xdj.z - oj.z) * xs), g.xf4[j].w);
             float4 o = so.off[code];
             const float3 d = rv_of(xi, xj, o);
             if (d.x * d.x + d.y * d.y + d.z * d.z > lim2) return;
@@ -311,16 +323,17 @@ __device__ __forceinline__ void slot_rel_build(const Geo &g, Dyn *dyn, int t, co
     const double o3[3] = {ob.x, ob.y, ob.z};
     float l3[3];
     double u3[3];
+    const double xs = g.xs;     // (1 in binary64 mode: xll below holds remainders of unscaled values)
     for (int d = 0; d < 3; d++)
     {
         double u = x[d] - o3[d];
-        float uf = d2f_rn(u);
+        float uf = d2f_rn(u * xs);
         // unwrap across a periodic face (binary64 test near half a box)
         if (g.pbc[d] && fabsf(uf) > 0.49f * g.l_f[d])
         {
             if (u > 0.5 * g.l[d]) u -= g.l[d];
             else if (u < -0.5 * g.l[d]) u += g.l[d];
-            uf = d2f_rn(u);
+            uf = d2f_rn(u * xs);
         }
         l3[d] = uf;
         u3[d] = u;
@@ -409,7 +422,8 @@ __global__ void k_prep_skin(__grid_constant__ const L loc, int lazy)
     // relative to the current cell (a rebuild starts from these)
     const double4_32a oc = g.corig[S.cell_of[i]];
     const double ux = x[0] - oc.x, uy = x[1] - oc.y, uz = x[2] - oc.z;
-    const float lx = (float)ux, ly = (float)uy, lz = (float)uz;
+    const double xs = g.xs;     // (1 in binary64 mode: the remainders below are of unscaled values)
+    const float lx = (float)(ux * xs), ly = (float)(uy * xs), lz = (float)(uz * xs);
     g.xf4[i] = make_float4(lx, ly, lz, kb);
     if (g.prec == FMDG_PREC_FP64)
     {
@@ -614,8 +628,8 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
     if (loc_idle(loc, g)) return;
     const int group = g.st.group;
     __shared__ SmemPotT<!MIXED, LEAN> sp;
-    __shared__ SkinOffT<!MIXED> so;
-    load_pot(g, sp);
+    __shared__ SkinOffT<!MIXED || !LEAN> so;   // lean binary32 kernels: no remainders (exact on a cubic grid)
+    load_pot(g, sp, skin_params(g));
     load_offsets(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
@@ -655,7 +669,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 // branch-free walk (table rows read for every entry, entries
                 // beyond the cutoff add zero); near-cutoff entries decided in
                 // binary64 after the walk, as in the lean force kernel
-                const float inv_h = (float)g.inv_dr2;
+                const float inv_h = scaled_index_factor(g);   // (scaled r^2: index only)
                 const float kmax = (float)(nint - 1);
                 const float4 *trho = g.pkf_rho + (size_t)sp.pairs[0].jloc * nint;
                 const float rc2f = sp.pf[0][2], band = 2e-5f * rc2f;
@@ -664,7 +678,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 int npend = 0, pend = 0;
                 float pr2 = 0.f;
                 for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                    const float3 rv = rv_lo(so, xi, xj, o);
+                    const float3 rv = rv_of(xi, xj, o);
                     const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                     const bool near = fabsf(r2 - rc2f) <= band;
                     const bool in = (r2 < rc2f) && !near;
@@ -690,7 +704,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
                 else if (npend > 1)
                 {
                     for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                        const float3 rv = rv_lo(so, xi, xj, o);
+                        const float3 rv = rv_of(xi, xj, o);
                         const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                         if (!(fabsf(r2 - rc2f) <= band)) return;
                         if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
@@ -704,7 +718,7 @@ __global__ void __launch_bounds__(L::max_threads, L::min_blocks) k_density_skin(
             }
             else
             {
-                const float inv_h = (float)g.inv_dr2;
+                const float inv_h = scaled_index_factor(g);   // (scaled r^2: index only)
                 const float kmax = (float)(nint - 1);
                 Acc32<1> ac;
                 for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
@@ -785,8 +799,8 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
     const int group = g.st.group;
     const double dt = g.st.dt;
     __shared__ SmemPotT<!MIXED, LEAN> sp;
-    __shared__ SkinOffT<!MIXED> so;
-    load_pot(g, sp);
+    __shared__ SkinOffT<!MIXED || !LEAN> so;   // lean binary32 kernels: no remainders (exact on a cubic grid)
+    load_pot(g, sp, skin_params(g));
     load_offsets(g, so);
     Dyn *dyn = g.dyn;
     const Side S = g.side[dyn->cur];
@@ -840,12 +854,16 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 const float4 pq = make_float4(sp.pf[0][0], sp.pf[0][1], sp.pf[0][2], sp.pf[0][3]);
                 const float rc2f = (CAT == CAT_MORSE) ? pq.w : pq.z;
                 const double rc2 = (CAT == CAT_MORSE) ? sp.pairs[0].p[3] : sp.pairs[0].p[2];
-                // Morse: 2^((r0 - r) alpha log2 e), force factor 2 alpha D0
-                const float m_c1 = pq.y * 1.44269504f, m_c2 = 2.f * pq.y * pq.x;
-                // LJ: 12 eps4
-                const float lj_c = 12.f * pq.x;
+                // scaled frame (Geo::xs; pq holds scaled parameters): real
+                // force factors from scaled geometry.  Morse: 2^((r0' - r')
+                // alpha' log2 e) with alpha' = alpha / xs, r0' = r0 xs, factor
+                // 2 alpha D0 xs = 2 alpha' D0 xs^2; LJ: 12 eps4 xs^2 / r'^2
+                const float xs2 = scaled_xs2(g);
+                const float m_c1 = pq.y * 1.44269504f, m_c2 = 2.f * pq.y * pq.x * xs2;
+                const float lj_c = 12.f * pq.x * xs2;
                 const float fpi = (CAT == CAT_EAM) ? g.fpb[t] : 0.f;
-                const float inv_h = (float)g.inv_dr2;
+                const float inv_h = (float)g.inv_dr2;         // derivatives with respect to the real r^2
+                const float inv_hi = scaled_index_factor(g);  // table index of the scaled r^2
                 const float kmax = (float)(nint - 1);
                 const int ee = sp.pairs[0].iloc;
                 const float4 *tpr = g.pkf_pr + (size_t)ee * nint * 2;
@@ -882,13 +900,13 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                     {
                         const float band = 1e-4f * rc2f;
                         for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                            const float3 rv = rv_lo(so, xi, xj, o);
+                            const float3 rv = rv_of(xi, xj, o);
                             const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                             bool in = r2 < rc2f;
                             if (fabsf(r2 - rc2f) <= band) in = geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2;
                             if (!in) return;
                             float b;
-                            const int ir2 = table_index(r2 * inv_h, kmax, b);
+                            const int ir2 = table_index(r2 * inv_hi, kmax, b);
                             float4 tph, trh;
                             ld_row32(tpr + 2 * ir2, tph, trh);
                             const float phi_d = spl_der(tph, b, inv_h);
@@ -918,7 +936,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         int npend = 0, pend = 0;
                         float3 prv = make_float3(0.f, 0.f, 0.f);
                         for_each_slot_pair<true>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                            const float3 rv = rv_lo(so, xi, xj, o);
+                            const float3 rv = rv_of(xi, xj, o);
                             const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                             const bool near = fabsf(r2 - rc2f) <= band;
                             const bool in = (r2 < rc2f) && !near;
@@ -954,7 +972,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         else if (npend > 1)
                         {
                             for_each_slot_pair<false>(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
-                                const float3 rv = rv_lo(so, xi, xj, o);
+                                const float3 rv = rv_of(xi, xj, o);
                                 const float r2 = rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
                                 if (!(fabsf(r2 - rc2f) <= band)) return;
                                 if (!(geom64_mi(g, g.xd[t], g.xd[js]).r2 < rc2)) return;
@@ -985,8 +1003,10 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
             else
             {
                 const float fpi = (CAT == CAT_EAM || CAT == CAT_HYBRID) ? g.fpb[t] : 0.f;
-                const float inv_h = (float)g.inv_dr2;
+                const float inv_h = (float)g.inv_dr2;         // derivatives with respect to the real r^2
+                const float inv_hi = scaled_index_factor(g);  // table index of the scaled r^2
                 const float kmax = (float)(nint - 1);
+                const float xs2 = scaled_xs2(g);
                 Acc32<5> ac;
                 for_each_slot_pair(g, S, so, t, i, xi, [&](int js, float4 xj, float4 o) {
                     if (group >= 0 && g.gslot[js] != group) return;
@@ -1001,6 +1021,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         {
                             float fa, e;
                             lj_pair(r2, sp.pf[pidx][0], sp.pf[pidx][1], fa, e);
+                            fa *= xs2;         // the real force factor (scaled frame)
                             ac.part[0] += rv.x * fa;
                             ac.part[1] += rv.y * fa;
                             ac.part[2] += rv.z * fa;
@@ -1014,6 +1035,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         {
                             float fa, e;
                             morse_pair(r2, sp.pf[pidx][0], sp.pf[pidx][1], sp.pf[pidx][2], fa, e);
+                            fa *= xs2;         // the real force factor (scaled frame)
                             ac.part[0] += fa * rv.x;
                             ac.part[1] += fa * rv.y;
                             ac.part[2] += fa * rv.z;
@@ -1026,7 +1048,7 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                         if (within_cut_skin(g, t, js, r2, sp.pf[pidx][2], pp.p[2]))
                         {
                             float b;
-                            const int ir2 = table_index(r2 * inv_h, kmax, b);
+                            const int ir2 = table_index(r2 * inv_hi, kmax, b);
                             const int ei = pp.iloc, ej = pp.jloc;
                             const float4 tph = g.pkf_phi[((size_t)ei * ne + ej) * nint + ir2];
                             const float phi_d = spl_der(tph, b, inv_h);
@@ -1048,6 +1070,13 @@ __global__ void __launch_bounds__(L::max_threads, LEAN ? L::lean_min_blocks : L:
                 pe = ac.total(3);
                 vir = 0.5 * ac.total(4);
             }
+        }
+        if (MIXED)
+        {
+            // binary32 pairs were summed in the scaled frame (Geo::xs): the
+            // real force is the sum over xs, the real virial over xs^2
+            for (int d = 0; d < 3; d++) f[d] *= g.inv_xs;
+            vir *= g.inv_xs * g.inv_xs;
         }
         if (active && g.ttm_on)
         {

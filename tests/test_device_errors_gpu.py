@@ -52,9 +52,15 @@ def test_position_error_event(gpu_lib):
     assert (FMD_ERR_UNEXPECTED_POSITION, True) in errs, errs
 
 
+# five atoms moved to within 0.02 A of atom 0: its density gains ~26 per
+# such neighbour (f(r) -> e^3.3 as r -> 0), ~132 in all, and leaves the
+# 0-120 F(rho) table
+CLUSTER = np.array([[0.02, 0.0, 0.0], [0.0, 0.02, 0.0], [0.0, 0.0, 0.02], [-0.02, 0.0, 0.0], [0.0, -0.02, 0.0]])
+
+
 def test_eam_density_range_error_event(gpu_lib):
     def edit(x, grid):
-        x[1] = x[0] + np.array([0.02, 0.0, 0.0])
+        x[1:6] = x[0] + CLUSTER
     errs = _errors_after(gpu_lib, "eam", edit, 0.00095)
     assert (FMD_ERR_OUTSIDE_REAL_INTERVAL, True) in errs, errs
 
@@ -65,7 +71,7 @@ def test_served_job_reports_device_errors(gpu_lib):
     j = dict(pot="eam", ncell=6, T=300.0, seed=91)
     x, v, l = serve.job_atoms(j)
     x = x.copy()
-    x[1] = x[0] + np.array([0.02, 0.0, 0.0])
+    x[1:6] = x[0] + CLUSTER
     srv = serve.Server(L, chunk_steps=4, eam=eam)
     bad = srv.submit("eam", x, v, l, 4)
     xg, vg, lg = serve.job_atoms(dict(j, seed=92))

@@ -184,7 +184,7 @@ def test_ttm_mixed_te_error(gpu_lib):
     """The laser-heated slab (200 steps through the pulse) in mixed
     precision: binary32 pair arithmetic moves the atoms slightly differently
     from the reference, the lattice temperature that couples to the
-    electrons follows, and the electron temperatures stay within 1e-6 of
+    electrons follows, and the electron temperatures stay within 1e-9 of
     the reference's binary64 values at every event and at the end."""
     import ctypes as C
     name = "ttm_slab"

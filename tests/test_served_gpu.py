@@ -260,6 +260,27 @@ def test_mixed_force_error_bound(L, eam, pot):
     assert err <= 1e-5, err
 
 
+@pytest.mark.parametrize("pot,ncell", [("lj", 6), ("morse", 5), ("morse", 8), ("eam", 10)])
+def test_mixed_force_error_cold(L, eam, pot, ncell):
+    """Cold crystals (50 K) have the smallest net forces, so the largest
+    relative errors: the packed mixed-precision kernels after 24 steps
+    against the binary64 oracle at the job's own positions, max |dF| <= 1e-5
+    max |F| (the stream's coldest jobs are at 50 K)."""
+    x, v, l, kind = _sys(pot, ncell, 50.0, 91)
+    srv = serve.Server(L, chunk_steps=8, eam=eam)
+    jid = srv.submit(pot, x, v, l, 24, precision=serve.PREC_MIXED, keep_state=True)
+    srv.drain()
+    assert srv.result(jid).state == 2
+    xp, vp, Fp, ids = srv.state(jid, len(x))
+    srv.close()
+    Fo = _oracle_forces(pot, l, kind, xp, vp, ids)
+    Fq = np.zeros_like(Fp)
+    Fq[ids] = Fp
+    err = np.abs(Fq - Fo).max() / np.abs(Fo).max()
+    print(pot, ncell, "cold mixed force error %.3e" % err)
+    assert err <= 1e-5, err
+
+
 def test_more_jobs_than_one_pack(L, eam):
     """40 jobs of one category and precision need two packs (at most 32
     systems travel in one launch); every job still equals its run alone bit
