@@ -48,6 +48,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# The served fleet runs dozens of packs on their own streams: more hardware
+# work queues (the default is 8) keep unrelated streams from queueing behind
+# one another.  Read when the CUDA context is created, so set before it.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 

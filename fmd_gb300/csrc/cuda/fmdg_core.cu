@@ -47,10 +47,25 @@ int dalloc(fmdg_sys_t *s, T **p, size_t n)
     if (n == 0) n = 1;
     cudaError_t e = cudaMallocAsync((void **)p, n * sizeof(T), s->stream);
     if (e != cudaSuccess) return fmdg_fail("cudaMallocAsync", e);
-    e = cudaStreamSynchronize(s->stream);
-    if (e != cudaSuccess) return fmdg_fail("cudaStreamSynchronize", e);
     return FMDG_OK;
 }
+
+// Every transfer of a system goes through its own stream: its memory is
+// allocated stream-ordered on that stream, and nothing else needs to wait.
+// Host-to-device copies do not block on the device (a served job's set-up
+// never waits behind the packed chunks queued on the GPU); device-to-host
+// reads synchronise the system's stream.
+int d2h_sync(fmdg_sys_t *s, void *dst, const void *src, size_t n)
+{
+    FMDG_CK(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s->stream));
+    FMDG_CK(cudaStreamSynchronize(s->stream));
+    return FMDG_OK;
+}
+#define FMDG_D2H(dst, src, n)                                            \
+    do {                                                                 \
+        const int r_ = d2h_sync(s, (dst), (src), (n));                   \
+        if (r_) return r_;                                               \
+    } while (0)
 
 void dfree(fmdg_sys_t *s, void *p) { if (p) cudaFreeAsync(p, s->stream); }
 
@@ -246,8 +261,8 @@ extern "C" int fmdg_create(fmdg_sys_t **out, int device)
     if (rc) return rc;
     rc = dalloc(s, &s->g.thermo, 1);
     if (rc) return rc;
-    FMDG_CK(cudaMemset(s->g.dyn, 0, sizeof(Dyn)));
-    FMDG_CK(cudaMemset(s->g.thermo, 0, sizeof(fmdg_thermo_t)));
+    FMDG_CK(cudaMemsetAsync(s->g.dyn, 0, sizeof(Dyn), s->stream));
+    FMDG_CK(cudaMemsetAsync(s->g.thermo, 0, sizeof(fmdg_thermo_t), s->stream));
     s->ttm_turi = -1;
     s->fblk = 128;
     // Verlet skin of the neighbour list (A) of mixed-precision systems;
@@ -337,8 +352,8 @@ extern "C" int fmdg_set_kinds(fmdg_sys_t *s, int nkinds, const double *mass, con
         rc = dalloc(s, (float2 **)&s->g.paird, 4 * FMDG_MAXK * FMDG_MAXK);
         if (rc) return rc;
     }
-    FMDG_CK(cudaMemcpy((void *)s->g.mass, s->h_mass, sizeof(double) * nkinds, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)s->g.eam_elem, s->h_eam_elem, sizeof(int) * nkinds, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync((void *)s->g.mass, s->h_mass, sizeof(double) * nkinds, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)s->g.eam_elem, s->h_eam_elem, sizeof(int) * nkinds, cudaMemcpyHostToDevice, s->stream));
     invalidate_graph(s);
     return FMDG_OK;
 }
@@ -356,7 +371,7 @@ extern "C" int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table)
             return fmdg_set_error("fmdg_set_pairs: every kind pair needs a potential");
         s->cats |= 1 << c;
     }
-    FMDG_CK(cudaMemcpy((void *)s->g.pairs, s->h_pairs, sizeof(fmdg_pair_t) * nk2, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync((void *)s->g.pairs, s->h_pairs, sizeof(fmdg_pair_t) * nk2, cudaMemcpyHostToDevice, s->stream));
     // binary32 and double-float copies of the parameters, formed here so
     // that kernel prologues do no binary64 or conversion work
     float4 pf[FMDG_MAXK * FMDG_MAXK];
@@ -367,8 +382,8 @@ extern "C" int fmdg_set_pairs(fmdg_sys_t *s, const fmdg_pair_t *table)
         pf[k] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
         for (int q = 0; q < 4; q++) pd[4 * k + q] = df_split(p[q]);
     }
-    FMDG_CK(cudaMemcpy((void *)s->g.pairf, pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)s->g.paird, pd, sizeof(float2) * 4 * nk2, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync((void *)s->g.pairf, pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)s->g.paird, pd, sizeof(float2) * 4 * nk2, cudaMemcpyHostToDevice, s->stream));
     s->g.has_eam = (s->cats >> FMDG_POT_EAM) & 1;
     invalidate_graph(s);
     return fmdg_skin_scale(s);
@@ -416,7 +431,7 @@ int fmdg_skin_scale(fmdg_sys_t *s)
                 q[2] = p[2] * xs * xs;
             pf[k] = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
         }
-        FMDG_CK(cudaMemcpy((void *)skin_params(g), pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync((void *)skin_params(g), pf, sizeof(float4) * nk2, cudaMemcpyHostToDevice, s->stream));
     }
     invalidate_graph(s);
     return FMDG_OK;
@@ -437,12 +452,12 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
         (rc = dalloc(s, (double **)&g.erho, nR)) || (rc = dalloc(s, (double **)&g.erhoDD, nR)) ||
         (rc = dalloc(s, (double **)&g.ephi, nP)) || (rc = dalloc(s, (double **)&g.ephiDD, nP)))
         return rc;
-    FMDG_CK(cudaMemcpy((void *)g.eF, F, nF * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)g.eFDD, F_DD, nF * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)g.erho, rho, nR * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)g.erhoDD, rhoDD, nR * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)g.ephi, phi, nP * 8, cudaMemcpyHostToDevice));
-    FMDG_CK(cudaMemcpy((void *)g.ephiDD, phiDD, nP * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync((void *)g.eF, F, nF * 8, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)g.eFDD, F_DD, nF * 8, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)g.erho, rho, nR * 8, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)g.erhoDD, rhoDD, nR * 8, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)g.ephi, phi, nP * 8, cudaMemcpyHostToDevice, s->stream));
+    FMDG_CK(cudaMemcpyAsync((void *)g.ephiDD, phiDD, nP * 8, cudaMemcpyHostToDevice, s->stream));
     g.nelem = nelem; g.Nrho = Nrho; g.Nr2 = Nr2; g.drho = drho; g.dr2 = dr2;
     g.inv_dr2 = 1.0 / dr2;
     g.inv_drho = 1.0 / drho;
@@ -480,12 +495,12 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
             }
         int rc2;
         if ((rc2 = dalloc(s, (double4_32a **)d64, h64.size())) || (rc2 = dalloc(s, (float4 **)d32, h32.size()))) return rc2;
-        FMDG_CK(cudaMemcpy((void *)*d64, h64.data(), h64.size() * sizeof(double4_32a), cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync((void *)*d64, h64.data(), h64.size() * sizeof(double4_32a), cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync((void *)*d32, h32.data(), h32.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
         if (ddf)
         {
             if ((rc2 = dalloc(s, (float4 **)ddf, hdf.size()))) return rc2;
-            FMDG_CK(cudaMemcpy((void *)*ddf, hdf.data(), hdf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+            FMDG_CK(cudaMemcpyAsync((void *)*ddf, hdf.data(), hdf.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
         }
         return FMDG_OK;
     };
@@ -496,8 +511,8 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
         // the one-element pair rows side by side for the lean force kernels
         const size_t nint = (size_t)Nr2 - 1;
         std::vector<float4> phi32(nint * nelem * nelem), rho32(nint * nelem), pr(2 * nint * nelem);
-        FMDG_CK(cudaMemcpy(phi32.data(), g.pkf_phi, phi32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
-        FMDG_CK(cudaMemcpy(rho32.data(), g.pkf_rho, rho32.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        FMDG_D2H(phi32.data(), g.pkf_phi, phi32.size() * sizeof(float4));
+        FMDG_D2H(rho32.data(), g.pkf_rho, rho32.size() * sizeof(float4));
         for (int e = 0; e < nelem; e++)
             for (size_t k = 0; k < nint; k++)
             {
@@ -505,12 +520,15 @@ extern "C" int fmdg_set_eam(fmdg_sys_t *s, int nelem, int Nrho, double drho, int
                 pr[2 * (e * nint + k) + 1] = rho32[(size_t)e * nint + k];
             }
         if ((rc = dalloc(s, (float4 **)&g.pkf_pr, pr.size()))) return rc;
-        FMDG_CK(cudaMemcpy((void *)g.pkf_pr, pr.data(), pr.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync((void *)g.pkf_pr, pr.data(), pr.size() * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
     }
     // the 32-byte row tables are read with 256-bit loads (ld_row32)
     if (((uintptr_t)g.pkf_pr | (uintptr_t)g.pkd_rho | (uintptr_t)g.pkd_phi) % 32)
         return fmdg_set_error("fmdg_set_eam: row tables not 32-byte aligned");
     invalidate_graph(s);
+    // other systems may read these tables on their own streams
+    // (fmdg_share_eam): the copies complete before this call returns
+    FMDG_CK(cudaStreamSynchronize(s->stream));
     return fmdg_skin_scale(s);
 }
 
@@ -591,7 +609,7 @@ size_t fmdg_bytes_estimate(int n, int ncell, int maxnb)
 // packed launches: steps the system still takes
 int fmdg_set_steps_left(fmdg_sys_t *s, int steps)
 {
-    FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, steps_left), &steps, sizeof steps, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync((char *)s->g.dyn + offsetof(Dyn, steps_left), &steps, sizeof steps, cudaMemcpyHostToDevice, s->stream));
     return FMDG_OK;
 }
 
@@ -651,8 +669,12 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     for (int i = 0; i < n; i++)
         if (kind[i] >= (unsigned)(s->nkinds > 0 ? s->nkinds : FMDG_MAXK))
             return fmdg_set_error("fmdg_upload: atom kind out of range");
+    // the device time and step of an earlier upload carry over; a fresh
+    // system's dynamic scalars are the zeros of fmdg_create (no device read,
+    // so a served job's set-up does not wait for the GPU)
     Dyn d;
-    FMDG_CK(cudaMemcpy(&d, g.dyn, sizeof d, cudaMemcpyDeviceToHost));
+    if (s->uploaded) FMDG_D2H(&d, g.dyn, sizeof d);
+    else memset(&d, 0, sizeof d);
     free_atoms(s);
     const int cap = n > 0 ? n : 1;
     g.cap = cap;
@@ -788,9 +810,10 @@ extern "C" int fmdg_upload(fmdg_sys_t *s, int n, const int *cell_count, const do
     d.time = keep_time;
     d.dt = keep_dt;
     FMDG_CK(cudaMemcpyAsync(g.dyn, &d, sizeof d, cudaMemcpyHostToDevice, st));
-    // the host staging buffers are released on return
-    FMDG_CK(cudaStreamSynchronize(st));
+    // (copies from pageable host memory are staged before the calls return,
+    // so the host buffers may go)
     s->atoms = true;
+    s->uploaded = true;
     return FMDG_OK;
 }
 
@@ -816,7 +839,7 @@ extern "C" int fmdg_download(fmdg_sys_t *s, int *cell_of, double *x, double *v, 
     const int n = d.n, cap = g.cap;
     std::vector<double> buf(3 * (size_t)cap);
     auto get3 = [&](const double *src, double *dst) -> int {
-        FMDG_CK(cudaMemcpy(buf.data(), src, 3 * (size_t)cap * 8, cudaMemcpyDeviceToHost));
+        FMDG_D2H(buf.data(), src, 3 * (size_t)cap * 8);
         for (int i = 0; i < n; i++)
             for (int k = 0; k < 3; k++) dst[3 * (size_t)i + k] = buf[(size_t)k * cap + i];
         return FMDG_OK;
@@ -826,11 +849,11 @@ extern "C" int fmdg_download(fmdg_sys_t *s, int *cell_of, double *x, double *v, 
     if (F && (rc = get3(g.F, F))) return rc;
     if (n > 0)
     {
-        if (vaream) FMDG_CK(cudaMemcpy(vaream, g.vaream, (size_t)n * 8, cudaMemcpyDeviceToHost));
-        if (kind) FMDG_CK(cudaMemcpy(kind, S.kind, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        if (group) FMDG_CK(cudaMemcpy(group, S.group, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        if (atomid) FMDG_CK(cudaMemcpy(atomid, S.atomid, (size_t)n * 4, cudaMemcpyDeviceToHost));
-        if (cell_of) FMDG_CK(cudaMemcpy(cell_of, S.cell_of, (size_t)n * 4, cudaMemcpyDeviceToHost));
+        if (vaream) FMDG_D2H(vaream, g.vaream, (size_t)n * 8);
+        if (kind) FMDG_D2H(kind, S.kind, (size_t)n * 4);
+        if (group) FMDG_D2H(group, S.group, (size_t)n * 4);
+        if (atomid) FMDG_D2H(atomid, S.atomid, (size_t)n * 4);
+        if (cell_of) FMDG_D2H(cell_of, S.cell_of, (size_t)n * 4);
     }
     return FMDG_OK;
 }
@@ -845,10 +868,10 @@ extern "C" int fmdg_set_state(fmdg_sys_t *s, const double *x, const double *v)
     const int n = d.n, cap = s->g.cap;
     std::vector<double> buf(3 * (size_t)cap, 0.0);
     auto put3 = [&](const double *src, double *dst) -> int {
-        FMDG_CK(cudaMemcpy(buf.data(), dst, 3 * (size_t)cap * 8, cudaMemcpyDeviceToHost));
+        FMDG_D2H(buf.data(), dst, 3 * (size_t)cap * 8);
         for (int i = 0; i < n; i++)
             for (int k = 0; k < 3; k++) buf[(size_t)k * cap + i] = src[3 * (size_t)i + k];
-        FMDG_CK(cudaMemcpy(dst, buf.data(), 3 * (size_t)cap * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync(dst, buf.data(), 3 * (size_t)cap * 8, cudaMemcpyHostToDevice, s->stream));
         return FMDG_OK;
     };
     if (x && (rc = put3(x, S.x))) return rc;
@@ -857,7 +880,7 @@ extern "C" int fmdg_set_state(fmdg_sys_t *s, const double *x, const double *v)
     {
         // positions set from outside: the skin list is rebuilt first
         const int one = 1;
-        FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, rebuild), &one, sizeof one, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync((char *)s->g.dyn + offsetof(Dyn, rebuild), &one, sizeof one, cudaMemcpyHostToDevice, s->stream));
     }
     return FMDG_OK;
 }
@@ -1050,7 +1073,7 @@ extern "C" int fmdg_set_time(fmdg_sys_t *s, double time, double dt)
     if (rc) return rc;
     d.time = time;
     d.dt = dt;
-    FMDG_CK(cudaMemcpy(s->g.dyn, &d, sizeof d, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync(s->g.dyn, &d, sizeof d, cudaMemcpyHostToDevice, s->stream));
     return FMDG_OK;
 }
 
@@ -1079,10 +1102,10 @@ extern "C" int fmdg_turi_add(fmdg_sys_t *s, const int dims_local[3], const int g
     if ((rc = dalloc(s, &t.acc, 5 * nc)) || (rc = dalloc(s, &t.tacc, nc)) || (rc = dalloc(s, &t.mass, nc)) ||
         (rc = dalloc(s, &t.vcm, 3 * nc)) || (rc = dalloc(s, &t.Ti, nc)) || (rc = dalloc(s, &t.num, nc)))
         return rc;
-    FMDG_CK(cudaMemset(t.num, 0, nc * sizeof(unsigned)));
-    FMDG_CK(cudaMemset(t.mass, 0, nc * sizeof(double)));
-    FMDG_CK(cudaMemset(t.vcm, 0, 3 * nc * sizeof(double)));
-    FMDG_CK(cudaMemset(t.Ti, 0, nc * sizeof(double)));
+    FMDG_CK(cudaMemsetAsync(t.num, 0, nc * sizeof(unsigned), s->stream));
+    FMDG_CK(cudaMemsetAsync(t.mass, 0, nc * sizeof(double), s->stream));
+    FMDG_CK(cudaMemsetAsync(t.vcm, 0, 3 * nc * sizeof(double), s->stream));
+    FMDG_CK(cudaMemsetAsync(t.Ti, 0, nc * sizeof(double), s->stream));
     *handle = s->nturi++;
     invalidate_graph(s);
     return FMDG_OK;
@@ -1105,13 +1128,13 @@ extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, c
             (rc = dalloc(s, &t.srcz, nz)) || (rc = dalloc(s, &t.Te_pre, nz)))
             return rc;
         std::vector<double> m1(nz, -1.0), z0(nz, 0.0);
-        FMDG_CK(cudaMemcpy(t.Te, m1.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.Te2, m1.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.Te_pre, m1.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.xi, z0.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.Ke, z0.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.Ce, z0.data(), nz * 8, cudaMemcpyHostToDevice));
-        FMDG_CK(cudaMemcpy(t.Gc, z0.data(), nz * 8, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync(t.Te, m1.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.Te2, m1.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.Te_pre, m1.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.xi, z0.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.Ke, z0.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.Ce, z0.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
+        FMDG_CK(cudaMemcpyAsync(t.Gc, z0.data(), nz * 8, cudaMemcpyHostToDevice, s->stream));
     }
     dfree(s, (void *)t.p.T_C); dfree(s, (void *)t.p.Ct); dfree(s, (void *)t.p.C_DD);
     dfree(s, (void *)t.p.T_G); dfree(s, (void *)t.p.Gt); dfree(s, (void *)t.p.G_DD);
@@ -1129,7 +1152,7 @@ extern "C" int fmdg_ttm_setup(fmdg_sys_t *s, int turi, int itc_lo, int itc_hi, c
         auto up = [&](const double *h, int n, const double **d) -> int {
             int r = dalloc(s, (double **)d, n);
             if (r) return r;
-            FMDG_CK(cudaMemcpy((void *)*d, h, (size_t)n * 8, cudaMemcpyHostToDevice));
+            FMDG_CK(cudaMemcpyAsync((void *)*d, h, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream));
             return FMDG_OK;
         };
         if ((rc = up(p->T_C, p->nC, &q.T_C)) || (rc = up(p->Ct, p->nC, &q.Ct)) || (rc = up(p->C_DD, p->nC, &q.C_DD)) ||
@@ -1159,7 +1182,7 @@ extern "C" int fmdg_ttm_set_te(fmdg_sys_t *s, int turi, const double *Te)
 {
     if (turi < 0 || turi >= s->nturi || !s->turi[turi].Te) return fmdg_set_error("fmdg_ttm_set_te: no TTM");
     DTuri &t = s->turi[turi];
-    FMDG_CK(cudaMemcpy(t.Te, Te, (size_t)t.dims[2] * 8, cudaMemcpyHostToDevice));
+    FMDG_CK(cudaMemcpyAsync(t.Te, Te, (size_t)t.dims[2] * 8, cudaMemcpyHostToDevice, s->stream));
     return FMDG_OK;
 }
 
@@ -1170,14 +1193,14 @@ extern "C" int fmdg_turi_download(fmdg_sys_t *s, int turi, unsigned *num, double
     FMDG_CK(cudaStreamSynchronize(s->stream));
     DTuri &t = s->turi[turi];
     const size_t nc = t.ncells;
-    if (num) FMDG_CK(cudaMemcpy(num, t.num, nc * 4, cudaMemcpyDeviceToHost));
-    if (mass) FMDG_CK(cudaMemcpy(mass, t.mass, nc * 8, cudaMemcpyDeviceToHost));
-    if (vcm) FMDG_CK(cudaMemcpy(vcm, t.vcm, 3 * nc * 8, cudaMemcpyDeviceToHost));
-    if (Ti) FMDG_CK(cudaMemcpy(Ti, t.Ti, nc * 8, cudaMemcpyDeviceToHost));
+    if (num) FMDG_D2H(num, t.num, nc * 4);
+    if (mass) FMDG_D2H(mass, t.mass, nc * 8);
+    if (vcm) FMDG_D2H(vcm, t.vcm, 3 * nc * 8);
+    if (Ti) FMDG_D2H(Ti, t.Ti, nc * 8);
     if (t.Te)
     {
-        if (Te) FMDG_CK(cudaMemcpy(Te, t.Te, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
-        if (xi) FMDG_CK(cudaMemcpy(xi, t.xi, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
+        if (Te) FMDG_D2H(Te, t.Te, (size_t)t.dims[2] * 8);
+        if (xi) FMDG_D2H(xi, t.xi, (size_t)t.dims[2] * 8);
     }
     return FMDG_OK;
 }
@@ -1187,7 +1210,7 @@ extern "C" int fmdg_ttm_download_te(fmdg_sys_t *s, int turi, int presolve, doubl
     if (turi < 0 || turi >= s->nturi || !s->turi[turi].Te) return fmdg_set_error("fmdg_ttm_download_te: no TTM");
     FMDG_CK(cudaStreamSynchronize(s->stream));
     DTuri &t = s->turi[turi];
-    FMDG_CK(cudaMemcpy(Te, presolve ? t.Te_pre : t.Te, (size_t)t.dims[2] * 8, cudaMemcpyDeviceToHost));
+    FMDG_D2H(Te, presolve ? t.Te_pre : t.Te, (size_t)t.dims[2] * 8);
     return FMDG_OK;
 }
 
@@ -1265,7 +1288,7 @@ extern "C" int fmdg_get_errors(fmdg_sys_t *s, unsigned *bits, int clear)
     if (clear && d.err)
     {
         unsigned z = 0;
-        FMDG_CK(cudaMemcpy((char *)s->g.dyn + offsetof(Dyn, err), &z, sizeof z, cudaMemcpyHostToDevice));
+        FMDG_CK(cudaMemcpyAsync((char *)s->g.dyn + offsetof(Dyn, err), &z, sizeof z, cudaMemcpyHostToDevice, s->stream));
     }
     return FMDG_OK;
 }
@@ -1342,7 +1365,7 @@ extern "C" int fmdg_flush_l2(fmdg_sys_t *s)
         s->l2bytes = (size_t)256 << 20;
         int rc = dalloc(s, (char **)&s->l2buf, s->l2bytes);
         if (rc) return rc;
-        FMDG_CK(cudaMemset(s->l2buf, 0, s->l2bytes));
+        FMDG_CK(cudaMemsetAsync(s->l2buf, 0, s->l2bytes, s->stream));
     }
     k_flush<<<1216, 256, 0, s->stream>>>((unsigned *)s->l2buf, s->l2bytes / 4);
     FMDG_CK(cudaGetLastError());

@@ -164,6 +164,7 @@ struct fmdg_sys
     Geo g;
     Geo *d_geo;
     bool box_set, atoms;
+    bool uploaded;                // atoms were uploaded at least once (the device time carries over)
     int nkinds;
     fmdg_pair_t h_pairs[FMDG_MAXK * FMDG_MAXK];
     double h_mass[FMDG_MAXK];

@@ -6,7 +6,8 @@ API on the GPU.
   NVE energy drift (max |E(t) - E(0)| / |E(0)| over 20 samples) is compared:
   binary64 and mixed precision within 2x the oracle's drift (+1e-7).
 * EAM copper, 256 000 atoms: step-0 forces of both precisions against the
-  oracle, and the 5000-step NVE drift of each within 2x the oracle's.
+  oracle, and the NVE drift of each within 2x the oracle's over the first
+  2000 steps (the configured potential collapses the crystal later on).
 * Morse collision, 512 000-atom slab + a 20 A projectile sphere at 2 km/s,
   periodic x, y, 100 A vacuum in z: step-0 forces against the oracle
   (binary64 1e-10, mixed 1e-5 of max |F|), then 200 steps: no atom lost
@@ -93,11 +94,14 @@ def test_eam256k_full_size(gpu_lib):
     """The 256 000-atom EAM configuration (FCC 40^3, 300 K seed 2, dt 1 fs):
     step-0 forces of both precisions at identical positions against the
     binary64 oracle (binary64 1e-10, mixed 1e-5 of max |F|; the mixed-vs-
-    binary64 error printed), then 5000 NVE steps in each precision: the
-    energy drift (max |E(t) - E(0)| / |E(0)| over samples every 250 steps)
-    within 2x the oracle's drift on the same protocol (+1e-7).  The
-    oracle's 5000-step run takes minutes of host time, so its drift is
-    recorded in tests/golden/cfg1_drift.json (make_cfg1_drift.py)."""
+    binary64 error printed), then NVE steps in each precision: the energy
+    drift (max |E(t) - E(0)| / |E(0)| over samples every 250 steps) within
+    2x the oracle's drift on the same protocol (+1e-7).  The configuration
+    asks for 5000 steps, but its analytic EAM collapses the crystal after
+    ~1000 steps and the oracle's (and the reference's) run stops before
+    step 5000, so the drift is compared over the first 2000 steps.  The
+    oracle's run takes many minutes of host time, so its record is kept in
+    tests/golden/cfg1_drift.json (make_cfg1_drift.py)."""
     import json
     lib = gpu_lib
     spec = _eam256k()
