@@ -271,6 +271,17 @@ __device__ double spline_adv(const double *xs, const double *ys, const double *d
     return a * ys[klo] + b * ys[khi] + ((a * a * a - a) * dd[klo] + (b * b * b - b) * dd[khi]) * (h * h) / 6.0;
 }
 
+// 1/x to a few ulps for positive x of binary32 range: a binary32 seed
+// refined by two Newton-Raphson steps r <- r + r (1 - x r), each of which
+// squares the relative error (2^-23 -> 2^-46 -> the binary64 rounding)
+__device__ __forceinline__ double recip_newton(double x)
+{
+    double r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
 // The solver's per-cell arrays: the turi's own (global memory) or copies
 // in shared memory for the duration of the launch.
 struct TtmCells
@@ -316,6 +327,7 @@ __global__ void k_ttm_solve(Geo g, DTuri t, double dt, int staged)
     const int nz = t.dims[2];
     const bool calc_source = fabs(time - p.laser_t0) < p.laser_tdiff;
     const double dte = dt / p.ratio;
+    const double dte_C = dte / p.C_gamma, K_dz2 = p.K / p.dz2;   // type 1
     TtmCells a{t.Te, t.Te2, t.Ti, t.srcz, t.xi, t.Ke, t.Ce, t.Gc, t.num, nullptr};
     if (staged)
     {
@@ -411,8 +423,14 @@ __global__ void k_ttm_solve(Geo g, DTuri t, double dt, int staged)
             const int ihi = (Te[i + 1] < 0) ? i : i + 1;
             double nv;
             if (p.type == 1)
-                nv = te + dte / (p.C_gamma * te) *
-                     (p.K * (Te[ihi] - 2 * te + Te[ilo]) / p.dz2 - p.G * (te - a.Ti[i]) + source);
+            {
+                // dte / (C_gamma te) * (K lap / dz2 - G (te - Ti) + source)
+                // with the constant quotients formed once per launch and one
+                // reciprocal: the substeps are a chain of dependent binary64
+                // operations, and an IEEE division is the longest link
+                const double q = dte_C * recip_newton(te);
+                nv = te + q * (K_dz2 * (Te[ihi] - 2 * te + Te[ilo]) - p.G * (te - a.Ti[i]) + source);
+            }
             else
             {
                 const double KeL = 0.5 * (a.Ke[i] + a.Ke[ilo]);
@@ -476,7 +494,34 @@ int sm_count(int device)
     return cached[device];
 }
 
+__global__ void k_recip_check(const double *x, int n, double *ours, double *ref)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ours[i] = recip_newton(x[i]);
+    ref[i] = 1.0 / x[i];
+}
+
 } // namespace
+
+extern "C" int fmdg_check_recip(fmdg_sys_t *s, const double *x, int n, double *ours, double *ref)
+{
+    if (n < 0) return fmdg_set_error("fmdg_check_recip: negative count");
+    if (n == 0) return FMDG_OK;
+    double *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, (size_t)n * 24);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d, x, (size_t)n * 8, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+    {
+        k_recip_check<<<fmdg_grid(n, 256), 256, 0, s->stream>>>(d, n, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ours, d + n, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ref, d + 2 * (size_t)n, (size_t)n * 8, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(d);
+    return e == cudaSuccess ? FMDG_OK : fmdg_fail("fmdg_check_recip", e);
+}
 
 int fmdg_launch_turi_fields(fmdg_sys_t *s, int k, double dt)
 {

@@ -262,6 +262,9 @@ int fmdg_measure_fma_peak(fmdg_sys_t *s, int fp64, double *tflops);
    kernels (d2f_rn): for n inputs, its results and the conversion
    instruction's */
 int fmdg_check_d2f(fmdg_sys_t *s, const double *x, int n, float *ours, float *ref);
+/* self-check of the TTM solver's binary64 reciprocal (a binary32 seed and
+   two Newton-Raphson steps): for n inputs, its results and 1.0 / x */
+int fmdg_check_recip(fmdg_sys_t *s, const double *x, int n, double *ours, double *ref);
 /* write a buffer larger than L2 so the next kernel starts cold */
 int fmdg_flush_l2(fmdg_sys_t *s);
 

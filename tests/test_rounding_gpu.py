@@ -45,3 +45,28 @@ def test_d2f_matches_conversion(gpu_lib):
     keep = (np.abs(x) >= 2.0 ** -126) | (x == 0.0)
     with np.errstate(over="ignore"):
         np.testing.assert_array_equal(ref[keep].view(np.uint32), x[keep].astype(np.float32).view(np.uint32))
+
+
+def test_ttm_reciprocal_error_bound(gpu_lib):
+    """The TTM solver's reciprocal (binary32 seed, two Newton-Raphson steps)
+    stays within 2 ulps of 1.0 / x over the electron temperatures and heat
+    capacities it meets (1e-3 to 1e9) and across binary32 seed ties."""
+    L = gpu_lib.L
+    L.fmdg_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    L.fmdg_check_recip.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.fmdg_destroy.argtypes = [C.c_void_p]
+    h = C.c_void_p()
+    assert L.fmdg_create(C.byref(h), 0) == 0
+    rng = np.random.default_rng(12)
+    f = rng.uniform(1.0, 2.0, 20000).astype(np.float32)
+    mid = (f.astype(np.float64) + np.nextafter(f, np.float32(np.inf)).astype(np.float64)) / 2.0
+    x = np.concatenate([np.exp(rng.uniform(np.log(1e-3), np.log(1e9), 200000)), rng.uniform(290.0, 3e4, 100000),
+                        mid, np.nextafter(mid, 0.0), [1.0, 2.0, 3.0, 300.0, 1e9]])
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    ours = np.zeros_like(x)
+    ref = np.zeros_like(x)
+    assert L.fmdg_check_recip(h, x.ctypes.data, len(x), ours.ctypes.data, ref.ctypes.data) == 0
+    L.fmdg_destroy(h)
+    np.testing.assert_array_equal(ref, 1.0 / x)
+    ulps = np.abs(ours - ref) / np.spacing(ref)
+    assert ulps.max() <= 2.0, ulps.max()
