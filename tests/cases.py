@@ -96,6 +96,12 @@ def _custom_state():
     return dict(names=["Ar"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def _fine_state():
+    x, v = workloads.fcc_state(12, 12, 12, 5.26, 90.0, MASS["Ar"], seed=43, disp=0.05)
+    v[:, 2] += np.where(x[:, 0] < 31.56, 1.5, -1.5)
+    return dict(names=["Ar"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def write_ttm_tables(work):
     """Synthetic type-2 tables (same two-column layout and units as the
     reference's table files: T in 1e4 K; C in 1e5 J/m^3K; G in 1e17 W/m^3K)."""
@@ -141,6 +147,14 @@ CASES = {
                         run=("integrate", -1, 0.002), steps=20, every=10,
                         turi=dict(cat=0, dims=(2, 2, 3),
                                   fields=["TEMPERATURE", "NUMBER_DENSITY", "VCM", "MASS"])),
+    # a custom turi of 11^3 = 1331 cells over 6912 atoms: more cells than
+    # the per-block shared-memory bins hold, so the field passes add every
+    # run total to the cell directly
+    "turi_fine": dict(box=(63.12, 63.12, 63.12), pbc=(1, 1, 1), names=["Ar"],
+                      pots=[("lj", 0, 0, 3.405, 0.0104, 8.5125)], state=_fine_state,
+                      run=("integrate", -1, 0.002), steps=10, every=5,
+                      turi=dict(cat=0, dims=(11, 11, 11),
+                                fields=["TEMPERATURE", "NUMBER_DENSITY", "VCM", "MASS"])),
     # the reference's own data files (examples/data): the Mishin copper setfl
     # (as examples/02_collision.c:78 loads it) and the type-2 TTM tables of
     # examples/04_ttm2.c:116-160 (Ce_Cu.dat, G_Cu.dat, its Zhigilei K,
