@@ -90,6 +90,11 @@ def _ttm_slab_state():
     return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def _ttm_slab_full_state():
+    x, v = workloads.fcc_state(20, 20, 100, 3.615, 300.0, MASS["Cu"], seed=4, origin=(0.0, 0.0, 20.0))
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def _custom_state():
     x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
     v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
@@ -188,6 +193,23 @@ CASES = {
 }
 
 
+# Full-size cases, kept out of CASES (the per-case golden tests store every
+# atom's state; these goldens hold the turi fields and thermo series only):
+# the TTM configuration's slab at its full 20 x 20 FCC-cell cross-section
+# (160 000 atoms), 120 steps around the pulse at 0.06 ps.
+FULL_CASES = {
+    "ttm_slab_full": dict(box=(20 * 3.615, 20 * 3.615, 100 * 3.615 + 40.0), pbc=(1, 1, 0), names=["Cu"],
+                          pots=[("eam_analytic", 0, 0)], state=_ttm_slab_full_state, run=("integrate", -1, 0.001),
+                          steps=120, every=40,
+                          turi=dict(cat=1, dims=(1, 1, 50), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100,
+                                    frac=0.1, laser=(500.0, 0.0, 0.06e-12, 100e-15, 15e-9))),
+}
+
+
+def case_of(name: str) -> dict:
+    return CASES[name] if name in CASES else FULL_CASES[name]
+
+
 def write_data(workdir: str, data: dict):
     """Write data files (name -> bytes) into the work folder."""
     for fname, raw in data.items():
@@ -204,7 +226,7 @@ def setup(lib: api.Lib, name: str, workdir: str, state: dict | None = None, data
     """Create an FMD instance for case `name` through the fmd.h API and load
     its seeded state.  `data`: the case's data files (name -> bytes), written
     into workdir first.  Returns (md, state)."""
-    case = CASES[name]
+    case = case_of(name)
     if state is None:
         state = case["state"]()
     if data:
@@ -357,7 +379,7 @@ def read_array3(arr, dims, cat):
 
 def run(lib: api.Lib, name: str, md, rec: Recorder | None = None, steps=None):
     """Run the case's dynamics for `steps` time steps (default: the case's)."""
-    case = CASES[name]
+    case = case_of(name)
     r = case["run"]
     n = case["steps"] if steps is None else steps
     dt = r[2]

@@ -12,6 +12,10 @@ Outputs: tests/golden/<case>.npz and tests/golden/bin_<case>.npz.  Cases
 that load the reference's example data files (examples/data: the Mishin
 copper setfl, the type-2 TTM tables) record those files' bytes in their .npz
 (keys data:<file name>), so the tests run without a reference checkout.
+The full-size cases of cases.FULL_CASES (minutes of single-threaded
+reference time each) are generated by name only:
+
+    python tests/golden/make_golden.py ttm_slab_full
 """
 from __future__ import annotations
 
@@ -73,6 +77,32 @@ def golden_case(lib, name, work):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "N0", len(d0["id"]), "N1", len(d1["id"]), "PE0", d0["pe"], "rows", len(rec.rows),
           "errors", rec.errors)
+
+
+def golden_full(lib, name, work):
+    """A full-size case (cases.FULL_CASES): the initial state is regenerated
+    from its seed by the test, so only the observables are kept -- the
+    thermo series, every field-update event with its array, the final TTM
+    state and the atom count."""
+    case = cases.FULL_CASES[name]
+    md, st = cases.setup(lib, name, work)
+    rec = cases.Recorder(lib)
+    rec.record_fields(md, case["turi"]["_handle"])
+    lib.fmd_setEventHandler(md, None, rec.cb)
+    lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+    cases.run(lib, name, md, rec)
+    out = dict(n0=np.array(len(st["x"])), n1=np.array(len(lib.dump(md)["id"])), thermo=np.array(rec.rows),
+               errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2))
+    ev = [(t, tu, f) for (t, tu, f, _) in rec.fields]
+    out["field_events"] = np.array(ev, dtype=np.float64).reshape(-1, 3)
+    for k, (t, tu, f, vals) in enumerate(rec.fields):
+        if vals is not None:
+            out["field_%03d" % k] = vals
+    for kk, vv in lib.ttm_1d(md).items():
+        out["ttm_" + kk] = vv
+    lib.fmd_free(md)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "N", out["n0"], out["n1"], "events", len(ev), "rows", len(rec.rows), "errors", rec.errors)
 
 
 def golden_binning(lib, name, work, rounds=4, seed=99):
@@ -194,6 +224,8 @@ def main():
         for name in names:
             if name == "argon_c":
                 golden_argon_c(work)
+            elif name in cases.FULL_CASES:
+                golden_full(lib, name, work)
             elif name.startswith("bin_"):
                 golden_binning(lib, name[4:], work)
             elif name.startswith("io_"):

@@ -17,8 +17,9 @@ API on the GPU.
   sum |m v|; mixed: centre-of-mass velocity change below 1e-4 A/ps).
 * laser-heated EAM slab with a 1-D TTM grid (20 x 20 x 100 FCC cells =
   160 000 atoms, vacuum above and below, 50 TTM cells along z): 120 steps
-  around the pulse: no error, every active cell's electron temperature
-  finite and above the initial 300 K where the pulse arrives.
+  around the pulse against the compiled reference's run of the same
+  protocol: every field event and array, the final Te, Ti, xi and counts
+  per cell to 1e-10.
 """
 import ctypes as C
 import os
@@ -216,32 +217,51 @@ def test_morse_collision_full_size(gpu_lib, precision):
 
 
 def test_ttm_slab_full_size(gpu_lib):
+    """The TTM configuration's slab at full size (20 x 20 x 100 FCC cells,
+    160 000 atoms, 50 electron cells), 120 binary64 steps around the pulse
+    at 0.06 ps, against the reference run of the same protocol
+    (tests/golden/ttm_slab_full.npz, made by make_golden.py from the
+    compiled reference): the thermo series to 1e-9, every field-update
+    event in order, every field array it carries (Te and the atomic fields)
+    and the final Te, Ti, xi and atom counts per cell to 1e-10 relative; no
+    error event, the electrons heated where the pulse arrives."""
+    from test_parity_golden_gpu import TTM_TOL, FIELD_TOL, _rel
     lib = gpu_lib
-    a = 3.615
-    nx, nz = 20, 100
-    lx, lz = nx * a, nz * a + 40.0
-    x, v = workloads.fcc_state(nx, nx, nz, a, 300.0, 63.546, seed=4, origin=(0.0, 0.0, 20.0))
-    n = len(x)
-    assert n == 160000
-    state = dict(names=["Cu"], kind=np.zeros(n, np.uint32), group=np.zeros(n, np.int32), x=x, v=v)
-    case = dict(box=(lx, lx, lz), pbc=(1, 1, 0), names=["Cu"], pots=[("eam_analytic", 0, 0)],
-                turi=dict(cat=1, dims=(1, 1, 50), gamma=96.6, K=400.0, G=1e17, Te=300.0, ratio=100, frac=0.1,
-                          laser=(500.0, 0.0, 0.06e-12, 100e-15, 15e-9)))
-    cases.CASES["ttm_slab_full"] = dict(case, state=lambda: state, run=("integrate", -1, 0.001), steps=120, every=40)
-    try:
-        with tempfile.TemporaryDirectory() as work:
-            md, _ = cases.setup(lib, "ttm_slab_full", work, state)
-            rec = cases.Recorder(lib)
-            lib.fmd_setEventHandler(md, None, rec.cb)
-            lib.fmd_dync_integrate(md, -1, 0.1195, 0.001)
-            assert rec.errors == [], rec.errors
-            ttm = lib.ttm_1d(md)
-            te = np.asarray(ttm["Te"])
-            active = te >= 0.0
-            assert active.sum() > 10
-            assert np.all(np.isfinite(te[active]))
-            assert te[active].max() > 300.5
-            assert len(lib.dump(md)["id"]) == n
-            lib.fmd_free(md)
-    finally:
-        del cases.CASES["ttm_slab_full"]
+    name = "ttm_slab_full"
+    case = cases.FULL_CASES[name]
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz")))
+    state = case["state"]()
+    assert len(state["x"]) == 160000 == int(g["n0"])
+    with tempfile.TemporaryDirectory() as work:
+        md, _ = cases.setup(lib, name, work, state)
+        rec = cases.Recorder(lib)
+        rec.record_fields(md, case["turi"]["_handle"])
+        lib.fmd_setEventHandler(md, None, rec.cb)
+        lib.fmd_dync_integrate(md, -1, 0.0, case["run"][2])
+        cases.run(lib, name, md, rec)
+        assert rec.errors == [], rec.errors
+        ttm = lib.ttm_1d(md)
+        assert len(lib.dump(md)["id"]) == int(g["n1"])
+        lib.fmd_free(md)
+    # temperature, total and kinetic energy every 40 steps
+    np.testing.assert_allclose(np.array(rec.rows)[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
+    ev = np.array([(t, tu, f) for (t, tu, f, _) in rec.fields]).reshape(-1, 3)
+    np.testing.assert_array_equal(ev[:, 1:], g["field_events"][:, 1:])
+    np.testing.assert_allclose(ev[:, 0], g["field_events"][:, 0], rtol=0, atol=1e-12)
+    worst = {}
+    for k, (t, _, f, vals) in enumerate(rec.fields):
+        key = "field_%03d" % k
+        if key not in g:
+            continue
+        cat = rec.field_cats.get(int(f))
+        e = _rel(vals, g[key])
+        worst[cat] = max(worst.get(cat, 0.0), e)
+        assert e <= (TTM_TOL if cat == api.FMD_FIELD_TTM_TE else FIELD_TOL), (key, t, cat, e)
+    lo, hi = 1, len(g["ttm_Te"]) - 1
+    np.testing.assert_array_equal(ttm["num"][lo:hi], g["ttm_num"][lo:hi])
+    errs = {q: _rel(ttm[q][lo:hi], g["ttm_" + q][lo:hi]) for q in ("Te", "xi", "Ti")}
+    print("TTM slab 160k: field errors by category", worst, "final", errs)
+    assert errs["Te"] <= TTM_TOL and errs["xi"] <= FIELD_TOL and errs["Ti"] <= FIELD_TOL, errs
+    te = np.asarray(ttm["Te"])
+    active = te >= 0.0
+    assert active.sum() > 10 and np.all(np.isfinite(te[active])) and te[active].max() > 300.5
