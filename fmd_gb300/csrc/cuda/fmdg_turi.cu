@@ -16,11 +16,11 @@
 // total is added to the cell as a 64-bit fixed-point integer (integer
 // atomics give the same total whatever order the additions arrive in),
 // first into per-block bins in shared memory, then once per block and cell
-// into the turi.  Scales: mass 2^44 (per kind, exact integer sums),
-// momentum 2^40, thermal kinetic term 2^36 (internal units; resolution
-// 9e-13 and 1.5e-11 per run, far below the binary64 rounding of the
-// reference's own sums relative to the cell totals); a term beyond the
-// fixed-point range sets FMDG_ERRBIT_INTERNAL and is skipped.  These passes
+// into the turi.  Scales: mass 2^48 (per kind, exact integer sums),
+// momentum 2^46, thermal kinetic term 2^42 (internal units; resolution
+// 1.4e-14 and 2.3e-13 per run, near the binary64 rounding of a single
+// atom's term); a term beyond the fixed-point range is skipped and a sum
+// that would wrap is detected, both setting FMDG_ERRBIT_INTERNAL.  These passes
 // are binary64 work on a part whose binary64 pipe is narrow: the run trees
 // cost five adds per value where a lane-by-lane group sum cost 32.
 // The solver runs in one thread block: the grid has tens to hundreds of
@@ -91,11 +91,26 @@ __device__ __forceinline__ T run_sum(T v, int lane, int end)
     return v;
 }
 
-// fixed-point scales of the per-cell sums (powers of two: v * scale is exact)
-constexpr double FX_MASS = 17592186044416.0;   // 2^44
-constexpr double FX_MOM = 1099511627776.0;     // 2^40
-constexpr double FX_KIN = 68719476736.0;       // 2^36
-constexpr double FX_LIMIT = 4.0e18;            // |v * scale| below 2^62: room for the sums
+// Fixed-point scales of the per-cell sums (powers of two: v * scale is
+// exact).  FMD's internal mass unit makes m ~ 0.004-0.007 for argon and
+// copper, m v ~ 1e-2 and m v^2 ~ 1e-2 per atom at room temperature: the
+// scales put one quantum at ~1e-16 of such a term, and a cell total stays
+// below 2^63 up to 1.3e5 (momentum) and 2.1e6 (thermal term) internal
+// units -- 1e5 copper atoms at 20 A/ps, or at ~1e4 K.  A term or a sum
+// beyond the range sets FMDG_ERRBIT_INTERNAL.
+constexpr double FX_MASS = 281474976710656.0;  // 2^48
+constexpr double FX_MOM = 70368744177664.0;    // 2^46
+constexpr double FX_KIN = 4398046511104.0;     // 2^42
+constexpr double FX_LIMIT = 4.0e18;            // |v * scale| below 2^62 for one term
+
+// integer add into a bin (shared or global) with signed-overflow detection
+// from the value the atomic returns
+__device__ __forceinline__ void add_checked(Dyn *dyn, unsigned long long *dst, unsigned long long q)
+{
+    const unsigned long long old = atomicAdd(dst, q);
+    const long long o = (long long)old, a = (long long)q, r = (long long)(old + q);
+    if (((o ^ r) & (a ^ r)) < 0) atomic_or_err(dyn, FMDG_ERRBIT_INTERNAL);
+}
 
 // a run total as a fixed-point term; a term out of range is dropped (0) and
 // sets FMDG_ERRBIT_INTERNAL
@@ -171,9 +186,10 @@ __global__ void __launch_bounds__(TURI_THREADS) k_turi_pass_a(Geo g, DTuri t, do
             for (int d = 0; d < 3; d++) q[1 + d] = fixed_term(dyn, p[d], FX_MOM);
             q[4] = (unsigned long long)(end - lane + 1);
             if (SH)
-                for (int k = 0; k < 5; k++) atomicAdd(&sbin[5 * key + k], q[k]);
+                for (int k = 0; k < 5; k++) add_checked(dyn, &sbin[5 * key + k], q[k]);
             else
-                for (int k = 0; k < 5; k++) atomicAdd(reinterpret_cast<unsigned long long *>(&t.acc[5 * key + k]), q[k]);
+                for (int k = 0; k < 5; k++)
+                    add_checked(dyn, reinterpret_cast<unsigned long long *>(&t.acc[5 * key + k]), q[k]);
         }
     }
     if (bad) atomic_or_err(dyn, FMDG_ERRBIT_TTM);
@@ -181,7 +197,7 @@ __global__ void __launch_bounds__(TURI_THREADS) k_turi_pass_a(Geo g, DTuri t, do
     {
         __syncthreads();
         for (int c = threadIdx.x; c < 5 * t.ncells; c += blockDim.x)
-            if (sbin[c]) atomicAdd(reinterpret_cast<unsigned long long *>(&t.acc[c]), sbin[c]);
+            if (sbin[c]) add_checked(dyn, reinterpret_cast<unsigned long long *>(&t.acc[c]), sbin[c]);
     }
 }
 
@@ -236,15 +252,15 @@ __global__ void __launch_bounds__(TURI_THREADS) k_turi_pass_b(Geo g, DTuri t, do
         if (head && key >= 0)
         {
             const unsigned long long q = fixed_term(dyn, e, FX_KIN);
-            if (SH) atomicAdd(&sbin[key], q);
-            else atomicAdd(reinterpret_cast<unsigned long long *>(&t.tacc[key]), q);
+            if (SH) add_checked(dyn, &sbin[key], q);
+            else add_checked(dyn, reinterpret_cast<unsigned long long *>(&t.tacc[key]), q);
         }
     }
     if (SH)
     {
         __syncthreads();
         for (int c = threadIdx.x; c < t.ncells; c += blockDim.x)
-            if (sbin[c]) atomicAdd(reinterpret_cast<unsigned long long *>(&t.tacc[c]), sbin[c]);
+            if (sbin[c]) add_checked(dyn, reinterpret_cast<unsigned long long *>(&t.tacc[c]), sbin[c]);
     }
 }
 
