@@ -95,6 +95,11 @@ def _ttm_slab_full_state():
     return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def _eam256k_state():
+    x, v = workloads.fcc_state(40, 40, 40, 3.615, 300.0, MASS["Cu"], seed=2)
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def _custom_state():
     x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
     v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
@@ -194,10 +199,15 @@ CASES = {
 
 
 # Full-size cases, kept out of CASES (the per-case golden tests store every
-# atom's state; these goldens hold the turi fields and thermo series only):
-# the TTM configuration's slab at its full 20 x 20 FCC-cell cross-section
-# (160 000 atoms), 120 steps around the pulse at 0.06 ps.
+# atom's state; these goldens hold observables only: the thermo series, the
+# turi fields, and the final state of the atoms with the `sample` lowest
+# ids): the EAM configuration, and the TTM configuration's slab at its full
+# 20 x 20 FCC-cell cross-section (160 000 atoms), 120 steps around the pulse
+# at 0.06 ps.
 FULL_CASES = {
+    # the 256 000-atom EAM configuration (FCC 40^3, 300 K, seed 2), 100 steps
+    "eam256k_full": dict(box=(40 * 3.615,) * 3, pbc=(1, 1, 1), names=["Cu"], pots=[("eam_analytic", 0, 0)],
+                         state=_eam256k_state, run=("integrate", -1, 0.001), steps=100, every=25, sample=2048),
     "ttm_slab_full": dict(box=(20 * 3.615, 20 * 3.615, 100 * 3.615 + 40.0), pbc=(1, 1, 0), names=["Cu"],
                           pots=[("eam_analytic", 0, 0)], state=_ttm_slab_full_state, run=("integrate", -1, 0.001),
                           steps=120, every=40,

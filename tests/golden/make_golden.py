@@ -16,6 +16,7 @@ The full-size cases of cases.FULL_CASES (minutes of single-threaded
 reference time each) are generated by name only:
 
     python tests/golden/make_golden.py ttm_slab_full
+    python tests/golden/make_golden.py eam256k_full
 """
 from __future__ import annotations
 
@@ -82,27 +83,37 @@ def golden_case(lib, name, work):
 def golden_full(lib, name, work):
     """A full-size case (cases.FULL_CASES): the initial state is regenerated
     from its seed by the test, so only the observables are kept -- the
-    thermo series, every field-update event with its array, the final TTM
-    state and the atom count."""
+    thermo series, the potential energy before and after, the final state
+    of the atoms with the lowest ids, every field-update event with its
+    array, the final TTM state and the atom count."""
     case = cases.FULL_CASES[name]
     md, st = cases.setup(lib, name, work)
     rec = cases.Recorder(lib)
-    rec.record_fields(md, case["turi"]["_handle"])
-    lib.fmd_setEventHandler(md, None, rec.cb)
+    if "turi" in case:
+        rec.record_fields(md, case["turi"]["_handle"])
+        lib.fmd_setEventHandler(md, None, rec.cb)
     lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+    pe0 = lib.dump(md)["pe"]
     cases.run(lib, name, md, rec)
-    out = dict(n0=np.array(len(st["x"])), n1=np.array(len(lib.dump(md)["id"])), thermo=np.array(rec.rows),
+    d1 = lib.dump(md)
+    out = dict(n0=np.array(len(st["x"])), n1=np.array(len(d1["id"])), thermo=np.array(rec.rows),
+               s0_pe=np.array(pe0), s1_pe=np.array(d1["pe"]),
                errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2))
-    ev = [(t, tu, f) for (t, tu, f, _) in rec.fields]
-    out["field_events"] = np.array(ev, dtype=np.float64).reshape(-1, 3)
-    for k, (t, tu, f, vals) in enumerate(rec.fields):
-        if vals is not None:
-            out["field_%03d" % k] = vals
-    for kk, vv in lib.ttm_1d(md).items():
-        out["ttm_" + kk] = vv
+    if "sample" in case:
+        sel = np.argsort(d1["id"])[:case["sample"]]
+        out.update(sample_id=d1["id"][sel], sample_x=d1["x"][sel], sample_v=d1["v"][sel], sample_F=d1["F"][sel],
+                   F_absmax=np.array(np.abs(d1["F"]).max()))
+    if "turi" in case:
+        ev = [(t, tu, f) for (t, tu, f, _) in rec.fields]
+        out["field_events"] = np.array(ev, dtype=np.float64).reshape(-1, 3)
+        for k, (t, tu, f, vals) in enumerate(rec.fields):
+            if vals is not None:
+                out["field_%03d" % k] = vals
+        for kk, vv in lib.ttm_1d(md).items():
+            out["ttm_" + kk] = vv
     lib.fmd_free(md)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
-    print(name, "N", out["n0"], out["n1"], "events", len(ev), "rows", len(rec.rows), "errors", rec.errors)
+    print(name, "N", out["n0"], out["n1"], "rows", len(rec.rows), "errors", rec.errors)
 
 
 def golden_binning(lib, name, work, rounds=4, seed=99):

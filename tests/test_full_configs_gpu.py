@@ -9,7 +9,9 @@ API on the GPU.
   oracle's over the first 2000 steps (the configured potential collapses
   the crystal later on), the step-0 potential energy, and the forces
   against the oracle at the positions of step 250 (the configuration starts
-  on exact lattice sites, where the forces vanish).
+  on exact lattice sites, where the forces vanish); 100 binary64 steps
+  against the compiled reference's run (thermo series, energies, final
+  state of 2048 atoms).
 * Morse collision, 512 000-atom slab + a 20 A projectile sphere at 2 km/s,
   periodic x, y, 100 A vacuum in z: step-0 forces against the oracle
   (binary64 1e-10, mixed 1e-5 of max |F|), then 200 steps: no atom lost
@@ -154,6 +156,42 @@ def test_eam256k_full_size(gpu_lib):
     assert abs(ref["energies"][0] - e0_oracle) <= 1e-10 * abs(e0_oracle)
     bound = 2.0 * ref["drift"] + 1e-7
     assert drifts[0] <= bound and drifts[1] <= bound, (drifts, ref["drift"])
+
+
+def test_eam256k_reference_run(gpu_lib):
+    """The 256 000-atom EAM configuration, 100 binary64 steps, against the
+    compiled reference's run of the same protocol
+    (tests/golden/eam256k_full.npz; the test regenerates the seeded state):
+    the thermo series every 25 steps to 1e-9, the potential energy before
+    and after to 1e-10, and the final positions, velocities and forces of
+    the 2048 atoms with the lowest ids (positions within 1e-8 A, velocities
+    to 1e-8 relative, forces to 1e-9 of the largest force)."""
+    lib = gpu_lib
+    name = "eam256k_full"
+    case = cases.FULL_CASES[name]
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz")))
+    state = case["state"]()
+    assert len(state["x"]) == 256000 == int(g["n0"])
+    with tempfile.TemporaryDirectory() as work:
+        md, _ = cases.setup(lib, name, work, state)
+        lib.fmd_dync_integrate(md, -1, 0.0, case["run"][2])
+        pe0 = lib.dump(md)["pe"]
+        rec = cases.Recorder(lib)
+        cases.run(lib, name, md, rec)
+        d1 = lib.dump(md)
+        lib.fmd_free(md)
+    assert rec.errors == [], rec.errors
+    assert len(d1["id"]) == int(g["n1"])
+    np.testing.assert_allclose(np.array(rec.rows)[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
+    assert abs(pe0 - float(g["s0_pe"])) <= 1e-10 * abs(float(g["s0_pe"]))
+    assert abs(d1["pe"] - float(g["s1_pe"])) <= 1e-10 * abs(float(g["s1_pe"]))
+    sel = np.argsort(d1["id"])[:len(g["sample_id"])]
+    np.testing.assert_array_equal(d1["id"][sel], g["sample_id"])
+    dx = np.abs(d1["x"][sel] - g["sample_x"]).max()
+    dv = np.abs(d1["v"][sel] - g["sample_v"]).max() / np.abs(g["sample_v"]).max()
+    dF = np.abs(d1["F"][sel] - g["sample_F"]).max() / float(g["F_absmax"])
+    print("EAM 256k vs the reference after 100 steps: dx %.2e A, dv %.2e, dF %.2e" % (dx, dv, dF))
+    assert dx <= 1e-8 and dv <= 1e-8 and dF <= 1e-9, (dx, dv, dF)
 
 
 def _collision(seed=3):
