@@ -100,6 +100,30 @@ def _eam256k_state():
     return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
 
 
+def collision_atoms(seed=3):
+    """The Morse collision configuration: an 80 x 80 x 20 FCC copper slab
+    (300 K) and a projectile of the FCC sites within 20 A of a point 25 A
+    above it, moving at -2 km/s along z; returns (box, x, v)."""
+    a = 3.615
+    lx = 80 * a
+    x, v = workloads.fcc_state(80, 80, 20, a, 300.0, MASS["Cu"], seed=seed, origin=(0.0, 0.0, 2.0))
+    top = 2.0 + 20 * a
+    lz = 20 * a + 100.0
+    c = np.array([lx / 2, lx / 2, top + 25.0])
+    n = 13
+    sph = workloads.fcc_sites(n, n, n, a, origin=tuple(c - n * a / 2))
+    sph = sph[np.linalg.norm(sph - c, axis=1) <= 20.0]
+    rng = np.random.default_rng(seed + 1)
+    vs = workloads.maxwell_velocities(len(sph), MASS["Cu"], 300.0, rng)
+    vs[:, 2] -= 20.0                      # -2 km/s (src/general.h:40: 1e-2 A/ps per m/s)
+    return (lx, lx, lz), np.concatenate([x, sph]), np.concatenate([v, vs])
+
+
+def _collision_state():
+    _, x, v = collision_atoms()
+    return dict(names=["Cu"], kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), x=x, v=v)
+
+
 def _custom_state():
     x, v = workloads.fcc_state(8, 8, 8, 5.26, 90.0, MASS["Ar"], seed=42, disp=0.05)
     v[:, 2] += np.where(x[:, 0] < 21.04, 1.5, -1.5)
@@ -208,6 +232,10 @@ FULL_CASES = {
     # the 256 000-atom EAM configuration (FCC 40^3, 300 K, seed 2), 100 steps
     "eam256k_full": dict(box=(40 * 3.615,) * 3, pbc=(1, 1, 1), names=["Cu"], pots=[("eam_analytic", 0, 0)],
                          state=_eam256k_state, run=("integrate", -1, 0.001), steps=100, every=25, sample=2048),
+    # the Morse collision configuration (515 000 atoms, open z), 100 steps
+    "morse_collision_full": dict(box=(80 * 3.615, 80 * 3.615, 20 * 3.615 + 100.0), pbc=(1, 1, 0), names=["Cu"],
+                                 pots=[("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)], state=_collision_state,
+                                 run=("integrate", -1, 0.001), steps=100, every=25, sample=2048, spread=True),
     "ttm_slab_full": dict(box=(20 * 3.615, 20 * 3.615, 100 * 3.615 + 40.0), pbc=(1, 1, 0), names=["Cu"],
                           pots=[("eam_analytic", 0, 0)], state=_ttm_slab_full_state, run=("integrate", -1, 0.001),
                           steps=120, every=40,

@@ -17,6 +17,7 @@ reference time each) are generated by name only:
 
     python tests/golden/make_golden.py ttm_slab_full
     python tests/golden/make_golden.py eam256k_full
+    python tests/golden/make_golden.py morse_collision_full
 """
 from __future__ import annotations
 
@@ -100,7 +101,11 @@ def golden_full(lib, name, work):
                s0_pe=np.array(pe0), s1_pe=np.array(d1["pe"]),
                errors=np.array(rec.errors, dtype=np.int64).reshape(-1, 2))
     if "sample" in case:
-        sel = np.argsort(d1["id"])[:case["sample"]]
+        order = np.argsort(d1["id"])
+        if case.get("spread"):      # ids spread over the whole range
+            sel = order[np.unique(np.linspace(0, len(order) - 1, case["sample"]).astype(np.int64))]
+        else:                       # the lowest ids
+            sel = order[:case["sample"]]
         out.update(sample_id=d1["id"][sel], sample_x=d1["x"][sel], sample_v=d1["v"][sel], sample_F=d1["F"][sel],
                    F_absmax=np.array(np.abs(d1["F"]).max()))
     if "turi" in case:

@@ -16,7 +16,8 @@ API on the GPU.
   periodic x, y, 100 A vacuum in z: step-0 forces against the oracle
   (binary64 1e-10, mixed 1e-5 of max |F|), then 200 steps: no atom lost
   before the impact, transverse momentum conserved (binary64: to 1e-9 of
-  sum |m v|; mixed: centre-of-mass velocity change below 1e-4 A/ps).
+  sum |m v|; mixed: centre-of-mass velocity change below 1e-4 A/ps); 100
+  binary64 steps against the compiled reference's run of the same protocol.
 * laser-heated EAM slab with a 1-D TTM grid (20 x 20 x 100 FCC cells =
   160 000 atoms, vacuum above and below, 50 TTM cells along z): 120 steps
   around the pulse against the compiled reference's run of the same
@@ -158,20 +159,17 @@ def test_eam256k_full_size(gpu_lib):
     assert drifts[0] <= bound and drifts[1] <= bound, (drifts, ref["drift"])
 
 
-def test_eam256k_reference_run(gpu_lib):
-    """The 256 000-atom EAM configuration, 100 binary64 steps, against the
-    compiled reference's run of the same protocol
-    (tests/golden/eam256k_full.npz; the test regenerates the seeded state):
-    the thermo series every 25 steps to 1e-9, the potential energy before
-    and after to 1e-10, and the final positions, velocities and forces of
-    the 2048 atoms with the lowest ids (positions within 1e-8 A, velocities
-    to 1e-8 relative, forces to 1e-9 of the largest force)."""
-    lib = gpu_lib
-    name = "eam256k_full"
+def _reference_run(lib, name, n_expect):
+    """Run full-size case `name` (cases.FULL_CASES) in binary64 and compare
+    it with the compiled reference's run of the same protocol
+    (tests/golden/<name>.npz; the seeded state is regenerated here): the
+    thermo series to 1e-9, the potential energy before and after to 1e-10,
+    and the final positions (1e-8 A), velocities (1e-8 relative) and forces
+    (1e-9 of the largest) of the sampled atoms.  Returns the deviations."""
     case = cases.FULL_CASES[name]
     g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz")))
     state = case["state"]()
-    assert len(state["x"]) == 256000 == int(g["n0"])
+    assert len(state["x"]) == n_expect == int(g["n0"])
     with tempfile.TemporaryDirectory() as work:
         md, _ = cases.setup(lib, name, work, state)
         lib.fmd_dync_integrate(md, -1, 0.0, case["run"][2])
@@ -185,32 +183,35 @@ def test_eam256k_reference_run(gpu_lib):
     np.testing.assert_allclose(np.array(rec.rows)[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
     assert abs(pe0 - float(g["s0_pe"])) <= 1e-10 * abs(float(g["s0_pe"]))
     assert abs(d1["pe"] - float(g["s1_pe"])) <= 1e-10 * abs(float(g["s1_pe"]))
-    sel = np.argsort(d1["id"])[:len(g["sample_id"])]
-    np.testing.assert_array_equal(d1["id"][sel], g["sample_id"])
+    pos = np.empty(int(d1["id"].max()) + 1, np.int64)
+    pos[d1["id"]] = np.arange(len(d1["id"]))
+    sel = pos[g["sample_id"]]
     dx = np.abs(d1["x"][sel] - g["sample_x"]).max()
     dv = np.abs(d1["v"][sel] - g["sample_v"]).max() / np.abs(g["sample_v"]).max()
     dF = np.abs(d1["F"][sel] - g["sample_F"]).max() / float(g["F_absmax"])
-    print("EAM 256k vs the reference after 100 steps: dx %.2e A, dv %.2e, dF %.2e" % (dx, dv, dF))
+    print("%s vs the reference after %d steps: dx %.2e A, dv %.2e, dF %.2e" % (name, case["steps"], dx, dv, dF))
     assert dx <= 1e-8 and dv <= 1e-8 and dF <= 1e-9, (dx, dv, dF)
+    return dx, dv, dF
+
+
+def test_eam256k_reference_run(gpu_lib):
+    """The 256 000-atom EAM configuration, 100 binary64 steps, against the
+    compiled reference's run of the same protocol (`_reference_run`; the
+    2048 atoms with the lowest ids sampled)."""
+    _reference_run(gpu_lib, "eam256k_full", 256000)
+
+
+def test_morse_collision_reference_run(gpu_lib):
+    """The Morse collision configuration (515 000 atoms, open z), 100
+    binary64 steps, against the compiled reference's run of the same
+    protocol (`_reference_run`; 2048 atoms sampled across the id range,
+    slab and projectile)."""
+    _reference_run(gpu_lib, "morse_collision_full", len(cases.FULL_CASES["morse_collision_full"]["state"]()["x"]))
 
 
 def _collision(seed=3):
-    a = 3.615
-    lx = 80 * a
-    x, v = workloads.fcc_state(80, 80, 20, a, 300.0, 63.546, seed=seed, origin=(0.0, 0.0, 2.0))
-    top = 2.0 + 20 * a
-    lz = 20 * a + 100.0
-    # projectile: FCC sites within 20 A of a centre 25 A above the slab
-    c = np.array([lx / 2, lx / 2, top + 25.0])
-    n = 13
-    sph = workloads.fcc_sites(n, n, n, a, origin=tuple(c - n * a / 2))
-    sph = sph[np.linalg.norm(sph - c, axis=1) <= 20.0]
-    rng = np.random.default_rng(seed + 1)
-    vs = workloads.maxwell_velocities(len(sph), 63.546, 300.0, rng)
-    vs[:, 2] -= 20.0                      # -2 km/s (src/general.h:40: 1e-2 A/ps per m/s)
-    x = np.concatenate([x, sph])
-    v = np.concatenate([v, vs])
-    return dict(box=(lx, lx, lz), pbc=(1, 1, 0), kinds=[("Cu", 63.546)],
+    box, x, v = cases.collision_atoms(seed)
+    return dict(box=box, pbc=(1, 1, 0), kinds=[("Cu", 63.546)],
                 pots=[("morse", 0, 0, 0.3429, 1.3588, 2.866, 8.0)], x=x, v=v,
                 kind=np.zeros(len(x), np.uint32), group=np.zeros(len(x), np.int32), dt=0.001)
 
