@@ -17,6 +17,10 @@
  *   group thermodynamics ................. src/matter.c:31-68
  *   natural cubic spline ................. src/cspline.h:26-27, src/cspline.c:50-74
  *   setfl loading, r -> r^2 resampling ... src/eam.c:324-480
+ *   turi fields (number, mass, vcm, T) .. src/turi.c:959-1335
+ *   TTM activation, types 1 and 2, xi .... src/ttm.c:154-383, src/turi.c:1337-1373
+ *   TTM friction term .................... src/forces.c:292-330, :376-378
+ *   symplectic Euler ..................... src/integrators.c:129-225
  * Ghost cells are not materialised: a neighbour cell across a periodic face
  * is the interior cell on the far side with its positions shifted by +/- l,
  * and the partial force of that image is added to its owner directly (the
@@ -46,6 +50,18 @@ typedef struct
     unsigned *kind, *id;
 } ocell_t;
 
+/* a 1-D TTM turi (one cell across x and y) */
+typedef struct
+{
+    int on;
+    oracle_ttm_params_t p;
+    double *tabs;              /* owned copies of the type-2 tables */
+    int nz, g2l, lo, hi;       /* local cells incl. margins; itc = (int)(z/h) + g2l; interior [lo, hi) */
+    double tcellh, vol, start, stop;
+    unsigned *num;
+    double *mass, *vcm, *Ti, *Te, *Te2, *xi, *Ke, *Ce, *Gc;
+} ottm_t;
+
 struct oracle_sys
 {
     double l[3], cellh[3];
@@ -69,6 +85,8 @@ struct oracle_sys
     int nthreads;
     /* flat indexing for accumulation buffers */
     int *start;
+    double time, dt;           /* simulation time and step of the TTM runs */
+    ottm_t ttm;
 };
 
 /* ------------------------------------------------------------ cells */
@@ -151,10 +169,18 @@ oracle_sys_t *oracle_create(void)
     return o;
 }
 
+static void free_ttm(ottm_t *t)
+{
+    free(t->tabs); free(t->num); free(t->mass); free(t->vcm); free(t->Ti); free(t->Te); free(t->Te2);
+    free(t->xi); free(t->Ke); free(t->Ce); free(t->Gc);
+    memset(t, 0, sizeof *t);
+}
+
 void oracle_destroy(oracle_sys_t *o)
 {
     if (!o) return;
     free_grid(o);
+    free_ttm(&o->ttm);
     free(o->F); free(o->FDD); free(o->rho); free(o->rhoDD); free(o->phi); free(o->phiDD);
     free(o);
 }
@@ -723,6 +749,268 @@ static double run_pass(oracle_sys_t *o, int pass, int group, double *F, double *
     return pe;
 }
 
+/* ------------------------------------------------------------ TTM */
+
+/* src/turi.c:38-42 */
+static int ttm_window(const oracle_sys_t *o)
+{
+    const ottm_t *t = &o->ttm;
+    return (o->time >= t->start - o->dt / 2.0) && ((o->time < t->stop + o->dt / 2.0) || t->stop < t->start);
+}
+
+/* local turi cell of a position (truncation, src/turi.c:971-973); a cell
+   outside the local grid sets error bit 4 and is clamped */
+static int ttm_cell(oracle_sys_t *o, const double *x)
+{
+    const ottm_t *t = &o->ttm;
+    int c = (int)(x[2] / t->tcellh) + t->g2l;
+    if (c < 0 || c >= t->nz)
+    {
+        o->err |= 4u;
+        c = c < 0 ? 0 : t->nz - 1;
+    }
+    return c;
+}
+
+/* F_z += xi m (v_z - vcm_z) of the atom's cell (src/forces.c:292-330) */
+static void ttm_friction(oracle_sys_t *o, int group)
+{
+    ottm_t *t = &o->ttm;
+    for (int c = 0; c < o->ncell; c++)
+    {
+        ocell_t *cl = icell(o, c);
+        for (int i = 0; i < cl->n; i++)
+        {
+            if (group >= 0 && cl->group[i] != group) continue;
+            const int k = ttm_cell(o, cl->x + 3 * i);
+            cl->F[3 * i + 2] += t->xi[k] * o->mass[cl->kind[i]] * (cl->v[3 * i + 2] - t->vcm[3 * k + 2]);
+        }
+    }
+}
+
+/* mass, vcm, number and temperature of every turi cell (src/turi.c:1112-1178,
+   1190-1261): sums over all atoms of the interior cells, vcm = sum m v / M,
+   T = sum m |v - vcm|^2 / (3 k_B N) */
+static void ttm_fields(oracle_sys_t *o)
+{
+    ottm_t *t = &o->ttm;
+    for (int k = t->lo; k < t->hi; k++)
+    {
+        t->mass[k] = 0.0;
+        t->Ti[k] = 0.0;
+        t->num[k] = 0;
+        for (int d = 0; d < 3; d++) t->vcm[3 * k + d] = 0.0;
+    }
+    for (int c = 0; c < o->ncell; c++)
+    {
+        ocell_t *cl = icell(o, c);
+        for (int i = 0; i < cl->n; i++)
+        {
+            const int k = ttm_cell(o, cl->x + 3 * i);
+            const double m = o->mass[cl->kind[i]];
+            t->mass[k] += m;
+            for (int d = 0; d < 3; d++) t->vcm[3 * k + d] += m * cl->v[3 * i + d];
+        }
+    }
+    for (int k = t->lo; k < t->hi; k++)
+        for (int d = 0; d < 3; d++) t->vcm[3 * k + d] /= t->mass[k];
+    for (int c = 0; c < o->ncell; c++)
+    {
+        ocell_t *cl = icell(o, c);
+        for (int i = 0; i < cl->n; i++)
+        {
+            const int k = ttm_cell(o, cl->x + 3 * i);
+            const double m = o->mass[cl->kind[i]];
+            double vt2 = 0.0;
+            for (int d = 0; d < 3; d++)
+            {
+                const double vt = cl->v[3 * i + d] - t->vcm[3 * k + d];
+                vt2 += vt * vt;
+            }
+            t->Ti[k] += m * vt2;
+            t->num[k]++;
+        }
+    }
+    for (int k = t->lo; k < t->hi; k++) t->Ti[k] /= (3.0 * K_B * t->num[k]);
+}
+
+/* natural spline on tabulated knots, bisection as src/cspline.h:29-44 */
+static double table_spline(const double *xs, const double *ys, const double *dd, int n, double x)
+{
+    int klo = 0, khi = n - 1;
+    while (khi - klo > 1)
+    {
+        const int k = (khi + klo) >> 1;
+        if (xs[k] > x) khi = k;
+        else klo = k;
+    }
+    const double h = xs[khi] - xs[klo];
+    const double a = (xs[khi] - x) / h, b = (x - xs[klo]) / h;
+    return SVAL(a, b, ys, klo, khi, dd, h);
+}
+
+/* type 2: C, K (Zhigilei) and G of the active cells (src/ttm.c:154-192) */
+static void ttm_type2_coeffs(oracle_sys_t *o)
+{
+    ottm_t *t = &o->ttm;
+    const oracle_ttm_params_t *p = &t->p;
+    for (int i = t->lo; i < t->hi; i++)
+    {
+        const double te = t->Te[i];
+        if (te < 0.0) continue;
+        if (te < p->T_C[0] || te > p->T_C[p->nC - 1]) o->err |= 16u;
+        t->Ce[i] = table_spline(p->T_C, p->Ct, p->C_DD, p->nC, te);
+        t->Ke[i] = 1. / 3. * t->Ce[i] * p->Kzh_v2 / (p->Kzh_A * (te * te) + p->Kzh_B * t->Ti[i]);
+        if (te < p->T_G[0] || te > p->T_G[p->nG - 1]) o->err |= 16u;
+        t->Gc[i] = table_spline(p->T_G, p->Gt, p->G_DD, p->nG, te);
+    }
+}
+
+/* cell deactivation below min_atoms, activation from the count-weighted
+   neighbour average, xi reset (src/ttm.c:194-248) */
+static void ttm_presolve(oracle_sys_t *o)
+{
+    ottm_t *t = &o->ttm;
+    for (int i = t->lo; i < t->hi; i++)
+    {
+        t->xi[i] = 0.0;
+        if (t->Te[i] < 0.0 && t->num[i] >= t->p.min_atoms)
+        {
+            int count = 0;
+            double sum = 0.0;
+            const int im1 = (i == t->lo) ? 0 : i - 1;
+            if (t->Te[im1] >= 0.0) { sum += t->Te[im1] * t->num[im1]; count += t->num[im1]; }
+            if (t->Te[i + 1] >= 0.0) { sum += t->Te[i + 1] * t->num[i + 1]; count += t->num[i + 1]; }
+            t->Te[i] = (count > 0) ? sum / count : t->Ti[i];
+        }
+        if (t->num[i] < t->p.min_atoms) t->Te[i] = t->Te2[i] = -1.0;
+    }
+    if (t->p.type == 2) ttm_type2_coeffs(o);
+}
+
+/* `ratio` explicit substeps with Neumann reflection at inactive neighbours
+   and the Gaussian source, then xi (src/ttm.c:250-383) */
+static void ttm_solve(oracle_sys_t *o)
+{
+    ottm_t *t = &o->ttm;
+    const oracle_ttm_params_t *p = &t->p;
+    const int calc_source = fabs(o->time - p->laser_t0) < p->laser_tdiff;
+    const double dte = o->dt / p->ratio;
+    for (int j = 0; j < p->ratio; j++)
+    {
+        double spc = 0.0;
+        if (calc_source)
+        {
+            const double tt = o->time + j * dte - p->laser_t0;
+            spc = p->laser_factor * exp(p->laser_m_2sig2_inv * (tt * tt));
+        }
+        for (int i = t->lo; i < t->hi; i++)
+        {
+            const double te = t->Te[i];
+            if (te < 0) continue;
+            double source = 0.0;
+            if (calc_source)
+            {
+                const double z = (i - t->g2l + 0.5) * t->tcellh;
+                source = spc * exp(p->laser_m_absdepth_inv * (z - p->frontsurf));
+            }
+            const int im1 = (i == t->lo) ? 0 : i - 1;
+            const int ilo = (t->Te[im1] < 0) ? i : im1;
+            const int ihi = (t->Te[i + 1] < 0) ? i : i + 1;
+            if (p->type == 1)
+                t->Te2[i] = te + dte / (p->C_gamma * te) *
+                            (p->K * (t->Te[ihi] - 2 * te + t->Te[ilo]) / p->dz2 - p->G * (te - t->Ti[i]) + source);
+            else
+            {
+                const double KeL = 0.5 * (t->Ke[i] + t->Ke[ilo]);
+                const double KeR = 0.5 * (t->Ke[i] + t->Ke[ihi]);
+                t->Te2[i] = te + dte / t->Ce[i] *
+                            ((KeR * (t->Te[ihi] - te) - KeL * (te - t->Te[ilo])) / p->dz2 -
+                             t->Gc[i] * (te - t->Ti[i]) + source);
+            }
+            t->xi[i] += t->Te2[i];
+        }
+        double *tmp = t->Te2;
+        t->Te2 = t->Te;
+        t->Te = tmp;
+        if (p->type == 2 && j < p->ratio - 1) ttm_type2_coeffs(o);
+    }
+    for (int i = t->lo; i < t->hi; i++)
+        if (t->num[i] >= p->min_atoms)
+        {
+            const double Gi = (p->type == 1) ? p->G : t->Gc[i];
+            t->xi[i] = Gi * t->vol * (t->xi[i] / p->ratio - t->Ti[i]) / (3 * K_B * t->num[i] * t->Ti[i]);
+        }
+}
+
+int oracle_ttm_setup(oracle_sys_t *o, int nz, int g2l_z, int lo, int hi, double tcellh_z, double tcell_volume,
+                     double starttime, double stoptime, const oracle_ttm_params_t *p, double Te_init)
+{
+    if (nz < 3 || lo < 1 || hi > nz - 1 || lo >= hi || p->ratio < 1 || (p->type != 1 && p->type != 2)) return -1;
+    ottm_t *t = &o->ttm;
+    free_ttm(t);
+    t->p = *p;
+    if (p->type == 2)
+    {
+        const int nc = p->nC, ng = p->nG;
+        if (nc < 2 || ng < 2) return -1;
+        t->tabs = (double *)malloc(sizeof(double) * 3 * (size_t)(nc + ng));
+        double *q = t->tabs;
+        memcpy(q, p->T_C, sizeof(double) * nc); t->p.T_C = q; q += nc;
+        memcpy(q, p->Ct, sizeof(double) * nc); t->p.Ct = q; q += nc;
+        memcpy(q, p->C_DD, sizeof(double) * nc); t->p.C_DD = q; q += nc;
+        memcpy(q, p->T_G, sizeof(double) * ng); t->p.T_G = q; q += ng;
+        memcpy(q, p->Gt, sizeof(double) * ng); t->p.Gt = q; q += ng;
+        memcpy(q, p->G_DD, sizeof(double) * ng); t->p.G_DD = q;
+    }
+    t->nz = nz; t->g2l = g2l_z; t->lo = lo; t->hi = hi;
+    t->tcellh = tcellh_z; t->vol = tcell_volume; t->start = starttime; t->stop = stoptime;
+    t->num = (unsigned *)calloc(nz, sizeof(unsigned));
+    t->mass = (double *)calloc(nz, sizeof(double));
+    t->vcm = (double *)calloc(3 * (size_t)nz, sizeof(double));
+    t->Ti = (double *)calloc(nz, sizeof(double));
+    t->Te = (double *)malloc(sizeof(double) * nz);
+    t->Te2 = (double *)malloc(sizeof(double) * nz);
+    t->xi = (double *)calloc(nz, sizeof(double));
+    t->Ke = (double *)calloc(nz, sizeof(double));
+    t->Ce = (double *)calloc(nz, sizeof(double));
+    t->Gc = (double *)calloc(nz, sizeof(double));
+    for (int i = 0; i < nz; i++) t->Te[i] = t->Te2[i] = (i >= lo && i < hi) ? Te_init : -1.0;
+    t->on = 1;
+    return 0;
+}
+
+int oracle_set_time(oracle_sys_t *o, double time, double dt)
+{
+    o->time = time;
+    o->dt = dt;
+    return 0;
+}
+
+int oracle_turi_update(oracle_sys_t *o)
+{
+    if (!o->ttm.on || !ttm_window(o)) return 0;
+    ttm_fields(o);
+    ttm_presolve(o);
+    ttm_solve(o);
+    return 0;
+}
+
+int oracle_ttm_1d(oracle_sys_t *o, unsigned *num, double *vcm, double *Ti, double *Te, double *xi)
+{
+    const ottm_t *t = &o->ttm;
+    if (!t->on) return -1;
+    for (int i = 0; i < t->nz; i++)
+    {
+        if (num) num[i] = t->num[i];
+        if (Ti) Ti[i] = t->Ti[i];
+        if (Te) Te[i] = t->Te[i];
+        if (xi) xi[i] = t->xi[i];
+        if (vcm) for (int d = 0; d < 3; d++) vcm[3 * i + d] = t->vcm[3 * i + d];
+    }
+    return t->nz;
+}
+
 /* src/forces.c:332-382 */
 int oracle_compute_forces(oracle_sys_t *o, int group)
 {
@@ -772,6 +1060,7 @@ int oracle_compute_forces(oracle_sys_t *o, int group)
     o->th.virial = vir;
     free(F);
     free(va);
+    if (o->ttm.on && ttm_window(o)) ttm_friction(o, group);
     return 0;
 }
 
@@ -849,6 +1138,37 @@ int oracle_vv_steps(oracle_sys_t *o, int nsteps, double dt, int group, int therm
             }
         }
         group_sums(o, group);
+    }
+    return 0;
+}
+
+/* symplectic Euler under TTM coupling (src/integrators.c:129-225): v += dt
+   F / m, x += dt v, refresh, group sums; time += dt; the turi fields and
+   the TTM solve; forces with the friction term */
+int oracle_se_steps(oracle_sys_t *o, int nsteps, double dt, int group)
+{
+    o->dt = dt;
+    for (int s = 0; s < nsteps; s++)
+    {
+        for (int c = 0; c < o->ncell; c++)
+        {
+            ocell_t *cl = icell(o, c);
+            for (int i = 0; i < cl->n; i++)
+            {
+                if (group >= 0 && cl->group[i] != group) continue;
+                const double m = o->mass[cl->kind[i]];
+                for (int d = 0; d < 3; d++)
+                {
+                    cl->v[3 * i + d] += dt * cl->F[3 * i + d] / m;
+                    cl->x[3 * i + d] += dt * cl->v[3 * i + d];
+                }
+            }
+        }
+        if (oracle_refresh(o) != 0) return -1;
+        group_sums(o, group);
+        o->time += dt;
+        oracle_turi_update(o);
+        oracle_compute_forces(o, group);
     }
     return 0;
 }

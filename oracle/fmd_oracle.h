@@ -9,7 +9,9 @@
  * same binary64 arithmetic: per-cell atom lists with swap-remove refresh and
  * periodic migration, half-shell cell-pair loops with Newton's third law,
  * LJ / Morse / EAM (r^2-grid cubic splines) / hybrid pair updates, velocity
- * Verlet with Berendsen scaling, group thermodynamics.  Ghost cells are
+ * Verlet with Berendsen scaling, group thermodynamics, and the 1-D
+ * two-temperature model (turi fields, electron solver types 1 and 2,
+ * friction term, symplectic Euler).  Ghost cells are
  * represented by image shifts of the interior cells.  Parity pins: the
  * golden vectors in tests/golden/ were produced by the reference compiled
  * from its own sources; tests/test_oracle_cpu.py checks this restatement
@@ -69,6 +71,38 @@ int oracle_thermo(oracle_sys_t *o, int group, oracle_thermo_t *out);
 int oracle_vv_steps(oracle_sys_t *o, int nsteps, double dt, int group, int thermostat, double tau, double T0);
 int oracle_get_thermo(oracle_sys_t *o, oracle_thermo_t *out);
 unsigned oracle_errors(oracle_sys_t *o);
+
+/* 1-D two-temperature model (src/ttm.c, src/turi.c, src/forces.c:292-330,
+   src/integrators.c:129-225).  The parameters are the reference's derived
+   ones (what its fmd_ttm_set* calls and _fmd_ttm_getReady leave in its
+   ttm_t): heat capacity / conductivity / coupling in internal units, laser
+   constants, the activation threshold and the front surface. */
+typedef struct
+{
+    int type;                 /* 1: C = gamma Te, constant K and G; 2: tabulated C(Te), G(Te), Zhigilei K */
+    int ratio;                /* TTM substeps per MD step */
+    unsigned min_atoms;       /* cells with fewer atoms are inactive */
+    int nC, nG;
+    double C_gamma, K, G, dz2, frontsurf;
+    double laser_t0, laser_tdiff, laser_m_2sig2_inv, laser_m_absdepth_inv, laser_factor;
+    double Kzh_v2, Kzh_A, Kzh_B;
+    const double *T_C, *Ct, *C_DD, *T_G, *Gt, *G_DD;
+} oracle_ttm_params_t;
+
+/* a turi of one cell across x and y and nz local cells along z (margins
+   included), itc_z = (int)(z / tcellh_z) + g2l_z; interior [lo, hi); the
+   electron temperature starts at Te_init in the interior, -1 elsewhere */
+int oracle_ttm_setup(oracle_sys_t *o, int nz, int g2l_z, int lo, int hi, double tcellh_z, double tcell_volume,
+                     double starttime, double stoptime, const oracle_ttm_params_t *p, double Te_init);
+int oracle_set_time(oracle_sys_t *o, double time, double dt);
+/* the turi fields and the TTM solve at the current time (a run's first
+   update, src/integrators.c:187-189), when within the turi's window */
+int oracle_turi_update(oracle_sys_t *o);
+/* symplectic Euler steps, each followed by the turi update and the forces
+   with the TTM friction term (src/integrators.c:129-225) */
+int oracle_se_steps(oracle_sys_t *o, int nsteps, double dt, int group);
+/* the 1-D arrays (nz entries each; vcm 3 per cell) */
+int oracle_ttm_1d(oracle_sys_t *o, unsigned *num, double *vcm, double *Ti, double *Te, double *xi);
 
 #ifdef __cplusplus
 }

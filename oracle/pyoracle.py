@@ -20,6 +20,16 @@ class PairT(C.Structure):
     _fields_ = [("cat", C.c_int), ("iloc", C.c_int), ("jloc", C.c_int), ("pad", C.c_int), ("p", C.c_double * 4)]
 
 
+class TtmParamsT(C.Structure):
+    """oracle_ttm_params_t"""
+    _fields_ = [("type", C.c_int), ("ratio", C.c_int), ("min_atoms", C.c_uint), ("nC", C.c_int), ("nG", C.c_int),
+                ("C_gamma", C.c_double), ("K", C.c_double), ("G", C.c_double), ("dz2", C.c_double),
+                ("frontsurf", C.c_double), ("laser_t0", C.c_double), ("laser_tdiff", C.c_double),
+                ("laser_m_2sig2_inv", C.c_double), ("laser_m_absdepth_inv", C.c_double),
+                ("laser_factor", C.c_double), ("Kzh_v2", C.c_double), ("Kzh_A", C.c_double), ("Kzh_B", C.c_double),
+                ("T_C", P), ("Ct", P), ("C_DD", P), ("T_G", P), ("Gt", P), ("G_DD", P)]
+
+
 class ThermoT(C.Structure):
     _fields_ = [("kinetic", C.c_double), ("temperature", C.c_double), ("momentum", C.c_double * 3),
                 ("potential", C.c_double), ("count", C.c_double), ("virial", C.c_double)]
@@ -48,7 +58,12 @@ def _lib():
                        ("oracle_refresh", [P]), ("oracle_compute_forces", [P, C.c_int]),
                        ("oracle_thermo", [P, C.c_int, P]),
                        ("oracle_vv_steps", [P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double, C.c_double]),
-                       ("oracle_get_thermo", [P, P]), ("oracle_errors", [P])]:
+                       ("oracle_get_thermo", [P, P]), ("oracle_errors", [P]),
+                       ("oracle_ttm_setup", [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                             C.c_double, C.c_double, P, C.c_double]),
+                       ("oracle_set_time", [P, C.c_double, C.c_double]), ("oracle_turi_update", [P]),
+                       ("oracle_se_steps", [P, C.c_int, C.c_double, C.c_int]),
+                       ("oracle_ttm_1d", [P, P, P, P, P, P])]:
         f = getattr(L, name)
         f.argtypes = args
         f.restype = C.c_uint if name == "oracle_errors" else (None if name == "oracle_destroy" else C.c_int)
@@ -167,3 +182,43 @@ class Oracle:
 
     def errors(self):
         return self.L.oracle_errors(self.o)
+
+    # ---- 1-D two-temperature model --------------------------------------
+    def ttm_setup(self, pd, pk, Te_init, tables=None):
+        """The reference's derived TTM parameters as a golden file records
+        them (tests/golden/make_golden.py ttm_params): pd = C_gamma, K, G,
+        dz2, frontsurf, laser_t0, laser_tdiff, laser_m_2sig2_inv,
+        laser_m_absdepth_inv, laser_factor, Kzh v2, A, B, tcell_volume,
+        starttime, stoptime, tcellh_z; pk = type, ratio, min_atoms, nC, nG,
+        itc_start, itc_stop, nz, itc_glob_to_loc (z)."""
+        q = TtmParamsT()
+        q.type, q.ratio, q.min_atoms = int(pk[0]), int(pk[1]), int(pk[2])
+        (q.C_gamma, q.K, q.G, q.dz2, q.frontsurf, q.laser_t0, q.laser_tdiff, q.laser_m_2sig2_inv,
+         q.laser_m_absdepth_inv, q.laser_factor, q.Kzh_v2, q.Kzh_A, q.Kzh_B) = [float(v) for v in pd[:13]]
+        keep = []
+        if q.type == 2:
+            q.nC, q.nG = int(pk[3]), int(pk[4])
+            for name in ("T_C", "Ct", "C_DD", "T_G", "Gt", "G_DD"):
+                a = np.ascontiguousarray(tables[name], dtype=np.float64)
+                keep.append(a)
+                setattr(q, name, _ptr(a))
+        rc = self.L.oracle_ttm_setup(self.o, int(pk[7]), int(pk[8]), int(pk[5]), int(pk[6]), float(pd[16]),
+                                     float(pd[13]), float(pd[14]), float(pd[15]), C.byref(q), float(Te_init))
+        assert rc == 0, rc
+
+    def set_time(self, time, dt):
+        self.L.oracle_set_time(self.o, time, dt)
+
+    def turi_update(self):
+        self.L.oracle_turi_update(self.o)
+
+    def se_steps(self, nsteps, dt, group=-1):
+        assert self.L.oracle_se_steps(self.o, nsteps, dt, group) == 0
+
+    def ttm_1d(self, nmax=4096):
+        num = np.zeros(nmax, np.uint32)
+        vcm = np.zeros((nmax, 3))
+        Ti, Te, xi = np.zeros(nmax), np.zeros(nmax), np.zeros(nmax)
+        n = self.L.oracle_ttm_1d(self.o, _ptr(num), _ptr(vcm), _ptr(Ti), _ptr(Te), _ptr(xi))
+        assert n > 0, n
+        return dict(num=num[:n].copy(), vcm=vcm[:n].copy(), Ti=Ti[:n].copy(), Te=Te[:n].copy(), xi=xi[:n].copy())

@@ -131,6 +131,43 @@ void oref_ttm_geom(fmd_t *md, int *tdims_local, int *itc_start, int *itc_glob_to
     }
 }
 
+/* The active TTM turi's derived parameters (src/ttm.h:41-100, set by the
+   fmd_ttm_set* calls and _fmd_ttm_getReady, src/ttm.c:63-80): d[] = C_gamma,
+   K, G, dz2, frontsurf, laser_t0, laser_tdiff, laser_m_2sig2_inv,
+   laser_m_absdepth_inv, laser_factor_constant, Kzh.v2, Kzh.A, Kzh.B,
+   tcell_volume, starttime, stoptime, tcellh[2]; k[] = type (1, 2),
+   timestep_ratio, min_atoms_num, nC, nG, itc_start_owned[2], itc_stop[2],
+   tdims_local[2], itc_glob_to_loc[2].  Returns -1 without a 1-D TTM. */
+int oref_ttm_params(fmd_t *md, double *d, int *k)
+{
+    turi_t *t = md->active_ttm_turi;
+    if (t == NULL || t->ttm == NULL || t->ttm->dim != 1) return -1;
+    ttm_t *ttm = t->ttm;
+    const double dv[17] = {ttm->C_gamma, ttm->K, ttm->G, ttm->dz2, ttm->frontsurf, ttm->laser_t0,
+                           ttm->laser_tdiff, ttm->laser_m_2sig2_inv, ttm->laser_m_absdepth_inv,
+                           ttm->laser_factor_constant, ttm->Kzh.v2, ttm->Kzh.A, ttm->Kzh.B, t->tcell_volume,
+                           t->starttime, t->stoptime, t->tcellh[2]};
+    const int kv[9] = {t->cat == FMD_TURI_TTM_TYPE1 ? 1 : 2, (int)ttm->timestep_ratio, (int)ttm->min_atoms_num,
+                       ttm->nC, ttm->nG, t->itc_start_owned[2], t->itc_stop[2], (int)t->tdims_local[2],
+                       t->itc_glob_to_loc[2]};
+    memcpy(d, dv, sizeof dv);
+    memcpy(k, kv, sizeof kv);
+    return 0;
+}
+
+/* a type-2 TTM table (which: 0 T_C, 1 Ct, 2 C_DD, 3 T_G, 4 Gt, 5 G_DD) */
+int oref_ttm_table(fmd_t *md, int which, double *out)
+{
+    turi_t *t = md->active_ttm_turi;
+    if (t == NULL || t->ttm == NULL) return -1;
+    ttm_t *ttm = t->ttm;
+    const double *src[6] = {ttm->T_C, ttm->Ct, ttm->C_DD, ttm->T_G, ttm->Gt, ttm->G_DD};
+    const int n = which < 3 ? ttm->nC : ttm->nG;
+    if (which < 0 || which > 5 || src[which] == NULL) return -1;
+    memcpy(out, src[which], sizeof(double) * n);
+    return n;
+}
+
 /* EAM tables after load (src/eam.h:408-430): copies element `el`'s arrays */
 int oref_eam_tables(fmd_pot_t *pot, int el, int *Nrho, int *Nr2, double *drho, double *dr2,
                     double *cutoff_sqr, double *F, double *F_DD, double *rho, double *rhoDD,

@@ -41,6 +41,23 @@ REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libfmdref.so")
 REF_DATA = os.path.join(os.environ.get("FMD_REFERENCE", "/root/reference"), "examples", "data")
 
 
+def ttm_params(lib, md):
+    """The reference's derived parameters of the active 1-D TTM turi
+    (oracle/ref_probe.c oref_ttm_params, oref_ttm_table) for the oracle's
+    TTM restatement: ttm_pd (17 doubles), ttm_pk (9 ints), type-2 tables."""
+    d = np.zeros(17)
+    k = np.zeros(9, np.int32)
+    if lib.L.oref_ttm_params(C.c_void_p(md.value), d.ctypes.data_as(C.c_void_p), k.ctypes.data_as(C.c_void_p)) != 0:
+        return {}
+    out = dict(ttm_pd=d, ttm_pk=k)
+    if k[0] == 2:
+        for w, key in enumerate(("T_C", "Ct", "C_DD", "T_G", "Gt", "G_DD")):
+            buf = np.zeros(int(k[3] if w < 3 else k[4]))
+            lib.L.oref_ttm_table(C.c_void_p(md.value), w, buf.ctypes.data_as(C.c_void_p))
+            out["ttm_tab_" + key] = buf
+    return out
+
+
 def golden_case(lib, name, work):
     case = cases.CASES[name]
     data = {f: open(os.path.join(REF_DATA, f), "rb").read() for f in case.get("data", ())}
@@ -75,6 +92,7 @@ def golden_case(lib, name, work):
         if ttm is not None:
             for kk, vv in ttm.items():
                 out["ttm_" + kk] = vv
+            out.update(ttm_params(lib, md))
     lib.fmd_free(md)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "N0", len(d0["id"]), "N1", len(d1["id"]), "PE0", d0["pe"], "rows", len(rec.rows),
@@ -116,6 +134,7 @@ def golden_full(lib, name, work):
                 out["field_%03d" % k] = vals
         for kk, vv in lib.ttm_1d(md).items():
             out["ttm_" + kk] = vv
+        out.update(ttm_params(lib, md))
     lib.fmd_free(md)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "N", out["n0"], out["n1"], "rows", len(rec.rows), "errors", rec.errors)

@@ -108,3 +108,55 @@ def test_oracle_threads_agree():
     g, d0, _, _ = run_oracle_case("eam", threads=1)
     g2, e0, _, _ = run_oracle_case("eam", threads=4)
     assert np.abs(d0["F"] - e0["F"]).max() <= 1e-13 * np.abs(d0["F"]).max()
+
+
+TTM_CASES = [n for n in cases.CASES if cases.CASES[n].get("turi", {}).get("cat", 0) in (1, 2)]
+
+
+@pytest.mark.parametrize("name", TTM_CASES)
+def test_oracle_ttm_matches_reference(name):
+    """The oracle's two-temperature restatement (turi fields, activation,
+    electron solver types 1 and 2, friction term, symplectic Euler) on the
+    reference's TTM cases, with the reference's derived TTM parameters from
+    the golden file: the final Te, Ti, xi, vcm and atom counts per cell to
+    1e-10, the thermo series to 1e-9, the final cell order exact and the
+    positions within 1e-9 A."""
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    case = cases.CASES[name]
+    grp, dt = case["run"][1], case["run"][2]
+    with tempfile.TemporaryDirectory() as work:
+        o = oracle_for_case(name, g, work)
+    tables = {k[len("ttm_tab_"):]: g[k] for k in g if k.startswith("ttm_tab_")}
+    o.ttm_setup(g["ttm_pd"], g["ttm_pk"], case["turi"]["Te"], tables)
+    # a run's start (src/integrators.c:181-197): the turi update at the
+    # current time, then the forces with the friction term
+    o.set_time(0.0, dt)
+    o.turi_update()
+    o.forces(grp)
+    th = o.thermo(grp)
+    rows = [(0.0, th.temperature, th.kinetic + th.potential, th.kinetic)]
+    done = 0
+    while done < case["steps"]:
+        k = min(case["every"], case["steps"] - done)
+        o.se_steps(k, dt, grp)
+        done += k
+        th = o.thermo(grp)
+        rows.append((done * dt, th.temperature, th.kinetic + th.potential, th.kinetic))
+    t = o.ttm_1d()
+    d1 = o.dump()
+    o.close()
+    lo, hi = 1, len(g["ttm_Te"]) - 1
+    np.testing.assert_array_equal(t["num"][lo:hi], g["ttm_num"][lo:hi])
+
+    def rel(a, b):
+        ok = np.isfinite(b)
+        assert np.array_equal(ok, np.isfinite(a))
+        return float(np.abs(a[ok] - b[ok]).max() / max(np.abs(b[ok]).max(), 1e-300)) if ok.any() else 0.0
+
+    errs = {q: rel(t[q][lo:hi], g["ttm_" + q][lo:hi]) for q in ("Te", "Ti", "xi", "vcm")}
+    print(name, "oracle TTM vs reference:", errs)
+    assert max(errs.values()) <= 1e-10, errs
+    np.testing.assert_allclose(np.array(rows)[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
+    np.testing.assert_array_equal(d1["id"], g["s1_id"])
+    np.testing.assert_array_equal(d1["cell"], g["s1_cell"])
+    assert np.abs(d1["x"] - g["s1_x"]).max() <= 1e-9
