@@ -677,6 +677,35 @@ void _fmd_ttm_setLaserSource_gaussian(fmd_t *md, fmd_handle_t turi, fmd_ttm_lase
     t->laser_set = true;
 }
 
+/* white-box access to the derived parameters of the active 1-D TTM turi,
+   in the layout the golden files record for the reference (d: C_gamma, K,
+   G, dz2, frontsurf, laser_t0, laser_tdiff, laser_m_2sig2_inv,
+   laser_m_absdepth_inv, laser_factor, Kzh v2, A, B, tcell_volume,
+   starttime, stoptime, tcellh_z; k: type, ratio, min_atoms, nC, nG,
+   itc_start_z, itc_stop_z, nz, glob-to-loc offset z); the type-2 tables
+   through `tables` (T_C, Ct, C_DD, T_G, Gt, G_DD pointers, may be NULL).
+   For the CPU oracle's TTM runs (tests, the bench's CPU baseline).
+   Returns -1 without a TTM turi. */
+int fmdx_ttm_params(fmd_t *md, double *d, int *k, const double **tables)
+{
+    turi_t *t = md->active_ttm_turi;
+    if (t == NULL) return -1;
+    const double dv[17] = {t->C_gamma, t->K, t->G, t->tcellh[2] * t->tcellh[2], t->frontsurf, t->laser_t0,
+                           t->laser_set ? t->laser_tdiff : -1.0, t->laser_m_2sig2_inv, t->laser_m_absdepth_inv,
+                           t->laser_factor, t->Kzh_v2, t->Kzh_A, t->Kzh_B, t->tcell_volume, t->starttime,
+                           t->stoptime, t->tcellh[2]};
+    const int kv[9] = {t->cat == FMD_TURI_TTM_TYPE1 ? 1 : 2, t->ratio, (int)t->min_atoms_num, t->nC, t->nG,
+                       t->itc_start[2], t->itc_stop[2], t->tdims_local[2], t->itc_start[2]};
+    memcpy(d, dv, sizeof dv);
+    memcpy(k, kv, sizeof kv);
+    if (tables)
+    {
+        tables[0] = t->T_C; tables[1] = t->Ct; tables[2] = t->C_DD;
+        tables[3] = t->T_G; tables[4] = t->Gt; tables[5] = t->G_DD;
+    }
+    return 0;
+}
+
 /* white-box access to the 1-D TTM arrays of the active TTM turi (local
    cells incl. margins), for parity tests; returns the local length */
 int fmdx_ttm_1d(fmd_t *md, unsigned *num, double *vcm, double *Ti, double *Te, double *xi)

@@ -222,3 +222,41 @@ class Oracle:
         n = self.L.oracle_ttm_1d(self.o, _ptr(num), _ptr(vcm), _ptr(Ti), _ptr(Te), _ptr(xi))
         assert n > 0, n
         return dict(num=num[:n].copy(), vcm=vcm[:n].copy(), Ti=Ti[:n].copy(), Te=Te[:n].copy(), xi=xi[:n].copy())
+
+
+# unit factors of the reference (src/general.h:38-45)
+_METER, _SECOND = 1e10, 1e12
+_J_M3_K2, _W_M_K, _W_M2, _W_M3_K = 6.2415091259e-12, 6.2415091259e-4, 6.2415091259e-14, 6.2415091259e-24
+_K_B = 8.6173303e-5
+
+
+def ttm1_params(box, tdims_z, x, gamma, K, G, laser, frac, ratio, start=0.0, stop=-1.0):
+    """The derived parameters of a 1-D type-1 TTM turi of tdims_z cells
+    along z on a single domain, as the reference forms them from its
+    fmd.h-level inputs, in the (pd, pk) layout of the golden files:
+    turi geometry (src/turi.c:670-708: one margin cell each side, tcellh =
+    l / tdims), heat capacity gamma Te, constant K and G
+    (src/ttm.c setters, units src/general.h:38-45), the Gaussian pulse
+    (src/ttm.c:794-816: laser = fluence, reflectance, t0, duration,
+    absorption depth in SI units), and the front surface and activation
+    threshold from the atoms' extent (src/ttm.c:63-80: frontsurf = lowest z,
+    initial atoms per cell = N / V_extent * V_cell, threshold = that x
+    frac)."""
+    import math
+    tcellh = [box[0] / 1, box[1] / 1, box[2] / tdims_z]
+    vol_cell = tcellh[0] * tcellh[1] * tcellh[2]
+    fluence, R, t0, duration, depth = laser
+    Lp = depth * _METER
+    I0 = math.sqrt(4 * math.log(2) / math.pi) * fluence / duration * _W_M2
+    sigma = duration / math.sqrt(8 * math.log(2)) * _SECOND
+    x = np.asarray(x, dtype=np.float64)
+    ll, ul = x.min(axis=0), x.max(axis=0)
+    vol = 1.0
+    for d in range(3):
+        vol *= ul[d] - ll[d]
+    initial = int(len(x) / vol * vol_cell)
+    pd = np.array([gamma * _J_M3_K2, K * _W_M_K, G * _W_M3_K, tcellh[2] * tcellh[2], ll[2], t0 * _SECOND,
+                   4 * math.sqrt(2) * sigma, -0.5 / (sigma * sigma), -1. / Lp, I0 * (1 - R) / Lp, 0.0, 0.0, 0.0,
+                   vol_cell, start, stop, tcellh[2]])
+    pk = np.array([1, ratio, int(initial * frac), 0, 0, 1, 1 + tdims_z, tdims_z + 2, 1], dtype=np.int64)
+    return pd, pk

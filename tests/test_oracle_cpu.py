@@ -160,3 +160,20 @@ def test_oracle_ttm_matches_reference(name):
     np.testing.assert_array_equal(d1["id"], g["s1_id"])
     np.testing.assert_array_equal(d1["cell"], g["s1_cell"])
     assert np.abs(d1["x"] - g["s1_x"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["ttm1", "ttm_slab", "ttm_slab_full"])
+def test_ttm1_params_match_reference(name):
+    """The oracle side's derivation of a type-1 TTM turi's parameters from
+    the fmd.h-level inputs (pyoracle.ttm1_params: geometry, units, laser,
+    front surface, activation threshold) gives the reference's own values
+    bit for bit (what the compiled reference left in its ttm_t)."""
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    case = cases.case_of(name)
+    tu = case["turi"]
+    x = case["state"]()["x"] if name in cases.FULL_CASES else g["state_x"]
+    pd, pk = pyoracle.ttm1_params(case["box"], tu["dims"][2], x, tu["gamma"], tu["K"], tu["G"], tu["laser"],
+                                  tu["frac"], tu["ratio"])
+    used = [i for i in range(17) if i not in (10, 11, 12)]   # (Zhigilei K: type 2 only)
+    np.testing.assert_array_equal(pd[used], g["ttm_pd"][used])
+    np.testing.assert_array_equal(pk[[0, 1, 2, 5, 6, 7, 8]], g["ttm_pk"][[0, 1, 2, 5, 6, 7, 8]])
