@@ -211,3 +211,41 @@ def test_ttm_mixed_te_error(gpu_lib):
     final = _rel(ttm["Te"][lo:hi], g["ttm_Te"][lo:hi])
     print("mixed-mode electron temperature error: events %.3e, final %.3e" % (worst, final))
     assert worst <= MIXED_TE_TOL and final <= MIXED_TE_TOL, (worst, final)
+
+
+@pytest.mark.parametrize("name", [n for n in cases.CASES if cases.CASES[n].get("turi", {}).get("cat", 0) in (1, 2)])
+def test_ttm_setup_matches_reference(gpu_lib, name):
+    """The host side's TTM set-up (unit conversions, laser constants, turi
+    geometry, front surface and activation threshold of a run's start,
+    type-2 tables) leaves the same derived parameters as the reference's
+    (the golden file records the reference's ttm_t through
+    oracle/ref_probe.c): within 1e-14 relative (the difference is printed)."""
+    import ctypes as C
+    g = load_golden(name)
+    case = cases.CASES[name]
+    st = dict(names=case["names"], kind=g["state_kind"], group=g["state_group"], x=g["state_x"], v=g["state_v"])
+    L = gpu_lib.L
+    L.fmdx_ttm_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    with tempfile.TemporaryDirectory() as work:
+        md, _ = cases.setup(gpu_lib, name, work, state=st, data=cases.golden_data(g))
+        gpu_lib.fmd_dync_integrate(md, case["run"][1], 0.0, case["run"][2])
+        pd = np.zeros(17)
+        pk = np.zeros(9, np.int32)
+        tabs = (C.c_void_p * 6)()
+        assert L.fmdx_ttm_params(md, pd.ctypes.data, pk.ctypes.data, tabs) == 0
+        tables = {}
+        if pk[0] == 2:
+            for w, key in enumerate(("T_C", "Ct", "C_DD", "T_G", "Gt", "G_DD")):
+                n = int(pk[3] if w < 3 else pk[4])
+                tables[key] = np.ctypeslib.as_array(C.cast(tabs[w], C.POINTER(C.c_double)), shape=(n,)).copy()
+        gpu_lib.fmd_free(md)
+    used = list(range(17)) if pk[0] == 2 else [i for i in range(17) if i not in (10, 11, 12)]
+    np.testing.assert_allclose(pd[used], g["ttm_pd"][used], rtol=1e-14, atol=0)
+    ku = [0, 1, 2, 3, 4, 5, 6, 7, 8] if pk[0] == 2 else [0, 1, 2, 5, 6, 7, 8]
+    np.testing.assert_array_equal(pk[ku], g["ttm_pk"][ku])
+    for key, arr in tables.items():
+        np.testing.assert_allclose(arr, g["ttm_tab_" + key], rtol=1e-14, atol=1e-300)
+    print(name, "set-up vs reference: max relative difference %.1e" % max(
+        [float(np.max(np.abs(pd[used] - g["ttm_pd"][used]) / np.maximum(np.abs(g["ttm_pd"][used]), 1e-300)))] +
+        [float(np.max(np.abs(a - g["ttm_tab_" + k]) / np.maximum(np.abs(g["ttm_tab_" + k]), 1e-300)))
+         for k, a in tables.items()]))
