@@ -17,6 +17,7 @@ import sys
 import tempfile
 
 import numpy as np
+import pytest
 
 import cases
 
@@ -79,3 +80,44 @@ def test_cu01_tables_match_oracle(lib):
             # phi[0] is FLT_MAX in both (src/eam.c:460-477)
             np.testing.assert_array_equal(mine, theirs, err_msg=str(which))
         o.close()
+
+
+@pytest.mark.parametrize("name", ["ttm2", "ttm2_cu"])
+def test_ttm_tables_match_reference(name):
+    """Host-side TTM set-up without a device (fmd_create, the turi, the
+    fmd_ttm_set* calls): the type-2 tables of libfmd (read from the same
+    files, converted, spline-prepared) against the reference's, and the
+    unit conversions and laser constants that do not depend on the atoms."""
+    import ctypes as C
+    import tempfile
+
+    import cases
+    from fmd_gb300 import api, load
+    from test_parity_golden_gpu import check_ttm_tables
+    lib = load()
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz")))
+    case = cases.CASES[name]
+    with tempfile.TemporaryDirectory() as work:
+        cases.write_data(work, cases.golden_data(g))
+        md = C.c_void_p(lib.fmd_create())
+        lib.fmd_io_setShowErrorMessages(md, False)
+        lib.fmd_box_setSubdomains(md, 1, 1, 1)
+        lib.fmd_box_setSize(md, *case["box"])
+        lib.fmd_box_setPBC(md, *[bool(b) for b in case["pbc"]])
+        api.set_atom_kinds(lib, md, case["names"], [cases.MASS[n] for n in case["names"]])
+        cases.setup_turi(lib, md, dict(case["turi"]), work)
+        lib.L.fmdx_ttm_params.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        pd = np.zeros(17)
+        pk = np.zeros(9, np.int32)
+        tabs = (C.c_void_p * 6)()
+        assert lib.L.fmdx_ttm_params(md, pd.ctypes.data, pk.ctypes.data, tabs) == 0
+        tables = {}
+        for w, key in enumerate(("T_C", "Ct", "C_DD", "T_G", "Gt", "G_DD")):
+            n = int(pk[3] if w < 3 else pk[4])
+            tables[key] = np.ctypeslib.as_array(C.cast(tabs[w], C.POINTER(C.c_double)), shape=(n,)).copy()
+        lib.fmd_free(md)
+    check_ttm_tables(tables, g)
+    # Zhigilei constants, dz2, laser constants, cell volume, window, tcellh
+    same = [3, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16]
+    np.testing.assert_array_equal(pd[same], g["ttm_pd"][same])
+    np.testing.assert_array_equal(pk[[0, 1, 3, 4, 5, 6, 7, 8]], g["ttm_pk"][[0, 1, 3, 4, 5, 6, 7, 8]])
