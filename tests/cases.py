@@ -428,3 +428,23 @@ def run(lib: api.Lib, name: str, md, rec: Recorder | None = None, steps=None):
         lib.fmd_dync_integrate(md, r[1], duration, dt)
     else:
         lib.fmd_dync_equilibrate(md, r[1], duration, dt, r[3], r[4])
+
+
+def check_ttm_tables(tables, g):
+    """Type-2 tables against the reference's: the knots exactly, the values
+    (unit conversion of the file's numbers) to 1e-15 relative, and the
+    spline second derivatives by their effect on the interpolated values
+    (|dDD| h^2 / 6 within 1e-14 of the largest value): the tridiagonal
+    solve rounds differently, and a nearly straight table has second
+    derivatives at rounding level."""
+    for key, arr in tables.items():
+        ref = g["ttm_tab_" + key]
+        if key.startswith("T_"):
+            np.testing.assert_array_equal(arr, ref)
+        elif key.endswith("_DD"):
+            knots = g["ttm_tab_T_" + key[0]]
+            vals = g["ttm_tab_" + key[0] + "t"]
+            h = float(np.diff(knots).max())
+            assert np.abs(arr - ref).max() * h * h / 6.0 <= 1e-14 * np.abs(vals).max(), key
+        else:
+            np.testing.assert_allclose(arr, ref, rtol=1e-15, atol=0)

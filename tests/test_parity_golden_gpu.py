@@ -245,26 +245,6 @@ def test_ttm_setup_matches_reference(gpu_lib, name):
     np.testing.assert_allclose(pd[used], g["ttm_pd"][used], rtol=1e-14, atol=0)
     ku = [0, 1, 2, 3, 4, 5, 6, 7, 8] if pk[0] == 2 else [0, 1, 2, 5, 6, 7, 8]
     np.testing.assert_array_equal(pk[ku], g["ttm_pk"][ku])
-    check_ttm_tables(tables, g)
+    cases.check_ttm_tables(tables, g)
     print(name, "set-up vs reference: parameters max relative difference %.1e" %
           float(np.max(np.abs(pd[used] - g["ttm_pd"][used]) / np.maximum(np.abs(g["ttm_pd"][used]), 1e-300))))
-
-
-def check_ttm_tables(tables, g):
-    """Type-2 tables against the reference's: the knots exactly, the values
-    (unit conversion of the file's numbers) to 1e-15 relative, and the
-    spline second derivatives by their effect on the interpolated values
-    (|dDD| h^2 / 6 within 1e-14 of the largest value): the tridiagonal
-    solve rounds differently, and a nearly straight table has second
-    derivatives at rounding level."""
-    for key, arr in tables.items():
-        ref = g["ttm_tab_" + key]
-        if key.startswith("T_"):
-            np.testing.assert_array_equal(arr, ref)
-        elif key.endswith("_DD"):
-            knots = g["ttm_tab_T_" + key[0]]
-            vals = g["ttm_tab_" + key[0] + "t"]
-            h = float(np.diff(knots).max())
-            assert np.abs(arr - ref).max() * h * h / 6.0 <= 1e-14 * np.abs(vals).max(), key
-        else:
-            np.testing.assert_allclose(arr, ref, rtol=1e-15, atol=0)

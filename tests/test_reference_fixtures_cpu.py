@@ -93,7 +93,6 @@ def test_ttm_tables_match_reference(name):
 
     import cases
     from fmd_gb300 import api, load
-    from test_parity_golden_gpu import check_ttm_tables
     lib = load()
     g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz")))
     case = cases.CASES[name]
@@ -116,7 +115,7 @@ def test_ttm_tables_match_reference(name):
             n = int(pk[3] if w < 3 else pk[4])
             tables[key] = np.ctypeslib.as_array(C.cast(tabs[w], C.POINTER(C.c_double)), shape=(n,)).copy()
         lib.fmd_free(md)
-    check_ttm_tables(tables, g)
+    cases.check_ttm_tables(tables, g)
     # Zhigilei constants, dz2, laser constants, cell volume, window, tcellh
     same = [3, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16]
     np.testing.assert_array_equal(pd[same], g["ttm_pd"][same])
