@@ -113,19 +113,15 @@ def test_oracle_threads_agree():
 TTM_CASES = [n for n in cases.CASES if cases.CASES[n].get("turi", {}).get("cat", 0) in (1, 2)]
 
 
-@pytest.mark.parametrize("name", TTM_CASES)
-def test_oracle_ttm_matches_reference(name):
-    """The oracle's two-temperature restatement (turi fields, activation,
-    electron solver types 1 and 2, friction term, symplectic Euler) on the
-    reference's TTM cases, with the reference's derived TTM parameters from
-    the golden file: the final Te, Ti, xi, vcm and atom counts per cell to
-    1e-10, the thermo series to 1e-9, the final cell order exact and the
-    positions within 1e-9 A."""
+def run_oracle_ttm(name, threads=1):
+    """The oracle on a TTM golden case: the run's first turi update and
+    forces, then the case's symplectic-Euler steps; returns (golden, thermo
+    rows, TTM arrays, final dump)."""
     g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
     case = cases.CASES[name]
     grp, dt = case["run"][1], case["run"][2]
     with tempfile.TemporaryDirectory() as work:
-        o = oracle_for_case(name, g, work)
+        o = oracle_for_case(name, g, work, threads)
     tables = {k[len("ttm_tab_"):]: g[k] for k in g if k.startswith("ttm_tab_")}
     o.ttm_setup(g["ttm_pd"], g["ttm_pk"], case["turi"]["Te"], tables)
     # a run's start (src/integrators.c:181-197): the turi update at the
@@ -145,6 +141,28 @@ def test_oracle_ttm_matches_reference(name):
     t = o.ttm_1d()
     d1 = o.dump()
     o.close()
+    return g, np.array(rows), t, d1
+
+
+def test_oracle_ttm_threads_agree():
+    """The OpenMP pair loops under the TTM step give the same electron
+    temperatures and positions as one thread."""
+    _, r1, t1, d1 = run_oracle_ttm("ttm_slab", threads=1)
+    _, r4, t4, d4 = run_oracle_ttm("ttm_slab", threads=4)
+    lo, hi = 1, len(t1["Te"]) - 1
+    assert np.abs(t1["Te"][lo:hi] - t4["Te"][lo:hi]).max() <= 1e-11 * np.abs(t1["Te"][lo:hi]).max()
+    assert np.abs(d1["x"] - d4["x"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("name", TTM_CASES)
+def test_oracle_ttm_matches_reference(name):
+    """The oracle's two-temperature restatement (turi fields, activation,
+    electron solver types 1 and 2, friction term, symplectic Euler) on the
+    reference's TTM cases, with the reference's derived TTM parameters from
+    the golden file: the final Te, Ti, xi, vcm and atom counts per cell to
+    1e-10, the thermo series to 1e-9, the final cell order exact and the
+    positions within 1e-9 A."""
+    g, rows, t, d1 = run_oracle_ttm(name)
     lo, hi = 1, len(g["ttm_Te"]) - 1
     np.testing.assert_array_equal(t["num"][lo:hi], g["ttm_num"][lo:hi])
 
@@ -156,7 +174,7 @@ def test_oracle_ttm_matches_reference(name):
     errs = {q: rel(t[q][lo:hi], g["ttm_" + q][lo:hi]) for q in ("Te", "Ti", "xi", "vcm")}
     print(name, "oracle TTM vs reference:", errs)
     assert max(errs.values()) <= 1e-10, errs
-    np.testing.assert_allclose(np.array(rows)[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(rows[:, 1:], g["thermo"][:, 1:], rtol=1e-9, atol=1e-9)
     np.testing.assert_array_equal(d1["id"], g["s1_id"])
     np.testing.assert_array_equal(d1["cell"], g["s1_cell"])
     assert np.abs(d1["x"] - g["s1_x"]).max() <= 1e-9
