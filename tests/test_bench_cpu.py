@@ -81,3 +81,11 @@ def test_reference_arm_line():
     assert d["warmup"] == 3 and d["steps"] == 1 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_ttm_cpu_port_runs():
+    """The TTM line's CPU baseline (the oracle port's full symplectic-Euler
+    step with the turi fields, solver and friction term on the 800 000-atom
+    slab) runs and reports a positive rate."""
+    v, k = bench.cpu_port_ttm(2, target_s=0.1, max_steps=1)
+    assert v > 0 and k == 1
